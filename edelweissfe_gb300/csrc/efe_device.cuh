@@ -1,0 +1,415 @@
+// efe_device.cuh -- device-side building blocks: element shapes, quadrature rules and the
+// material point updates of the reference's "edelweiss" materials, all in FP64.
+//
+// Reference algorithms (paths relative to the EdelweissFE project root):
+//   shape functions      elements/displacementelement/_elementcomputationmatrices.py:106-212
+//   Jacobian / dN/dX     _elementcomputationmatrices.py:32-103, 215-540, displacementtlelement/
+//                        _elementcomputationmatrices.py:247-281 (derivatives evaluated at the
+//                        natural point (eta_i, xi_i, zeta_i) of quadrature point i)
+//   quadrature rules     elements/library.py:33-533
+//   linear elastic       materials/linearelastic/linearelastic.py:63-210
+//   von Mises            materials/vonmises/vonmises.py:35-254
+//   plane stress (hypo)  materials/base/basehypoelasticmaterial.py:71-130
+//   Neo-Hooke a/b/c      materials/neohooke/neohookepencegouformulation{a,b,c}.py:107-145
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/efe_gb300.h"
+
+namespace efe {
+
+// ------------------------------------------------------------------ shapes and rules
+template <int SHAPE> struct ShapeInfo;
+template <> struct ShapeInfo<EFE_QUAD4> { static constexpr int DIM = 2, NN = 4; };
+template <> struct ShapeInfo<EFE_QUAD8> { static constexpr int DIM = 2, NN = 8; };
+template <> struct ShapeInfo<EFE_HEXA8> { static constexpr int DIM = 3, NN = 8; };
+template <> struct ShapeInfo<EFE_HEXA20> { static constexpr int DIM = 3, NN = 20; };
+
+template <int RULE> struct RuleInfo;
+template <> struct RuleInfo<EFE_RULE_2D_1> { static constexpr int NQ = 1; };
+template <> struct RuleInfo<EFE_RULE_2D_2X2> { static constexpr int NQ = 4; };
+template <> struct RuleInfo<EFE_RULE_2D_3X3> { static constexpr int NQ = 9; };
+template <> struct RuleInfo<EFE_RULE_3D_1> { static constexpr int NQ = 1; };
+template <> struct RuleInfo<EFE_RULE_3D_2X2X2> { static constexpr int NQ = 8; };
+template <> struct RuleInfo<EFE_RULE_3D_3X3X3> { static constexpr int NQ = 27; };
+
+// natural coordinates of the nodes in the reference's node order (computeNOperator)
+__device__ __forceinline__ void node_natural(int shape, int a, int c[3]) {
+  // quad4 / corners of quad8: (-1,-1) (1,-1) (1,1) (-1,1); quad8 mids: (0,-1) (1,0) (0,1) (-1,0)
+  const signed char q8[8][2] = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1}, {0, -1}, {1, 0}, {0, 1}, {-1, 0}};
+  const signed char h20[20][3] = {{-1, -1, -1}, {-1, -1, 1}, {1, -1, 1}, {1, -1, -1}, {-1, 1, -1}, {-1, 1, 1},
+                                  {1, 1, 1},    {1, 1, -1},  {-1, -1, 0}, {0, -1, 1}, {1, -1, 0}, {0, -1, -1},
+                                  {-1, 1, 0},   {0, 1, 1},   {1, 1, 0},   {0, 1, -1}, {-1, 0, -1}, {-1, 0, 1},
+                                  {1, 0, 1},    {1, 0, -1}};
+  if (shape == EFE_QUAD4 || shape == EFE_QUAD8) {
+    c[0] = q8[a][0];
+    c[1] = q8[a][1];
+    c[2] = 0;
+  } else {
+    c[0] = h20[a][0];
+    c[1] = h20[a][1];
+    c[2] = h20[a][2];
+  }
+}
+
+// dN_a/dxi_r at natural point p (serendipity / Lagrange shape functions)
+template <int SHAPE>
+__device__ void shape_derivatives(const double p[3], double dN[ShapeInfo<SHAPE>::DIM][ShapeInfo<SHAPE>::NN]) {
+  constexpr int DIM = ShapeInfo<SHAPE>::DIM, NN = ShapeInfo<SHAPE>::NN;
+  constexpr bool quadratic = NN > (1 << DIM);
+  for (int a = 0; a < NN; ++a) {
+    int c[3];
+    node_natural(SHAPE, a, c);
+    bool corner = true;
+    int mid = -1;
+    for (int k = 0; k < DIM; ++k)
+      if (c[k] == 0) {
+        corner = false;
+        mid = k;
+      }
+    if (!quadratic || corner) {
+      double lin[3];
+      for (int k = 0; k < DIM; ++k) lin[k] = 1.0 + c[k] * p[k];
+      double base = 1.0;
+      for (int k = 0; k < DIM; ++k) base *= lin[k];
+      const double inv = 1.0 / (1 << DIM);
+      double s = 0.0;
+      if (quadratic) {
+        for (int k = 0; k < DIM; ++k) s += c[k] * p[k];
+        s -= (DIM - 1);
+      }
+      for (int r = 0; r < DIM; ++r) {
+        double db = c[r];
+        for (int k = 0; k < DIM; ++k)
+          if (k != r) db *= lin[k];
+        if (quadratic)
+          dN[r][a] = (db * s + base * c[r]) * inv;
+        else
+          dN[r][a] = db * inv;
+      }
+    } else {
+      const double inv = 1.0 / (1 << (DIM - 1));
+      double prod = 1.0;
+      for (int k = 0; k < DIM; ++k)
+        if (k != mid) prod *= (1.0 + c[k] * p[k]);
+      const double q = 1.0 - p[mid] * p[mid];
+      for (int r = 0; r < DIM; ++r) {
+        if (r == mid) {
+          dN[r][a] = -2.0 * p[mid] * prod * inv;
+        } else {
+          double t = q * c[r];
+          for (int k = 0; k < DIM; ++k)
+            if (k != mid && k != r) t *= (1.0 + c[k] * p[k]);
+          dN[r][a] = t * inv;
+        }
+      }
+    }
+  }
+}
+
+// quadrature point q of a rule: library coordinates (xi, eta, zeta) and weight
+__device__ __forceinline__ void quadrature_point(int rule, int q, double& xi, double& eta, double& zeta, double& w) {
+  const double g = 1.0 / sqrt(3.0);
+  const double s = sqrt(0.6);
+  zeta = 0.0;
+  switch (rule) {
+    case EFE_RULE_2D_1:
+      xi = 0.0;
+      eta = 0.0;
+      w = 4.0;
+      return;
+    case EFE_RULE_2D_2X2: {
+      const signed char X[4] = {1, 1, -1, -1}, Y[4] = {1, -1, -1, 1};
+      xi = g * X[q];
+      eta = g * Y[q];
+      w = 1.0;
+      return;
+    }
+    case EFE_RULE_2D_3X3: {
+      const signed char X[9] = {0, -1, -1, 1, 1, -1, 0, 1, 0}, Y[9] = {0, -1, 1, 1, -1, 0, 1, 0, -1};
+      const double w1 = (5.0 / 9.0) * (5.0 / 9.0), w2 = (5.0 / 9.0) * (8.0 / 9.0), w3 = (8.0 / 9.0) * (8.0 / 9.0);
+      xi = s * X[q];
+      eta = s * Y[q];
+      w = (q == 0) ? w3 : (q < 5 ? w1 : w2);
+      return;
+    }
+    case EFE_RULE_3D_1:
+      xi = eta = zeta = 0.0;
+      w = 8.0;
+      return;
+    case EFE_RULE_3D_2X2X2: {
+      const signed char Y[4] = {-1, -1, 1, 1}, Z[4] = {-1, 1, 1, -1};
+      xi = g * (q < 4 ? -1.0 : 1.0);
+      eta = g * Y[q & 3];
+      zeta = g * Z[q & 3];
+      w = 1.0;
+      return;
+    }
+    default: {  // EFE_RULE_3D_3X3X3
+      const double W[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
+      const int i = q / 9, j = (q / 3) % 3, k = q % 3;
+      xi = s * (i - 1);
+      eta = s * (j - 1);
+      zeta = s * (k - 1);
+      w = W[i] * W[j] * W[k];
+      return;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ small dense helpers
+__device__ __forceinline__ double det3(const double A[3][3]) {
+  return A[0][0] * (A[1][1] * A[2][2] - A[1][2] * A[2][1]) - A[0][1] * (A[1][0] * A[2][2] - A[1][2] * A[2][0]) +
+         A[0][2] * (A[1][0] * A[2][1] - A[1][1] * A[2][0]);
+}
+__device__ __forceinline__ void inv3(const double A[3][3], double d, double B[3][3]) {
+  const double id = 1.0 / d;
+  B[0][0] = (A[1][1] * A[2][2] - A[1][2] * A[2][1]) * id;
+  B[0][1] = (A[0][2] * A[2][1] - A[0][1] * A[2][2]) * id;
+  B[0][2] = (A[0][1] * A[1][2] - A[0][2] * A[1][1]) * id;
+  B[1][0] = (A[1][2] * A[2][0] - A[1][0] * A[2][2]) * id;
+  B[1][1] = (A[0][0] * A[2][2] - A[0][2] * A[2][0]) * id;
+  B[1][2] = (A[0][2] * A[1][0] - A[0][0] * A[1][2]) * id;
+  B[2][0] = (A[1][0] * A[2][1] - A[1][1] * A[2][0]) * id;
+  B[2][1] = (A[0][1] * A[2][0] - A[0][0] * A[2][1]) * id;
+  B[2][2] = (A[0][0] * A[1][1] - A[0][1] * A[1][0]) * id;
+}
+
+// ------------------------------------------------------------------ materials
+// Isotropic elasticity matrix entries, formed like the reference: f = E/((1+v)(1-2v)),
+// C11 = f(1-v), C12 = f v, C44 = f (1-2v)/2   (linearelastic.py:95-117, vonmises.py:126-149)
+struct Iso {
+  double c11, c12, c44;
+};
+__device__ __forceinline__ Iso iso3d(double E, double v) {
+  const double f = E / ((1.0 + v) * (1.0 - 2.0 * v));
+  return Iso{f * (1.0 - v), f * v, f * ((1.0 - 2.0 * v) / 2.0)};
+}
+__device__ __forceinline__ void iso_apply(const Iso& C, const double e[6], double s[6]) {
+  s[0] = C.c11 * e[0] + C.c12 * e[1] + C.c12 * e[2];
+  s[1] = C.c12 * e[0] + C.c11 * e[1] + C.c12 * e[2];
+  s[2] = C.c12 * e[0] + C.c12 * e[1] + C.c11 * e[2];
+  s[3] = C.c44 * e[3];
+  s[4] = C.c44 * e[4];
+  s[5] = C.c44 * e[5];
+}
+
+// Tangent of a hypoelastic 3D update in the form C = C_iso(c11, c12, c44) - a n (x) n,
+// which covers linear elasticity (a = 0) and the consistent J2 tangent (vonmises.py:241-251).
+struct Tangent3 {
+  double c11, c12, c44, a;
+  double n[6];
+};
+__device__ __forceinline__ double tangent3_entry(const Tangent3& T, int i, int j) {
+  double v;
+  if (i < 3 && j < 3)
+    v = (i == j) ? T.c11 : T.c12;
+  else
+    v = (i == j) ? T.c44 : 0.0;
+  return v - T.a * T.n[i] * T.n[j];
+}
+
+// von Mises radial return (vonmises.py:186-254).  Updates sig and kappa in place.
+// Returns false when the scalar Newton does not converge in 15 iterations (CutbackRequest).
+__device__ inline bool von_mises_3d(const double* props, double sig[6], const double de[6], double& kappa, Tangent3& T) {
+  const double E = props[0], v = props[1], fy0 = props[2], H = props[3], dfy = props[4], delta = props[5];
+  const Iso Ei = iso3d(E, v);
+  T.c11 = Ei.c11;
+  T.c12 = Ei.c12;
+  T.c44 = Ei.c44;
+  T.a = 0.0;
+  for (int i = 0; i < 6; ++i) T.n[i] = 0.0;
+  double nrm = 0.0;
+  for (int i = 0; i < 6; ++i) nrm += de[i] * de[i];
+  if (sqrt(nrm) < 1e-14) return true;  // zero increment: C = Ei (:211-213)
+  const double G = E / (2.0 * (1.0 + v));
+  double tr[6], ds[6];
+  iso_apply(Ei, de, ds);
+  for (int i = 0; i < 6; ++i) tr[i] = sig[i] + ds[i];
+  double dev[6];
+  dev[0] = 2.0 / 3.0 * tr[0] - 1.0 / 3.0 * tr[1] - 1.0 / 3.0 * tr[2];
+  dev[1] = -1.0 / 3.0 * tr[0] + 2.0 / 3.0 * tr[1] - 1.0 / 3.0 * tr[2];
+  dev[2] = -1.0 / 3.0 * tr[0] - 1.0 / 3.0 * tr[1] + 2.0 / 3.0 * tr[2];
+  dev[3] = tr[3];
+  dev[4] = tr[4];
+  dev[5] = tr[5];
+  const double devNorm =
+      sqrt(dev[0] * dev[0] + dev[1] * dev[1] + dev[2] * dev[2] + 2.0 * (dev[3] * dev[3] + dev[4] * dev[4] + dev[5] * dev[5]));
+  const double k0 = kappa;
+  const double sq23 = sqrt(2.0 / 3.0), sq6 = sqrt(6.0);
+  const double fy_k0 = fy0 + H * k0 + dfy * (1.0 - exp(-delta * k0));
+  if (devNorm - sq23 * fy_k0 > 0.0) {
+    double dK = 0.0;
+    int counter = 0;
+    bool ok = true;
+    while (true) {
+      const double k = k0 + dK;
+      const double R = devNorm - sq6 * G * dK - sq23 * (fy0 + H * k + dfy * (1.0 - exp(-delta * k)));
+      if (!(fabs(R) > 1e-12)) break;
+      if (counter == 15) {
+        ok = false;
+        break;
+      }
+      const double dR = -sq6 * G - sq23 * (H + dfy * delta * exp(-delta * k));
+      dK -= R / dR;
+      ++counter;
+    }
+    const double dLambda = sqrt(1.5) * dK;
+    kappa = k0 + dK;
+    const double inv = 1.0 / devNorm;
+    for (int i = 0; i < 6; ++i) {
+      T.n[i] = dev[i] * inv;
+      sig[i] = tr[i] - 2.0 * G * dLambda * T.n[i];
+    }
+    const double dfyk = H + dfy * delta * exp(-delta * kappa);
+    const double beta = 4.0 * G * G * dLambda / devNorm;  // coefficient of IDevHalfShear
+    T.a = 2.0 * G * (1.0 / (1.0 + dfyk / (3.0 * G)) - 2.0 * G * dLambda / devNorm);
+    T.c11 = Ei.c11 - beta * (2.0 / 3.0);
+    T.c12 = Ei.c12 + beta * (1.0 / 3.0);
+    T.c44 = Ei.c44 - beta * 0.5;
+    return ok;
+  }
+  for (int i = 0; i < 6; ++i) sig[i] = tr[i];
+  return true;
+}
+
+__device__ __forceinline__ void linear_elastic_3d(const double* props, double sig[6], const double de[6],
+                                                  Tangent3& T) {
+  const Iso Ei = iso3d(props[0], props[1]);
+  double ds[6];
+  iso_apply(Ei, de, ds);
+  for (int i = 0; i < 6; ++i) sig[i] += ds[i];
+  T.c11 = Ei.c11;
+  T.c12 = Ei.c12;
+  T.c44 = Ei.c44;
+  T.a = 0.0;
+  for (int i = 0; i < 6; ++i) T.n[i] = 0.0;
+}
+
+// symmetric 3x3 in-plane tangent (rows/cols 11, 22, 12): C00 C01 C02 C11 C12 C22
+struct Tangent2 {
+  double c[6];
+};
+__device__ __forceinline__ void tangent2_from3(const Tangent3& T, Tangent2& C) {
+  // plane strain: rows/cols [0,1,3] of the 6x6 tangent (element.py:217-219,336)
+  const int id[3] = {0, 1, 3};
+  int k = 0;
+  for (int i = 0; i < 3; ++i)
+    for (int j = i; j < 3; ++j) C.c[k++] = tangent3_entry(T, id[i], id[j]);
+}
+
+// LinearElasticMaterial.computePlaneStress (linearelastic.py:127-154); de[2] is overwritten
+__device__ __forceinline__ void linear_elastic_plane_stress(const double* props, double sig[6], double de[6],
+                                                            Tangent2& C) {
+  const double E = props[0], v = props[1];
+  const double f = E / (1.0 - v * v);
+  const double c11 = f * 1.0, c12 = f * v, c33 = f * ((1.0 - v) / 2.0);
+  sig[0] += c11 * de[0] + c12 * de[1];
+  sig[1] += c12 * de[0] + c11 * de[1];
+  sig[3] += c33 * de[3];
+  de[2] = -v / (1.0 - v) * (de[0] + de[1]);
+  C.c[0] = c11;
+  C.c[1] = c12;
+  C.c[2] = 0.0;
+  C.c[3] = c11;
+  C.c[4] = 0.0;
+  C.c[5] = c33;
+}
+
+// BaseHypoElasticMaterial.computePlaneStress applied to von Mises (basehypoelasticmaterial.py:71-130):
+// local Newton on de[2]; every local step calls the 3D update with a zero stress vector and the
+// material state, so kappa accumulates the plastic increments of all local steps; the converged
+// 3D stress is added to sig.  Returns false on a cutback request.
+__device__ inline bool von_mises_plane_stress(const double* props, double sig[6], double de[6], double& kappa, Tangent2& C) {
+  Tangent3 T;
+  double s3[6];
+  de[2] = -de[0] - de[1];
+  int counter = 1;
+  bool ok = true;
+  while (true) {
+    for (int i = 0; i < 6; ++i) s3[i] = 0.0;
+    if (!von_mises_3d(props, s3, de, kappa, T)) {
+      ok = false;
+      break;
+    }
+    const double residual = fabs(s3[2]);
+    if (residual < 1e-11 || (counter > 7 && residual < 1e-8)) break;
+    const double C22 = tangent3_entry(T, 2, 2);
+    double rev = 1.0 / C22;
+    if (isnan(rev) || fabs(rev) > 1e10) rev = 1e10 * (rev > 0 ? 1.0 : (rev < 0 ? -1.0 : rev));
+    de[2] -= rev * s3[2];
+    ++counter;
+    if (counter > 13) {
+      ok = false;
+      break;
+    }
+  }
+  for (int i = 0; i < 6; ++i) sig[i] += s3[i];
+  const int id[3] = {0, 1, 3};
+  const double C22 = tangent3_entry(T, 2, 2);
+  int k = 0;
+  for (int i = 0; i < 3; ++i)
+    for (int j = i; j < 3; ++j)
+      C.c[k++] = tangent3_entry(T, id[i], id[j]) - tangent3_entry(T, 2, id[j]) * tangent3_entry(T, id[i], 2) / C22;
+  return ok;
+}
+
+// Neo-Hooke (Pence-Gou a/b/c): Kirchhoff stress tau (3x3), energy, and the coefficients of
+//   dtau_ij/dF_kl = c1 (d_ik F_jl + F_il d_jk) + c2 d_ij Finv_lk + c3 B_ij Finv_lk + c4 d_ij F_kl
+// (neohookepencegouformulationa.py:128-141, b.py:128-145, c.py:128-143).
+struct NeoHookeOut {
+  double tau[3][3];
+  double Bm[3][3];
+  double c1, c2, c3, c4, energy;
+};
+__device__ inline void neo_hooke(int material, double mu, double K, const double F[3][3], NeoHookeOut& o) {
+  double B[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) B[i][j] = F[i][0] * F[j][0] + F[i][1] * F[j][1] + F[i][2] * F[j][2];
+  const double J = det3(F);
+  double I1 = B[0][0] + B[1][1] + B[2][2];
+  double sB, sI;  // tau = sB * B + sI * I
+  if (material == EFE_MAT_NEOHOOKE_WA) {
+    const double lambdaBar = (K - 2.0 / 3.0 * mu) * (J * J - J) - mu;
+    const double muBar = (K - 2.0 / 3.0 * mu) * (2.0 * J * J - J);
+    sB = mu;
+    sI = lambdaBar;
+    o.c1 = mu;
+    o.c2 = muBar;
+    o.c3 = 0.0;
+    o.c4 = 0.0;
+    o.energy = mu / 2.0 * (I1 - 3.0) + (K / 2.0 - mu / 3.0) * (J - 1.0) * (J - 1.0) - mu * log(J);
+  } else if (material == EFE_MAT_NEOHOOKE_WB) {
+    const double J23 = pow(J, 2.0 / 3.0);
+    const double lambdaHat = K / 2.0 * (J * J + 1.0 / (J * J));
+    const double muBar = mu / (3.0 * J23);
+    const double lambdaBar = K / 4.0 * (J * J - 1.0 / (J * J)) - muBar * I1;
+    sB = mu / J23;
+    sI = lambdaBar;
+    o.c1 = 3.0 * muBar;
+    o.c2 = lambdaHat + 2.0 / 3.0 * I1 * muBar;
+    o.c3 = -2.0 * muBar;
+    o.c4 = -2.0 * muBar;
+    o.energy = mu / 2.0 * (I1 / J23 - 3.0) + K / 8.0 * (J * J + 1.0 / (J * J) - 2.0);
+  } else {  // EFE_MAT_NEOHOOKE_WC; its energy uses trace(F) as I1 (c.py:141)
+    const double p = pow(J, 2.0 / 3.0 - K / mu);
+    const double muBar = mu * p;
+    const double lambdaBar = (K / mu - 2.0 / 3.0) * muBar;
+    sB = mu;
+    sI = -muBar;
+    o.c1 = mu;
+    o.c2 = lambdaBar;
+    o.c3 = 0.0;
+    o.c4 = 0.0;
+    const double trF = F[0][0] + F[1][1] + F[2][2];
+    o.energy = mu / 2.0 * (trF - 3.0) + 3.0 * mu * mu / (3.0 * K - 2.0 * mu) * (p - 1.0);
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      o.tau[i][j] = sB * B[i][j] + (i == j ? sI : 0.0);
+      o.Bm[i][j] = B[i][j];
+    }
+}
+
+}  // namespace efe

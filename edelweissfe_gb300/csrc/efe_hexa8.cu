@@ -1,0 +1,26 @@
+// efe_hexa8.cu -- kernel instantiations for the hexa8 element shape (one translation unit per shape).
+#include "efe_launch.cuh"
+
+namespace efe {
+
+cudaError_t assemble_hexa8(int rule, int form, int kprec, const GroupArgs& g, cudaStream_t st) {
+  switch (rule) {
+    case EFE_RULE_3D_1: return launch_rule<EFE_HEXA8, EFE_RULE_3D_1>(form, kprec, g, st);
+    case EFE_RULE_3D_2X2X2: return launch_rule<EFE_HEXA8, EFE_RULE_3D_2X2X2>(form, kprec, g, st);
+    case EFE_RULE_3D_3X3X3: return launch_rule<EFE_HEXA8, EFE_RULE_3D_3X3X3>(form, kprec, g, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t geometry_hexa8(int rule, int64_t nEl, int64_t off, const int32_t* conn, const double* coords,
+                             const double* th, double* G, double* S, int32_t* status, const Hexa20Fix& fix,
+                             cudaStream_t st) {
+  switch (rule) {
+    case EFE_RULE_3D_1: return launch_geometry<EFE_HEXA8, EFE_RULE_3D_1>(nEl, off, conn, coords, th, G, S, status, fix, st);
+    case EFE_RULE_3D_2X2X2: return launch_geometry<EFE_HEXA8, EFE_RULE_3D_2X2X2>(nEl, off, conn, coords, th, G, S, status, fix, st);
+    case EFE_RULE_3D_3X3X3: return launch_geometry<EFE_HEXA8, EFE_RULE_3D_3X3X3>(nEl, off, conn, coords, th, G, S, status, fix, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace efe

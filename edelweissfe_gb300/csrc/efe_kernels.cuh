@@ -1,0 +1,583 @@
+// efe_kernels.cuh -- geometry set-up kernel and the fused element-evaluation + CSR-assembly kernel.
+//
+// One CTA evaluates a tile of EPB elements of one group in four phases:
+//   0. gather the element nodes' displacements (dU for small strain, U for total Lagrangian)
+//      and the CSR row lengths of the element nodes into shared memory;
+//   A. one thread per (element, quadrature point): kinematics, material update (FP64, state read
+//      from stateRef and written to stateTemp, structure-of-arrays, coalesced), residual
+//      contribution and the per-point factors of the tangent, staged in shared memory;
+//   C. one thread per (element, DOF): P_e = -sum_q r_q in quadrature-point order, atomically added
+//      to P and |P_e| to F (NIST.computeElements, nonlinearimplicitstatic.py:837-844);
+//   B. one thread per (element, node pair a, b): the 2x2 / 3x3 block of K_e for all quadrature
+//      points, scattered with atomics into the CSR data through the pair slot map
+//      (CSRGenerator.updateCSR, csrgenerator.pyx:100-115, without the VIJ vector).
+// KT is the type of the tangent (double, or float in the mixed mode).
+#pragma once
+#include "efe_device.cuh"
+
+namespace efe {
+
+struct GroupArgs {
+  int64_t nElements, elementOffset;
+  const int32_t* conn;
+  const int32_t* pairSlot;
+  const double* props;
+  const double* thickness;
+  const double* geomG;
+  const double* geomS;
+  const double* stateRef;
+  double* stateTemp;
+  const double* auxRef;
+  double* auxTemp;
+  int32_t nProps, material, plane;
+  // mesh
+  const int32_t* nodeDof;
+  const int32_t* nodeRowLen;
+  const double* U;
+  const double* dU;
+  void* Kdata;
+  double* P;
+  double* F;
+  int32_t* status;
+};
+
+struct Hexa20Fix {
+  double r[20];  // row 5 of the inverse of the Hexa20 polynomial-fit matrix (coefficient of t*u)
+};
+
+__device__ __forceinline__ void report(int32_t* status, int bits, int64_t globalElement, int npts) {
+  atomicOr(status + 0, bits);
+  atomicMax(status + 1, (int32_t)(0x7fffffff - globalElement));  // = INT32_MAX - first failing element
+  atomicAdd(status + 2, npts);
+}
+
+// ------------------------------------------------------------------ geometry (once per mesh)
+// J_i = dN/dxi (eta_i, xi_i, zeta_i) . X, with the reference's Hexa20 third-row term
+// (displacementelement/_elementcomputationmatrices.py:369-540 uses a5*zeta where d(a5 t u)/du = a5 xi).
+template <int SHAPE, int RULE>
+__global__ void geometry_kernel(int64_t nEl, int64_t elOffset, const int32_t* __restrict__ conn,
+                                const double* __restrict__ coords, const double* __restrict__ thickness,
+                                double* __restrict__ G, double* __restrict__ S, int32_t* status, Hexa20Fix fix) {
+  constexpr int DIM = ShapeInfo<SHAPE>::DIM, NN = ShapeInfo<SHAPE>::NN, NQ = RuleInfo<RULE>::NQ;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nEl * NQ) return;
+  const int64_t e = t / NQ;
+  const int q = (int)(t % NQ);
+  double xi, eta, zeta, w;
+  quadrature_point(RULE, q, xi, eta, zeta, w);
+  const double p[3] = {eta, xi, zeta};  // swapped evaluation point
+  double dN[DIM][NN];
+  shape_derivatives<SHAPE>(p, dN);
+  double X[NN][DIM];
+  for (int a = 0; a < NN; ++a) {
+    const int32_t n = conn[e * NN + a];
+    for (int c = 0; c < DIM; ++c) X[a][c] = coords[(int64_t)n * DIM + c];
+  }
+  double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 1}};
+  for (int r = 0; r < DIM; ++r)
+    for (int c = 0; c < DIM; ++c) {
+      double s = 0.0;
+      for (int a = 0; a < NN; ++a) s += dN[r][a] * X[a][c];
+      J[r][c] = s;
+    }
+  if constexpr (SHAPE == EFE_HEXA20) {
+    for (int c = 0; c < DIM; ++c) {
+      double a5 = 0.0;
+      for (int a = 0; a < NN; ++a) a5 += fix.r[a] * X[a][c];
+      J[2][c] += (zeta - xi) * a5;
+    }
+  }
+  double detJ, iJ[3][3];
+  if constexpr (DIM == 2) {
+    detJ = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    iJ[0][0] = J[1][1] / detJ;
+    iJ[0][1] = -J[0][1] / detJ;
+    iJ[1][0] = -J[1][0] / detJ;
+    iJ[1][1] = J[0][0] / detJ;
+  } else {
+    detJ = det3(J);
+    inv3(J, detJ, iJ);
+  }
+  if (!(detJ > 0.0) || !isfinite(detJ)) report(status, EFE_STATUS_BAD_JACOBIAN, elOffset + e, 1);
+  const int64_t stride = nEl * NQ;
+  // dN/dX_c = sum_r invJ[c][r] dN/dxi_r   (B = a . blockdiag(invJ) . dN, _B3D8 :679-817)
+  for (int c = 0; c < DIM; ++c)
+    for (int a = 0; a < NN; ++a) {
+      double s = 0.0;
+      for (int r = 0; r < DIM; ++r) s += iJ[c][r] * dN[r][a];
+      G[(int64_t)(c * NN + a) * stride + t] = s;
+    }
+  const double th = (DIM == 2 && thickness) ? thickness[e] : 1.0;
+  S[t] = detJ * w * th;
+}
+
+// ------------------------------------------------------------------ assembly
+enum Form { SS3 = 0, SS2 = 1, TLH = 2, TLV3 = 3, TLV2 = 4 };
+template <int FORM, int DIM> struct FormInfo;
+template <int DIM> struct FormInfo<SS3, DIM> { static constexpr int NVEC = 2, NSCAL = 3; };
+template <int DIM> struct FormInfo<SS2, DIM> { static constexpr int NVEC = 1, NSCAL = 6; };
+template <int DIM> struct FormInfo<TLH, DIM> { static constexpr int NVEC = 5, NSCAL = 2; };
+template <int DIM> struct FormInfo<TLV3, DIM> { static constexpr int NVEC = 4, NSCAL = 9; };
+template <int DIM> struct FormInfo<TLV2, DIM> { static constexpr int NVEC = 2, NSCAL = 10; };
+
+template <int SHAPE, int RULE, int FORM, typename KT, int EPB>
+struct Layout {
+  static constexpr int DIM = ShapeInfo<SHAPE>::DIM, NN = ShapeInfo<SHAPE>::NN, NQ = RuleInfo<RULE>::NQ;
+  static constexpr int NVEC = FormInfo<FORM, DIM>::NVEC, NSCAL = FormInfo<FORM, DIM>::NSCAL;
+  static constexpr int NDOF = NN * DIM;
+  // offsets in bytes; doubles first for alignment
+  static constexpr size_t u_off = 0;                                              // double [EPB][NN][DIM]
+  static constexpr size_t r_off = u_off + sizeof(double) * EPB * NDOF;            // double [EPB][NQ][NDOF]
+  static constexpr size_t sc_off = r_off + sizeof(double) * EPB * NQ * NDOF;      // KT [EPB][NQ][NSCAL]
+  static constexpr size_t v_off = sc_off + sizeof(KT) * EPB * NQ * NSCAL;         // KT [EPB][NQ][NN][NVEC][DIM]
+  static constexpr size_t rl_off = v_off + sizeof(KT) * EPB * NQ * NN * NVEC * DIM;  // int [EPB][NN]
+  static constexpr size_t bytes = rl_off + sizeof(int) * EPB * NN;
+};
+
+template <typename KT>
+__device__ __forceinline__ void kadd(KT* p, KT v) {
+  atomicAdd(p, v);
+}
+
+template <int SHAPE, int RULE, int FORM, typename KT, int EPB, int NT>
+__global__ void __launch_bounds__(NT) assemble_kernel(GroupArgs g) {
+  using L = Layout<SHAPE, RULE, FORM, KT, EPB>;
+  constexpr int DIM = L::DIM, NN = L::NN, NQ = L::NQ, NVEC = L::NVEC, NSCAL = L::NSCAL, NDOF = L::NDOF;
+  extern __shared__ __align__(16) unsigned char smem[];
+  double* su = reinterpret_cast<double*>(smem + L::u_off);
+  double* sr = reinterpret_cast<double*>(smem + L::r_off);
+  KT* ssc = reinterpret_cast<KT*>(smem + L::sc_off);
+  KT* sv = reinterpret_cast<KT*>(smem + L::v_off);
+  int* srl = reinterpret_cast<int*>(smem + L::rl_off);
+
+  const int64_t e0 = (int64_t)blockIdx.x * EPB;
+  const int64_t nEl = g.nElements;
+  const bool tl = (FORM == TLH || FORM == TLV3 || FORM == TLV2);
+  const double* Ux = tl ? g.U : g.dU;
+
+  // ---- phase 0: nodal displacements and row lengths
+  for (int t = threadIdx.x; t < EPB * NN; t += NT) {
+    const int le = t / NN, a = t % NN;
+    const int64_t e = e0 + le;
+    if (e < nEl) {
+      const int32_t node = g.conn[e * NN + a];
+      const int32_t dof = g.nodeDof[node];
+      for (int c = 0; c < DIM; ++c) su[(le * NN + a) * DIM + c] = Ux[dof + c];
+      srl[le * NN + a] = g.nodeRowLen[node];
+    }
+  }
+  __syncthreads();
+
+  // ---- phase A: material points
+  const int64_t stride = nEl * NQ;
+  for (int t = threadIdx.x; t < EPB * NQ; t += NT) {
+    const int le = t / NQ, q = t % NQ;
+    const int64_t e = e0 + le;
+    if (e >= nEl) continue;
+    const int64_t pt = e * NQ + q;
+    double Gm[DIM][NN];
+#pragma unroll
+    for (int c = 0; c < DIM; ++c)
+#pragma unroll
+      for (int a = 0; a < NN; ++a) Gm[c][a] = g.geomG[(int64_t)(c * NN + a) * stride + pt];
+    const double s = g.geomS[pt];
+    const double* u = su + le * NN * DIM;
+    const double* props = g.props + e * g.nProps;
+    double* rq = sr + (le * NQ + q) * NDOF;
+    KT* sc = ssc + (le * NQ + q) * NSCAL;
+    KT* vq = sv + (size_t)(le * NQ + q) * NN * NVEC * DIM;
+    bool ok = true;
+    double sig[6], eps[6], kappa = 0.0;
+    for (int f = 0; f < 6; ++f) {
+      sig[f] = g.stateRef[(int64_t)f * stride + pt];
+      eps[f] = g.stateRef[(int64_t)(6 + f) * stride + pt];
+    }
+    const bool hasM = g.material != EFE_MAT_LINEAR_ELASTIC;
+    if (hasM) kappa = g.stateRef[(int64_t)12 * stride + pt];
+
+    if constexpr (FORM == SS3 || FORM == SS2) {
+      // ------------------------------------------------ small strain (element.py:318-346)
+      double de[6] = {0, 0, 0, 0, 0, 0};
+      if constexpr (DIM == 3) {
+        for (int a = 0; a < NN; ++a) {
+          const double ux = u[a * 3 + 0], uy = u[a * 3 + 1], uz = u[a * 3 + 2];
+          const double gx = Gm[0][a], gy = Gm[1][a], gz = Gm[2][a];
+          de[0] += gx * ux;
+          de[1] += gy * uy;
+          de[2] += gz * uz;
+          de[3] += gy * ux + gx * uy;
+          de[4] += gz * ux + gx * uz;
+          de[5] += gz * uy + gy * uz;
+        }
+      } else {
+        for (int a = 0; a < NN; ++a) {
+          const double ux = u[a * DIM + 0], uy = u[a * DIM + 1];
+          const double gx = Gm[0][a], gy = Gm[1][DIM == 2 ? a : a];
+          de[0] += gx * ux;
+          de[1] += gy * uy;
+          de[3] += gy * ux + gx * uy;
+        }
+      }
+      if constexpr (FORM == SS3) {
+        Tangent3 T;
+        if (g.material == EFE_MAT_VON_MISES)
+          ok = von_mises_3d(props, sig, de, kappa, T);
+        else
+          linear_elastic_3d(props, sig, de, T);
+        // residual r_a = s * sigma . G_a   (small-strain Voigt order 11,22,33,12,13,23)
+        for (int a = 0; a < NN; ++a) {
+          const double gx = Gm[0][a], gy = Gm[1][a], gz = Gm[2 % DIM][a];
+          rq[a * DIM + 0] = (sig[0] * gx + sig[3] * gy + sig[4] * gz) * s;
+          rq[a * DIM + 1] = (sig[3] * gx + sig[1] * gy + sig[5] * gz) * s;
+          rq[a * DIM + 2 % DIM] = (sig[4] * gx + sig[5] * gy + sig[2] * gz) * s;
+        }
+        sc[0] = (KT)(T.c12 * s);
+        sc[1] = (KT)(T.c44 * s);
+        sc[2] = (KT)(T.a * s);
+        const double* n = T.n;
+        for (int a = 0; a < NN; ++a) {
+          const double gx = Gm[0][a], gy = Gm[1][a], gz = Gm[2 % DIM][a];
+          KT* v = vq + a * NVEC * DIM;
+          v[0] = (KT)gx;
+          v[1] = (KT)gy;
+          v[2 % DIM] = (KT)gz;
+          v[DIM + 0] = (KT)(n[0] * gx + n[3] * gy + n[4] * gz);
+          v[DIM + 1] = (KT)(n[3] * gx + n[1] * gy + n[5] * gz);
+          v[DIM + 2 % DIM] = (KT)(n[4] * gx + n[5] * gy + n[2] * gz);
+        }
+      } else {
+        Tangent2 C;
+        if (g.plane == EFE_PLANE_STRESS) {
+          if (g.material == EFE_MAT_VON_MISES)
+            ok = von_mises_plane_stress(props, sig, de, kappa, C);
+          else
+            linear_elastic_plane_stress(props, sig, de, C);
+        } else {
+          Tangent3 T;
+          if (g.material == EFE_MAT_VON_MISES)
+            ok = von_mises_3d(props, sig, de, kappa, T);
+          else
+            linear_elastic_3d(props, sig, de, T);
+          tangent2_from3(T, C);
+        }
+        for (int a = 0; a < NN; ++a) {
+          const double gx = Gm[0][a], gy = Gm[1 % DIM][a];
+          rq[a * DIM + 0] = (sig[0] * gx + sig[3] * gy) * s;
+          rq[a * DIM + 1 % DIM] = (sig[3] * gx + sig[1] * gy) * s;
+          KT* v = vq + a * NVEC * DIM;
+          v[0] = (KT)gx;
+          v[1 % DIM] = (KT)gy;
+        }
+        for (int k = 0; k < 6; ++k) sc[k] = (KT)(C.c[k] * s);
+      }
+      for (int f = 0; f < 6; ++f) eps[f] += de[f];
+    } else {
+      // ------------------------------------------------ total Lagrangian (displacementtlelement/element.py:346-427)
+      double F[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+      for (int i = 0; i < DIM; ++i)
+        for (int j = 0; j < DIM; ++j) {
+          double h = 0.0;
+          for (int a = 0; a < NN; ++a) h += u[a * DIM + i] * Gm[j][a];
+          F[i][j] += h;
+        }
+      // Green-Lagrange E = 1/2 (H + H^T + H^T H), H = F - I  (:386)
+      double Eg[3][3];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          double hh = 0.0;
+          for (int k = 0; k < DIM; ++k) hh += (F[k][i] - (k == i)) * (F[k][j] - (k == j));
+          Eg[i][j] = (i < DIM && j < DIM) ? 0.5 * ((F[i][j] - (i == j)) + (F[j][i] - (i == j)) + hh) : 0.0;
+        }
+      const double Ev[6] = {Eg[0][0], Eg[1][1], Eg[2][2], Eg[0][1], Eg[1][2], Eg[0][2]};
+      for (int f = 0; f < 6; ++f) g.auxTemp[(int64_t)f * stride + pt] = Ev[f];
+      double detF, iF[3][3];
+      if constexpr (DIM == 2) {
+        detF = F[0][0] * F[1][1] - F[0][1] * F[1][0];
+        iF[0][0] = F[1][1] / detF;
+        iF[0][1] = -F[0][1] / detF;
+        iF[1][0] = -F[1][0] / detF;
+        iF[1][1] = F[0][0] / detF;
+        iF[0][2] = iF[1][2] = iF[2][0] = iF[2][1] = 0.0;
+        iF[2][2] = 1.0;
+      } else {
+        detF = det3(F);
+        inv3(F, detF, iF);
+      }
+      if constexpr (FORM == TLH) {
+        NeoHookeOut o;
+        neo_hooke(g.material, props[0], props[1], F, o);
+        sig[0] = o.tau[0][0];
+        sig[1] = o.tau[1][1];
+        sig[2] = o.tau[2][2];
+        sig[3] = o.tau[0][1];
+        sig[4] = o.tau[1][2];
+        sig[5] = o.tau[0][2];
+        kappa = o.energy;
+        // strain slot = Voigt(E) at the active indices, zero elsewhere (:393, :404)
+        for (int f = 0; f < 6; ++f) eps[f] = 0.0;
+        eps[0] = Eg[0][0];
+        eps[1] = Eg[1][1];
+        if constexpr (DIM == 3) {
+          eps[2] = Eg[2][2];
+          eps[3] = 2.0 * Eg[0][1];
+          eps[4] = 2.0 * Eg[1][2];
+          eps[5] = 2.0 * Eg[0][2];
+        } else {
+          eps[3] = 2.0 * Eg[0][1];
+        }
+        sc[0] = (KT)(o.c1 * s);
+        sc[1] = (KT)(o.c4 * s);
+        for (int a = 0; a < NN; ++a) {
+          double h[3] = {0, 0, 0}, gg[3] = {0, 0, 0};
+          for (int i = 0; i < DIM; ++i)
+            for (int I = 0; I < DIM; ++I) {
+              h[i] += Gm[I][a] * iF[I][i];  // h_a = F^-T dN_a/dX  (NAi, :391)
+              gg[i] += F[i][I] * Gm[I][a];  // g_a = F dN_a/dX
+            }
+          double th[3], bh[3];
+          for (int j = 0; j < DIM; ++j) {
+            th[j] = 0.0;
+            bh[j] = 0.0;
+            for (int i = 0; i < DIM; ++i) {
+              th[j] += o.tau[j][i] * h[i];
+              bh[j] += o.Bm[j][i] * h[i];
+            }
+          }
+          // P_e -= s * (dN/dX^T F^-1 tau) = s * tau h_a  (:402, :414)
+          for (int j = 0; j < DIM; ++j) rq[a * DIM + j] = th[j] * s;
+          KT* v = vq + a * NVEC * DIM;
+          for (int j = 0; j < DIM; ++j) {
+            v[0 * DIM + j] = (KT)Gm[j][a];
+            v[1 * DIM + j] = (KT)h[j];
+            v[2 * DIM + j] = (KT)gg[j];
+            v[3 * DIM + j] = (KT)((o.c1 * gg[j] - th[j]) * s);
+            v[4 * DIM + j] = (KT)((o.c2 * h[j] + o.c3 * bh[j]) * s);
+          }
+        }
+      } else {
+        // hypoelastic material on the Green-Lagrange strain increment (:416-426)
+        double de[6] = {0, 0, 0, 0, 0, 0};
+        const double* Eo = g.auxRef;
+        double Eold[6];
+        for (int f = 0; f < 6; ++f) Eold[f] = Eo ? Eo[(int64_t)f * stride + pt] : 0.0;
+        if constexpr (DIM == 3) {
+          de[0] = Ev[0] - Eold[0];
+          de[1] = Ev[1] - Eold[1];
+          de[2] = Ev[2] - Eold[2];
+          de[3] = (Ev[3] - Eold[3]) * 2.0;
+          de[4] = (Ev[4] - Eold[4]) * 2.0;
+          de[5] = (Ev[5] - Eold[5]) * 2.0;
+        } else {
+          de[0] = Ev[0] - Eold[0];
+          de[1] = Ev[1] - Eold[1];
+          de[3] = (Ev[3] - Eold[3]) * 2.0;
+        }
+        if constexpr (FORM == TLV3) {
+          Tangent3 T;
+          if (g.material == EFE_MAT_VON_MISES)
+            ok = von_mises_3d(props, sig, de, kappa, T);
+          else
+            linear_elastic_3d(props, sig, de, T);
+          // TL Voigt order 11,22,33,12,23,13
+          const double Sm[3][3] = {{sig[0], sig[3], sig[5]}, {sig[3], sig[1], sig[4]}, {sig[5], sig[4], sig[2]}};
+          const double Nm[3][3] = {{T.n[0], T.n[3], T.n[5]}, {T.n[3], T.n[1], T.n[4]}, {T.n[5], T.n[4], T.n[2]}};
+          sc[0] = (KT)(T.c12 * s);
+          sc[1] = (KT)(T.c44 * s);
+          sc[2] = (KT)(T.a * s);
+          int k = 3;
+          for (int i = 0; i < 3; ++i)
+            for (int j = i; j < 3; ++j) sc[k++] = (KT)(F[i][0] * F[j][0] + F[i][1] * F[j][1] + F[i][2] * F[j][2]);
+          for (int a = 0; a < NN; ++a) {
+            double SG[3], NG[3];
+            for (int i = 0; i < 3; ++i) {
+              SG[i] = Sm[i][0] * Gm[0][a] + Sm[i][1] * Gm[1][a] + Sm[i][2] * Gm[2 % DIM][a];
+              NG[i] = Nm[i][0] * Gm[0][a] + Nm[i][1] * Gm[1][a] + Nm[i][2] * Gm[2 % DIM][a];
+            }
+            KT* v = vq + a * NVEC * DIM;
+            for (int c = 0; c < 3; ++c) {
+              const double fsg = F[c][0] * SG[0] + F[c][1] * SG[1] + F[c][2] * SG[2];
+              rq[a * DIM + c % DIM] = fsg * s;  // B0^T sigma = F sigma dN/dX
+              v[0 * DIM + c % DIM] = (KT)Gm[c % DIM][a];
+              v[1 * DIM + c % DIM] = (KT)(F[c][0] * Gm[0][a] + F[c][1] * Gm[1][a] + F[c][2] * Gm[2 % DIM][a]);
+              v[2 * DIM + c % DIM] = (KT)(F[c][0] * NG[0] + F[c][1] * NG[1] + F[c][2] * NG[2]);
+              v[3 * DIM + c % DIM] = (KT)(SG[c] * s);
+            }
+          }
+        } else {  // TLV2
+          Tangent2 C;
+          if (g.plane == EFE_PLANE_STRESS) {
+            if (g.material == EFE_MAT_VON_MISES)
+              ok = von_mises_plane_stress(props, sig, de, kappa, C);
+            else
+              linear_elastic_plane_stress(props, sig, de, C);
+          } else {
+            Tangent3 T;
+            if (g.material == EFE_MAT_VON_MISES)
+              ok = von_mises_3d(props, sig, de, kappa, T);
+            else
+              linear_elastic_3d(props, sig, de, T);
+            tangent2_from3(T, C);
+          }
+          // stress entering P: indices [0,1,3] (plane strain) or [0,1,2] (plane stress, :278-281);
+          // Hgeo always reads undoVoigtStress(2, stress) = [[s0, s2], [s2, s1]] (element.py:48-73)
+          const double s12p = (g.plane == EFE_PLANE_STRESS) ? sig[2] : sig[3];
+          const double Sp[2][2] = {{sig[0], s12p}, {s12p, sig[1]}};
+          const double Sg[2][2] = {{sig[0], sig[2]}, {sig[2], sig[1]}};
+          for (int k = 0; k < 6; ++k) sc[k] = (KT)(C.c[k] * s);
+          sc[6] = (KT)F[0][0];
+          sc[7] = (KT)F[0][1];
+          sc[8] = (KT)F[1][0];
+          sc[9] = (KT)F[1][1];
+          for (int a = 0; a < NN; ++a) {
+            const double gx = Gm[0][a], gy = Gm[1 % DIM][a];
+            const double spx = Sp[0][0] * gx + Sp[0][1] * gy, spy = Sp[1][0] * gx + Sp[1][1] * gy;
+            rq[a * DIM + 0] = (F[0][0] * spx + F[0][1] * spy) * s;
+            rq[a * DIM + 1 % DIM] = (F[1][0] * spx + F[1][1] * spy) * s;
+            KT* v = vq + a * NVEC * DIM;
+            v[0] = (KT)gx;
+            v[1 % DIM] = (KT)gy;
+            v[DIM + 0] = (KT)((Sg[0][0] * gx + Sg[0][1] * gy) * s);
+            v[DIM + 1 % DIM] = (KT)((Sg[1][0] * gx + Sg[1][1] * gy) * s);
+          }
+        }
+        for (int f = 0; f < 6; ++f) eps[f] += de[f];
+      }
+    }
+    // ---- state write (stateTemp = updated copy of stateRef)
+    for (int f = 0; f < 6; ++f) {
+      g.stateTemp[(int64_t)f * stride + pt] = sig[f];
+      g.stateTemp[(int64_t)(6 + f) * stride + pt] = eps[f];
+    }
+    if (hasM) g.stateTemp[(int64_t)12 * stride + pt] = kappa;
+    bool finite = true;
+    for (int f = 0; f < 6; ++f) finite = finite && isfinite(sig[f]);
+    if (!ok) report(g.status, EFE_STATUS_CUTBACK, g.elementOffset + e, 1);
+    if (!finite) atomicOr(g.status, EFE_STATUS_NONFINITE);
+  }
+  __syncthreads();
+
+  // ---- phase C: residual and flux
+  for (int t = threadIdx.x; t < EPB * NDOF; t += NT) {
+    const int le = t / NDOF, k = t % NDOF;
+    const int64_t e = e0 + le;
+    if (e >= nEl) continue;
+    double pe = 0.0;
+    for (int q = 0; q < NQ; ++q) pe -= sr[(le * NQ + q) * NDOF + k];
+    const int a = k / DIM, c = k % DIM;
+    const int32_t node = g.conn[e * NN + a];
+    const int32_t dof = g.nodeDof[node] + c;
+    atomicAdd(g.P + dof, pe);
+    atomicAdd(g.F + dof, fabs(pe));
+  }
+
+  // ---- phase B: tangent blocks
+  KT* K = reinterpret_cast<KT*>(g.Kdata);
+  for (int t = threadIdx.x; t < EPB * NN * NN; t += NT) {
+    const int le = t / (NN * NN), ab = t % (NN * NN);
+    const int a = ab / NN, b = ab % NN;
+    const int64_t e = e0 + le;
+    if (e >= nEl) continue;
+    KT acc[DIM][DIM];
+#pragma unroll
+    for (int j = 0; j < DIM; ++j)
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) acc[j][k] = KT(0);
+    for (int q = 0; q < NQ; ++q) {
+      const KT* sc = ssc + (le * NQ + q) * NSCAL;
+      const KT* va = sv + (size_t)((le * NQ + q) * NN + a) * NVEC * DIM;
+      const KT* vb = sv + (size_t)((le * NQ + q) * NN + b) * NVEC * DIM;
+      if constexpr (FORM == SS3) {
+        const KT Lq = sc[0], Mq = sc[1], Aq = sc[2];
+        const KT dot = va[0] * vb[0] + va[1] * vb[1] + va[2 % DIM] * vb[2 % DIM];
+#pragma unroll
+        for (int j = 0; j < DIM; ++j)
+#pragma unroll
+          for (int k = 0; k < DIM; ++k)
+            acc[j][k] += Lq * va[j] * vb[k] + Mq * ((j == k ? dot : KT(0)) + va[k] * vb[j]) -
+                         Aq * va[DIM + j] * vb[DIM + k];
+      } else if constexpr (FORM == SS2) {
+        // B columns (11,22,12): (a,0) = [gx, 0, gy], (a,1) = [0, gy, gx]
+        const KT c00 = sc[0], c01 = sc[1], c02 = sc[2], c11 = sc[3], c12 = sc[4], c22 = sc[5];
+        const KT ax = va[0], ay = va[1 % DIM], bx = vb[0], by = vb[1 % DIM];
+        // C * Bcol_b0 = C[:,0] bx + C[:,2] by ; C * Bcol_b1 = C[:,1] by + C[:,2] bx
+        const KT cb0[3] = {c00 * bx + c02 * by, c01 * bx + c12 * by, c02 * bx + c22 * by};
+        const KT cb1[3] = {c01 * by + c02 * bx, c11 * by + c12 * bx, c12 * by + c22 * bx};
+        acc[0][0] += ax * cb0[0] + ay * cb0[2];
+        acc[0][1 % DIM] += ax * cb1[0] + ay * cb1[2];
+        acc[1 % DIM][0] += ay * cb0[1] + ax * cb0[2];
+        acc[1 % DIM][1 % DIM] += ay * cb1[1] + ax * cb1[2];
+      } else if constexpr (FORM == TLH) {
+        const KT c1s = sc[0], c4s = sc[1];
+        const KT* Ga = va;
+        const KT* Gb = vb;
+        const KT* ha = va + DIM;
+        const KT* hb = vb + DIM;
+        const KT* gb = vb + 2 * DIM;
+        const KT* pb = vb + 3 * DIM;
+        const KT* qa = va + 4 * DIM;
+        KT dot = KT(0);
+#pragma unroll
+        for (int i = 0; i < DIM; ++i) dot += Ga[i] * Gb[i];
+#pragma unroll
+        for (int j = 0; j < DIM; ++j)
+#pragma unroll
+          for (int k = 0; k < DIM; ++k)
+            acc[j][k] += pb[j] * ha[k] + qa[j] * hb[k] + c4s * ha[j] * gb[k] + (j == k ? c1s * dot : KT(0));
+      } else if constexpr (FORM == TLV3) {
+        const KT Lq = sc[0], Mq = sc[1], Aq = sc[2];
+        const KT FF[3][3] = {{sc[3], sc[4], sc[5]}, {sc[4], sc[6], sc[7]}, {sc[5], sc[7], sc[8]}};
+        const KT* Ga = va;
+        const KT* Gb = vb;
+        const KT* ga = va + DIM;
+        const KT* gb = vb + DIM;
+        const KT* wa = va + 2 * DIM;
+        const KT* wb = vb + 2 * DIM;
+        const KT* ta = va + 3 * DIM;
+        KT dot = KT(0), geo = KT(0);
+#pragma unroll
+        for (int i = 0; i < DIM; ++i) {
+          dot += Ga[i] * Gb[i];
+          geo += ta[i] * Gb[i];
+        }
+#pragma unroll
+        for (int c = 0; c < DIM; ++c)
+#pragma unroll
+          for (int d = 0; d < DIM; ++d)
+            acc[c][d] += Lq * ga[c] * gb[d] + Mq * (FF[c][d] * dot + gb[c] * ga[d]) - Aq * wa[c] * wb[d] +
+                         (c == d ? geo : KT(0));
+      } else {  // TLV2
+        const KT* C = sc;
+        const KT F00 = sc[6], F01 = sc[7], F10 = sc[8], F11 = sc[9];
+        const KT ax = va[0], ay = va[1 % DIM], bx = vb[0], by = vb[1 % DIM];
+        const KT geo = va[DIM + 0] * bx + va[DIM + 1 % DIM] * by;
+        // B0 columns: (a,c) = [ax F_c0, ay F_c1, ax F_c1 + ay F_c0]
+        KT Ba[2][3], Bb[2][3];
+        const KT Fr[2][2] = {{F00, F01}, {F10, F11}};
+        for (int c = 0; c < 2; ++c) {
+          Ba[c][0] = ax * Fr[c][0];
+          Ba[c][1] = ay * Fr[c][1];
+          Ba[c][2] = ax * Fr[c][1] + ay * Fr[c][0];
+          Bb[c][0] = bx * Fr[c][0];
+          Bb[c][1] = by * Fr[c][1];
+          Bb[c][2] = bx * Fr[c][1] + by * Fr[c][0];
+        }
+        const KT Cm[3][3] = {{C[0], C[1], C[2]}, {C[1], C[3], C[4]}, {C[2], C[4], C[5]}};
+        for (int d = 0; d < 2; ++d) {
+          KT cb[3];
+          for (int i = 0; i < 3; ++i) cb[i] = Cm[i][0] * Bb[d][0] + Cm[i][1] * Bb[d][1] + Cm[i][2] * Bb[d][2];
+          for (int c = 0; c < 2; ++c)
+            acc[c % DIM][d % DIM] += Ba[c][0] * cb[0] + Ba[c][1] * cb[1] + Ba[c][2] * cb[2] + (c == d ? geo : KT(0));
+        }
+      }
+    }
+    // Ke[(a,j),(b,k)] -> CSR (row = dof(b,k), col = dof(a,j)) = slot(a,b) + k*rowLen(b) + j
+    const int32_t slot = g.pairSlot[(e * NN + a) * NN + b];
+    const int rl = srl[le * NN + b];
+#pragma unroll
+    for (int j = 0; j < DIM; ++j)
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) kadd(K + slot + (int64_t)k * rl + j, acc[j][k]);
+  }
+}
+
+}  // namespace efe

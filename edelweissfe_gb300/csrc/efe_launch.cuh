@@ -1,0 +1,84 @@
+// efe_launch.cuh -- tile sizing and launch of the kernels of one element shape.
+#pragma once
+#include "efe_kernels.cuh"
+
+namespace efe {
+
+// Elements per CTA: as many as fit in ~96 KB of shared memory (two CTAs per SM fit in 228 KB),
+// capped at 32.
+template <int SHAPE, int RULE, int FORM, typename KT>
+struct Tile {
+  static constexpr size_t per_element = Layout<SHAPE, RULE, FORM, KT, 1>::bytes;
+  static constexpr int fit = (int)((96 * 1024) / per_element);
+  static constexpr int EPB = fit < 1 ? 1 : (fit > 32 ? 32 : fit);
+  static constexpr int NT = (EPB * RuleInfo<RULE>::NQ >= 192) ? 256 : 128;
+  static constexpr size_t bytes = Layout<SHAPE, RULE, FORM, KT, EPB>::bytes;
+};
+
+template <int SHAPE, int RULE, int FORM, typename KT>
+cudaError_t launch_assemble(const GroupArgs& g, cudaStream_t st) {
+  using T = Tile<SHAPE, RULE, FORM, KT>;
+  static_assert(T::bytes <= 200 * 1024, "tile does not fit in shared memory");
+  auto kern = assemble_kernel<SHAPE, RULE, FORM, KT, T::EPB, T::NT>;
+  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::bytes);
+  if (err != cudaSuccess) return err;
+  const int64_t grid = (g.nElements + T::EPB - 1) / T::EPB;
+  if (grid == 0) return cudaSuccess;
+  kern<<<(unsigned)grid, T::NT, T::bytes, st>>>(g);
+  return cudaGetLastError();
+}
+
+template <int SHAPE, int RULE>
+cudaError_t launch_geometry(int64_t nEl, int64_t elOffset, const int32_t* conn, const double* coords,
+                            const double* thickness, double* G, double* S, int32_t* status, const Hexa20Fix& fix,
+                            cudaStream_t st) {
+  const int64_t n = nEl * RuleInfo<RULE>::NQ;
+  if (n == 0) return cudaSuccess;
+  const int nt = 128;
+  geometry_kernel<SHAPE, RULE><<<(unsigned)((n + nt - 1) / nt), nt, 0, st>>>(nEl, elOffset, conn, coords, thickness,
+                                                                             G, S, status, fix);
+  return cudaGetLastError();
+}
+
+// form selector: small strain 3D/2D, total Lagrangian hyperelastic, total Lagrangian hypoelastic 3D/2D
+template <int SHAPE, int RULE, typename KT>
+cudaError_t launch_form(int form, const GroupArgs& g, cudaStream_t st) {
+  constexpr int DIM = ShapeInfo<SHAPE>::DIM;
+  if constexpr (DIM == 3) {
+    switch (form) {
+      case SS3: return launch_assemble<SHAPE, RULE, SS3, KT>(g, st);
+      case TLH: return launch_assemble<SHAPE, RULE, TLH, KT>(g, st);
+      case TLV3: return launch_assemble<SHAPE, RULE, TLV3, KT>(g, st);
+    }
+  } else {
+    switch (form) {
+      case SS2: return launch_assemble<SHAPE, RULE, SS2, KT>(g, st);
+      case TLH: return launch_assemble<SHAPE, RULE, TLH, KT>(g, st);
+      case TLV2: return launch_assemble<SHAPE, RULE, TLV2, KT>(g, st);
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <int SHAPE, int RULE>
+cudaError_t launch_rule(int form, int kprec, const GroupArgs& g, cudaStream_t st) {
+  return kprec == EFE_K_FP32 ? launch_form<SHAPE, RULE, float>(form, g, st)
+                             : launch_form<SHAPE, RULE, double>(form, g, st);
+}
+
+// per-shape entry points (one translation unit each, compiled in parallel)
+cudaError_t assemble_quad4(int rule, int form, int kprec, const GroupArgs& g, cudaStream_t st);
+cudaError_t assemble_quad8(int rule, int form, int kprec, const GroupArgs& g, cudaStream_t st);
+cudaError_t assemble_hexa8(int rule, int form, int kprec, const GroupArgs& g, cudaStream_t st);
+cudaError_t assemble_hexa20(int rule, int form, int kprec, const GroupArgs& g, cudaStream_t st);
+#define EFE_GEOMETRY_DECL(name)                                                                          \
+  cudaError_t geometry_##name(int rule, int64_t nEl, int64_t off, const int32_t* conn, const double* coords, \
+                              const double* th, double* G, double* S, int32_t* status, const Hexa20Fix& fix,  \
+                              cudaStream_t st);
+EFE_GEOMETRY_DECL(quad4)
+EFE_GEOMETRY_DECL(quad8)
+EFE_GEOMETRY_DECL(hexa8)
+EFE_GEOMETRY_DECL(hexa20)
+#undef EFE_GEOMETRY_DECL
+
+}  // namespace efe

@@ -1,0 +1,165 @@
+/*
+ * efe_gb300.h -- C ABI of the GB300 (sm_103a) element-evaluation and CSR-assembly library.
+ *
+ * The library replaces, for the reference's "edelweiss" displacement elements, the per-element
+ * Python loop of NIST.computeElements and the COO->CSR scatter of CSRGenerator.updateCSR:
+ *
+ *   reference (EdelweissFE, paths relative to the project root)          replaced by
+ *   --------------------------------------------------------------------------------------------
+ *   solvers/nonlinearimplicitstatic.py:794-849  NIST.computeElements      efe_compute_elements
+ *   numerics/csrgenerator.pyx:100-115           CSRGenerator.updateCSR    efe_compute_elements
+ *                                                (K is scattered straight into CSR data)
+ *   numerics/csrgenerator.pyx:47-98             CSRGenerator.__init__     efe_pattern_count / efe_pattern_fill
+ *   numerics/dofmanager.py:522-557              DofManager VIJ pattern    (no VIJ vector is formed)
+ *   elements/displacementelement/element.py:194-205 initializeElement     efe_setup_geometry
+ *   elements/displacementtlelement/element.py:249-259 initializeElement   efe_setup_geometry
+ *   elements/displacementelement/element.py:373-379 acceptLastState      efe_accept_state
+ *   elements/displacementtlelement/element.py:454-461 acceptLastState    efe_accept_state
+ *   elements/marmotelement/element.pxd:97-103   MarmotElement::computeYourself (native ABI shape:
+ *                                                caller-owned buffers, pNewDT status -> CutbackRequest)
+ *
+ * Conventions
+ *   - All array arguments of efe_setup_geometry / efe_compute_elements / efe_accept_state are
+ *     DEVICE pointers owned by the caller; the library never allocates on these calls.
+ *     efe_pattern_count / efe_pattern_fill work on HOST arrays (set-up, once per mesh).
+ *   - `stream` is a cudaStream_t passed as void*; NULL means the legacy default stream.
+ *   - Return value 0 = success; otherwise an EFE_ERR_* code, and efe_last_error() describes it.
+ *     Numerical failures of material points are never raised on the device: they are reported
+ *     in `status` (see EFE_STATUS_*), and the host raises CutbackRequest (utils/exceptions.py:44-49).
+ *   - DOF numbering: every node carries `dim` consecutive DOFs starting at nodeDof[node]
+ *     (DofManager._reserveSpaceForNodeFields, dofmanager.py:259-300, one displacement field).
+ *   - Element matrix placement follows the reference VIJ layout (dofmanager.py:552-554): the
+ *     value Ke[(a,j),(b,k)] of element node pair (a,b), components (j,k), is added to the CSR
+ *     entry (row = dof(b,k), col = dof(a,j)).
+ *   - Per-quadrature-point arrays are structure-of-arrays: field f of point q of element e is at
+ *     [f * (nElements * nInt) + e * nInt + q].
+ */
+#ifndef EFE_GB300_H
+#define EFE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EFE_ABI_VERSION 1
+
+/* element shapes (node numbering of computeNOperator, _elementcomputationmatrices.py:106-212) */
+enum { EFE_QUAD4 = 0, EFE_QUAD8 = 1, EFE_HEXA8 = 2, EFE_HEXA20 = 3 };
+/* quadrature rules of elements/library.py:33-533 */
+enum {
+  EFE_RULE_2D_1 = 0,     /* 1 point, weight 4                         (CPE4R)          */
+  EFE_RULE_2D_2X2 = 1,   /* 2x2 Gauss                                  (CPE4, CPE8R)    */
+  EFE_RULE_2D_3X3 = 2,   /* 3x3 Gauss                                  (CPE4E, CPE8)    */
+  EFE_RULE_3D_1 = 3,     /* 1 point, weight 8                         (C3D8R)          */
+  EFE_RULE_3D_2X2X2 = 4, /* 2x2x2 Gauss                                (C3D8, C3D20R)   */
+  EFE_RULE_3D_3X3X3 = 5  /* 3x3x3 Gauss                                (C3D8E, C3D20)   */
+};
+/* kinematics */
+enum { EFE_SMALL_STRAIN = 0, EFE_TOTAL_LAGRANGIAN = 1 };
+/* in-plane assumption of 2D elements (library.py plStrain); solids use EFE_SOLID */
+enum { EFE_SOLID = 0, EFE_PLANE_STRAIN = 1, EFE_PLANE_STRESS = 2 };
+/* materials (edelweissfe/materials): property counts 2, 6, 2, 2, 2 */
+enum {
+  EFE_MAT_LINEAR_ELASTIC = 0, /* [E, nu]                              linearelastic.py:59-61 */
+  EFE_MAT_VON_MISES = 1,      /* [E, nu, fy0, HLin, dfy, delta]       vonmises.py:105-124    */
+  EFE_MAT_NEOHOOKE_WA = 2,    /* [mu, K]                              neohookepencegouformulationa.py:65-70 */
+  EFE_MAT_NEOHOOKE_WB = 3,
+  EFE_MAT_NEOHOOKE_WC = 4
+};
+/* precision of the assembled tangent (CSR data) */
+enum {
+  EFE_K_FP64 = 0, /* everything in FP64 (Kdata is double*)                                   */
+  EFE_K_FP32 = 1  /* tangent formed and accumulated in FP32 (Kdata is float*); residual, state
+                     and the return map stay FP64                                              */
+};
+/* status words (int32[3], zeroed by the caller): status[0] = OR of EFE_STATUS_* bits,
+   status[1] = INT32_MAX - (global index of the first failing element), 0 if none,
+   status[2] = number of failed material points */
+enum {
+  EFE_STATUS_CUTBACK = 1,      /* a material point asked for a cutback (CutbackRequest(.., 0.5)) */
+  EFE_STATUS_BAD_JACOBIAN = 2, /* det J <= 0 or not finite at set-up                               */
+  EFE_STATUS_NONFINITE = 4     /* a non-finite stress was produced                                 */
+};
+/* error codes */
+enum {
+  EFE_OK = 0,
+  EFE_ERR_ARGUMENT = 1,
+  EFE_ERR_UNSUPPORTED = 2,
+  EFE_ERR_CUDA = 3,
+  EFE_ERR_PATTERN = 4
+};
+
+typedef struct EfeMesh {
+  int32_t dim;               /* 2 or 3                                                        */
+  int32_t nNodes;            /* number of nodes (including nodes without DOFs)                */
+  int64_t nDof;              /* size of the DOF vectors                                      */
+  int64_t nnz;               /* number of CSR entries                                        */
+  const double* coords;      /* [nNodes][dim] reference coordinates                          */
+  const int32_t* nodeDof;    /* [nNodes] first DOF of the node, -1 if it has none            */
+  const int32_t* nodeRowLen; /* [nNodes] length of the CSR rows of the node's DOFs           */
+} EfeMesh;
+
+typedef struct EfeGroup {
+  int32_t shape, rule, kinematics, plane, material, nProps;
+  int64_t nElements;
+  int64_t elementOffset;     /* global index (element order) of the group's first element   */
+  const int32_t* conn;       /* [nElements][nNodes] node indices                              */
+  const int32_t* pairSlot;   /* [nElements][nNodes][nNodes]: CSR position of
+                                (row = first DOF of node b, col = first DOF of node a)        */
+  const double* props;       /* [nElements][nProps] material properties per element          */
+  const double* thickness;   /* [nElements] (2D); NULL for solids                            */
+  double* geomG;             /* [dim*nNodes][nElements*nInt]  dN_a/dX_c at row c*nNodes+a    */
+  double* geomS;             /* [nElements*nInt]  det J * weight * thickness                 */
+  double* stateRef;          /* [12 + nMatState][nElements*nInt]  stress(6) strain(6) material;
+                                read by efe_compute_elements, written by efe_accept_state      */
+  double* stateTemp;         /* same layout, written by efe_compute_elements                 */
+  double* auxRef;            /* TL only: Green-Lagrange strain of the last accepted state,
+                                [6][nElements*nInt] as (11,22,33,12,23,13); may be NULL for
+                                hyperelastic materials                                        */
+  double* auxTemp;           /* TL only: Green-Lagrange strain of this call                  */
+} EfeGroup;
+
+int32_t efe_abi_version(void);
+const char* efe_last_error(void);
+
+/* Number of material state variables per quadrature point (12 + m). */
+int32_t efe_state_size(int32_t material);
+/* Number of quadrature points of a rule, nodes of a shape. */
+int32_t efe_rule_points(int32_t rule);
+int32_t efe_shape_nodes(int32_t shape);
+
+/* Jacobians, dN/dX and det J * w * t of every element and quadrature point (once per mesh);
+   status[0] gets EFE_STATUS_BAD_JACOBIAN for det J <= 0. */
+int32_t efe_setup_geometry(const EfeMesh* mesh, const EfeGroup* group, int32_t* status, void* stream);
+
+/* One element pass: for every element of every group, material update from stateRef into
+   stateTemp, K_e scattered into Kdata (double or float per kPrecision), P_e into P, |P_e| into F.
+   U = total displacement (used by total-Lagrangian groups), dU = increment since the last
+   accepted state (used by small-strain groups).  P, F and Kdata are accumulated into: the caller
+   zeroes them first (nonlinearimplicitstatic.py:419).  time2 = [stepTime, totalTime] (host,
+   may be NULL) and dT are accepted for interface parity; the materials here do not use them. */
+int32_t efe_compute_elements(const EfeMesh* mesh, const EfeGroup* groups, int32_t nGroups, const double* U,
+                             const double* dU, const double* time2, double dT, int32_t kPrecision, void* Kdata,
+                             double* P, double* F, int32_t* status, void* stream);
+
+/* acceptLastState: stateTemp -> stateRef and auxTemp -> auxRef for every group. */
+int32_t efe_accept_state(const EfeGroup* groups, int32_t nGroups, void* stream);
+
+/* CSR pattern of the assembled matrix (host arrays; set-up).  conns[g] is [nEl[g]][nNodes[g]].
+   efe_pattern_count fills indptr[nDof+1] and nodeRowLen[nNodes] and returns nnz (or -1);
+   efe_pattern_fill then fills indices[nnz] (sorted per row, as scipy's canonical CSR) and the
+   pair slot maps pairSlots[g] ([nEl[g]][nNodes[g]][nNodes[g]]). */
+int64_t efe_pattern_count(int32_t dim, int32_t nNodes, const int32_t* nodeDof, int32_t nGroups,
+                          const int32_t* const* conns, const int64_t* nEl, const int32_t* nNodesPerEl,
+                          int64_t nDof, int32_t* indptr, int32_t* nodeRowLen);
+int32_t efe_pattern_fill(int32_t dim, int32_t nNodes, const int32_t* nodeDof, int32_t nGroups,
+                         const int32_t* const* conns, const int64_t* nEl, const int32_t* nNodesPerEl, int64_t nDof,
+                         const int32_t* indptr, int32_t* indices, int32_t* const* pairSlots);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EFE_GB300_H */
