@@ -1,0 +1,411 @@
+#!/usr/bin/env python3
+"""Benchmark of the element-evaluation + CSR-assembly pass (one Newton iteration's element loop).
+
+Workload (default, one GPU): boxGen C3D8 64x64x64 unit cube (262,144 elements, 8 quadrature
+points, 823,875 DOFs, 64,701,513 CSR entries), interior nodes jittered +-5 % of the element size
+(seed 1), von Mises J2 [E=210000, nu=0.3, fy0=250, H=1000].  The history is that of a plastic
+uniaxial load path: increment 1 (uniaxial strain 0.25 %) is evaluated and accepted; every timed
+step then evaluates increment 2 (a further 0.025 % plus seeded noise), so the radial return runs
+at (nearly) every point.  A step = zero P, F, K + one pass over all elements: material update,
+residual, tangent, scatter into CSR.  Inputs are larger than L2 (state 218 MB, CSR data
+259/518 MB), so no explicit L2 flush is needed.
+
+`value` is the mixed-precision mode (FP32 tangent, FP64 residual/state/return map) with inputs
+resident in HBM; `fp64` holds the all-FP64 mode; `e2e` times the same pass through the public
+API with host buffers (pinned U, dU in; P, F, K out).  `--impl reference` times the CPU oracle
+port of the reference algorithm on all host cores.
+
+Launch: python bench.py [--gpus N --steps K --warmup W] [--impl reference]; for N>1 under
+torchrun, each rank runs an independent replica (the element pass does not shard across GPUs).
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "assembled elem/s (K+R) mixed vs FP64 GPU, R rel err≤1e-12; adjoint grads/s"
+VM = [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0]
+N_CUBE = 64
+
+
+def workload(n=N_CUBE):
+    from edelweissfe_gb300 import meshes
+
+    coords, conn, nodeDof, nDof = meshes.box(n, n, n, nNodes=8)
+    coords = meshes.jitter(coords, 0.05, [1.0 / n] * 3, 1, [0, 0, 0], [1, 1, 1])
+    rng = np.random.default_rng(2)
+    y = coords[:, 1]
+    dU1 = np.zeros(nDof)
+    dU1[1::3] = 0.0025 * y
+    dU2 = np.zeros(nDof)
+    dU2[1::3] = 0.00025 * y
+    dU2 += rng.uniform(-1, 1, nDof) * 1e-6
+    return coords, conn, nodeDof, nDof, dU1, dU2
+
+
+def algorithmic_bytes(nEl, nQ, nState, nNodes, nDof, nnz, kbytes, nn=8, dim=3):
+    """Unique inputs read once, outputs written once: QP history read+write, connectivity, nodal
+    coordinates, dU, K values, R and F.  Geometry tables, slot maps and CSR indices are
+    implementation traffic and are not counted."""
+    return (nEl * nQ * nState * 8 * 2 + nEl * nn * 4 + nNodes * dim * 8 + nDof * 8 + nnz * kbytes + 2 * nDof * 8)
+
+
+class ClockSampler:
+    FIELDS = (
+        "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+        "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    )
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.path = os.path.join("/tmp", f"efe_clocks_{os.getpid()}.csv")
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"],
+                stdout=self.f, stderr=subprocess.DEVNULL,
+            )  # fmt: skip
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) >= 9:
+                rows.append(p)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        pw = [float(r[3]) for r in rows if r[3].replace(".", "").isdigit()]
+        load = [s for s, w in zip(sm, pw)] if sm else []
+        return {
+            "sm_mhz": statistics.median(load) if load else None,
+            "sm_max_mhz": max(mx) if mx else None,
+            "reasons": reasons,
+            "samples": len(rows),
+            "power_w_max": max(pw) if pw else None,
+        }
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(name):
+    """DRAM bytes per launch from the committed ncu summary (profiles/<name>.txt), or None."""
+    p = os.path.join(ROOT, "profiles", name + ".txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch_full_size:"):
+            return float(line.split(":")[1])
+    return None
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_gpu(args, rank, world):
+    import torch
+
+    from edelweissfe_gb300 import ElementGroup, GPUAssembler
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    coords, conn, nodeDof, nDof, dU1, dU2 = workload(args.n)
+    nEl = len(conn)
+    sampler = ClockSampler(dev.index)
+    results = {}
+    state = {}
+    sampler.start()
+    for precision in ("fp64", "mixed"):
+        asm = GPUAssembler(coords, nodeDof, nDof, [ElementGroup("C3D8", "vonmises", VM, conn)], precision=precision,
+                           device=dev)  # fmt: skip
+        P, F, K = asm.constructDofVector(), asm.constructDofVector(), asm.constructSystemMatrix()
+        d1 = torch.tensor(dU1, device=dev)
+        asm.computeElements(None, d1, d1, P, K, F)  # increment 1
+        asm.acceptLastState()
+        U = torch.tensor(dU1 + dU2, device=dev)
+        dU = torch.tensor(dU2, device=dev)
+        stream = torch.cuda.current_stream(dev)
+
+        def step(ev=None):
+            P.zero_()
+            F.zero_()
+            K.zero_()
+            asm.status.zero_()
+            if ev is not None:
+                ev[0].record(stream)
+            asm.launch(U, dU, P, K, F)
+            if ev is not None:
+                ev[1].record(stream)
+
+        for _ in range(args.warmup):
+            step()
+        asm.check_status()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+        t0.record(stream)
+        for k in range(args.steps):
+            step(evs[k])
+        t1.record(stream)
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
+        ms = t0.elapsed_time(t1) / args.steps
+        kms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
+        if world > 1:
+            tt = torch.tensor([ms, kms], device=dev)
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            ms, kms = float(tt[0]), float(tt[1])
+        asm.check_status()
+        state[precision] = dict(P=P.clone(), K=K.double().clone(), st=asm.group_state(0))
+        results[precision] = dict(ms=ms, kernel_ms=kms, nnz=asm.nnz, asm=asm)
+        if precision == "mixed":
+            results["e2e"] = run_e2e(asm, dU1 + dU2, dU2, args, dev)
+        del P, F, K
+    clocks = sampler.stop()
+    errs = {
+        "R_rel_mixed_vs_fp64": float((state["mixed"]["P"] - state["fp64"]["P"]).abs().max()
+                                     / state["fp64"]["P"].abs().max()),
+        "K_rel_mixed_vs_fp64": float((state["mixed"]["K"] - state["fp64"]["K"]).abs().max()
+                                     / state["fp64"]["K"].abs().max()),
+        "state_rel_mixed_vs_fp64": float(np.abs(state["mixed"]["st"] - state["fp64"]["st"]).max()
+                                         / np.abs(state["fp64"]["st"]).max()),
+        "plastic_point_fraction": float((state["fp64"]["st"][..., 12] > 0).mean()),
+    }  # fmt: skip
+    return results, errs, clocks, nEl, nDof, len(coords)
+
+
+def run_e2e(asm, U_host, dU_host, args, dev):
+    """The same pass through the public API with host buffers: pinned H2D of U and dU, the pass,
+    D2H of P, F and K, all inside the timed region (wall clock, synchronised)."""
+    import torch
+
+    Uh = torch.tensor(U_host).pin_memory()
+    dUh = torch.tensor(dU_host).pin_memory()
+    U, dU = asm.constructDofVector(), asm.constructDofVector()
+    P, F, K = asm.constructDofVector(), asm.constructDofVector(), asm.constructSystemMatrix()
+    Ph = torch.empty_like(P, device="cpu").pin_memory()
+    Fh = torch.empty_like(F, device="cpu").pin_memory()
+    Kh = torch.empty_like(K, device="cpu").pin_memory()
+
+    def step():
+        U.copy_(Uh, non_blocking=True)
+        dU.copy_(dUh, non_blocking=True)
+        P.zero_()
+        F.zero_()
+        K.zero_()
+        asm.computeElements(None, U, dU, P, K, F, check=True)
+        Ph.copy_(P, non_blocking=True)
+        Fh.copy_(F, non_blocking=True)
+        Kh.copy_(K, non_blocking=True)
+        torch.cuda.synchronize(dev)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize(dev)
+    ms = (time.perf_counter() - t) * 1e3 / args.steps
+    return dict(ms=ms, h2d=2 * U.numel() * 8, d2h=2 * P.numel() * 8 + K.numel() * K.element_size())
+
+
+# ------------------------------------------------------------------ CPU baseline (oracle port)
+_CPU = {}
+
+
+def _cpu_setup(n, block):
+    """Oracle model of the first `block` elements of the workload, with the increment-1 history."""
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    sys.path.insert(0, ROOT)
+    from oracle.assembly import Model
+
+    coords, conn, nodeDof, nDof, dU1, dU2 = workload(n)
+    sub = conn[:block].astype(np.int64)
+    g = dict(elType="C3D8", kind="vonmises", props=np.tile(VM, (len(sub), 1)), conn=sub,
+             thickness=np.ones(len(sub)), order=np.arange(len(sub)))  # fmt: skip
+    m = Model(coords, nodeDof, nDof, [g])
+    st = m.accept_state(m.compute_elements(dU1, dU1, m.initial_state())["stateTemp"])
+    _CPU.update(model=m, state=st, U=dU1 + dU2, dU=dU2, block=block)
+
+
+def _cpu_step(_=None):
+    """One pass of the oracle over the block (element evaluation + CSR scatter); (elements, seconds)."""
+    t = time.perf_counter()
+    _CPU["model"].compute_elements(_CPU["U"], _CPU["dU"], _CPU["state"])
+    return _CPU["block"], time.perf_counter() - t
+
+
+def cpu_baseline(n, block=4096, reps=3):
+    """Single-core oracle port on `reps` passes over `block` contiguous elements."""
+    _cpu_setup(n, block)
+    done = 0
+    secs = 0.0
+    for _ in range(reps):
+        d, s = _cpu_step()
+        done += d
+        secs += s
+    return done / secs, done, secs
+
+
+def run_reference(args):
+    """The reference algorithm (oracle port) on all host cores: one process per core, each
+    evaluating its own block of the workload per step; value = elements per wall second."""
+    import multiprocessing as mp
+
+    cores = os.cpu_count() or 1
+    block = 512
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores, initializer=_cpu_setup, initargs=(args.n, block)) as pool:
+        vals = []
+        for k in range(args.warmup + args.steps):
+            t = time.perf_counter()
+            out = pool.map(_cpu_step, range(cores), chunksize=1)
+            wall = time.perf_counter() - t
+            if k >= args.warmup:
+                vals.append(sum(o[0] for o in out) / wall)
+    value = float(np.median(vals))
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "elem/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": block * cores / value * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"C3D8 von Mises J2 {args.n}^3 unit cube (jitter 5%), plastic increment, one element pass",
+                   "sample_per_step": f"{cores} processes x {block} elements"},
+        "cpu_baseline": {"value": value, "unit": "elem/s", "cores": cores, "kind": "port",
+                         "sample": f"{cores} processes x {block} contiguous elements per step, oracle NumPy port "
+                                   "of the reference element/material/assembly algorithm"},
+        "e2e": {"value": value, "unit": "elem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }  # fmt: skip
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_CUBE, help="elements per cube edge")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+    if world > 1:
+        import torch
+
+        torch.distributed.init_process_group("nccl")
+    results, errs, clocks, nEl, nDof, nNodes = run_gpu(args, rank, world)
+    if rank != 0:
+        return
+    mixed, fp64, e2e = results["mixed"], results["fp64"], results["e2e"]
+    value = world * nEl / (mixed["ms"] * 1e-3)
+    peak, peak_kind = peaks()
+    abytes = algorithmic_bytes(nEl, 8, 13, nNodes, nDof, mixed["nnz"], 4)
+    achieved = abytes / (mixed["kernel_ms"] * 1e-3) / 1e9
+    traffic = ncu_traffic("assemble_c3d8_vm_64cube")
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        v, done, secs = cpu_baseline(args.n, block=8192, reps=3)
+        cpu = {"value": v, "unit": "elem/s", "cores": 1, "kind": "port",
+               "sample": f"{done} element evaluations (3 passes over the first 8192 elements), oracle NumPy port "
+                         f"of the reference algorithm, {secs:.1f} s"}  # fmt: skip
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "elem/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": mixed["ms"],
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64 residual/state/return map + f32 tangent (mixed)",
+        "data": "synthetic",
+        "config": {
+            "workload": f"C3D8 von Mises J2 {args.n}^3 unit cube (jitter 5%), plastic increment, one element pass",
+            "elements": nEl,
+            "dofs": nDof,
+            "nnz": mixed["nnz"],
+            "l2": "inputs larger than L2 (state 218 MB, CSR data 259 MB)",
+            "parallelism": f"replicas x{world}",
+        },
+        "fp64": {"value": world * nEl / (fp64["ms"] * 1e-3), "ms_per_step": fp64["ms"], "kernel_ms": fp64["kernel_ms"]},
+        "mixed_over_fp64": fp64["ms"] / mixed["ms"],
+        "errors": errs,
+        "roofline": {
+            "bound": "hbm",
+            "achieved": achieved,
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": achieved / peak,
+            "traffic": traffic,
+            "peak_kind": peak_kind,
+            "algorithmic_bytes_per_launch": abytes,
+            "kernel_ms": mixed["kernel_ms"],
+        },
+        "cpu_baseline": cpu,
+        "e2e": {
+            "value": world * nEl / (e2e["ms"] * 1e-3),
+            "unit": "elem/s",
+            "h2d_bytes_per_step": e2e["h2d"],
+            "d2h_bytes_per_step": e2e["d2h"],
+            "ms_per_step": e2e["ms"],
+        },
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

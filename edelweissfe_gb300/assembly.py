@@ -59,7 +59,10 @@ class GPUAssembler:
         self.lib = L.load()
         if not torch.cuda.is_available():
             raise RuntimeError("GPUAssembler needs a CUDA device (there is no CPU fallback)")
-        self.device = torch.device(device or "cuda")
+        dev = torch.device(device or "cuda")
+        if dev.index is None:
+            dev = torch.device("cuda", torch.cuda.current_device())
+        self.device = dev
         coords = np.ascontiguousarray(coords, np.float64)
         self.dim = coords.shape[1]
         self.nNodes = coords.shape[0]
@@ -126,8 +129,8 @@ class GPUAssembler:
         d["type"] = et
         d["conn"] = torch.from_numpy(self._conns_host[self.groups.index(g)]).to(dev)
         d["pairSlot"] = torch.from_numpy(self._slots_host[self.groups.index(g)]).to(dev)
-        d["props"] = torch.from_numpy(np.ascontiguousarray(props)).to(dev)
-        d["thickness"] = torch.from_numpy(np.ascontiguousarray(th)).to(dev)
+        d["props"] = torch.from_numpy(np.array(props, np.float64)).to(dev)
+        d["thickness"] = torch.from_numpy(np.array(th, np.float64)).to(dev)
         d["geomG"] = torch.zeros((et.dim * et.nNodes, nPts), dtype=torch.float64, device=dev)
         d["geomS"] = torch.zeros(nPts, dtype=torch.float64, device=dev)
         d["stateRef"] = torch.zeros((S, nPts), dtype=torch.float64, device=dev)
