@@ -146,7 +146,7 @@ def run_gpu(args, rank, world):
     results = {}
     state = {}
     sampler.start()
-    for precision in ("fp64", "mixed"):
+    for precision in (("fp64", "mixed") if args.precision == "both" else (args.precision,)):
         asm = GPUAssembler(coords, nodeDof, nDof, [ElementGroup("C3D8", "vonmises", VM, conn)], precision=precision,
                            device=dev)  # fmt: skip
         P, F, K = asm.constructDofVector(), asm.constructDofVector(), asm.constructSystemMatrix()
@@ -196,6 +196,8 @@ def run_gpu(args, rank, world):
             results["e2e"] = run_e2e(asm, dU1 + dU2, dU2, args, dev)
         del P, F, K
     clocks = sampler.stop()
+    if len(state) < 2:
+        return results, {}, clocks, nEl, nDof, len(coords)
     errs = {
         "R_rel_mixed_vs_fp64": float((state["mixed"]["P"] - state["fp64"]["P"]).abs().max()
                                      / state["fp64"]["P"].abs().max()),
@@ -332,6 +334,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_CUBE, help="elements per cube edge")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64"],
+                    help="profiling aid: run one mode only (the JSON line needs both)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -345,6 +349,11 @@ def main():
         torch.distributed.init_process_group("nccl")
     results, errs, clocks, nEl, nDof, nNodes = run_gpu(args, rank, world)
     if rank != 0:
+        return
+    if args.precision != "both":
+        r = results[args.precision]
+        print(json.dumps({"precision": args.precision, "ms_per_step": r["ms"], "kernel_ms": r["kernel_ms"],
+                          "elem_per_s": nEl / (r["ms"] * 1e-3)}))
         return
     mixed, fp64, e2e = results["mixed"], results["fp64"], results["e2e"]
     value = world * nEl / (mixed["ms"] * 1e-3)

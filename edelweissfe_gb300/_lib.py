@@ -64,6 +64,7 @@ class EfeGroup(ctypes.Structure):
         ("props", ctypes.c_void_p),
         ("thickness", ctypes.c_void_p),
         ("geomG", ctypes.c_void_p),
+        ("geomG32", ctypes.c_void_p),
         ("geomS", ctypes.c_void_p),
         ("stateRef", ctypes.c_void_p),
         ("stateTemp", ctypes.c_void_p),

@@ -30,6 +30,11 @@ from .exceptions import CutbackRequest
 from .pattern import build_pattern
 
 
+def _upload(a, dtype, dev):
+    """Row-major (C-contiguous) device copy of a host array: the C ABI indexes raw pointers."""
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=dtype)).to(dev).contiguous()
+
+
 @dataclass
 class ElementGroup:
     """Elements of one type and material (a section, `sections/base/sectionbase.py:86-108`).
@@ -74,11 +79,11 @@ class GPUAssembler:
         self.kdtype = torch.float64 if precision == "fp64" else torch.float32
         self._build_pattern()
         dev = self.device
-        self.coords = torch.from_numpy(coords).to(dev)
-        self.nodeDof = torch.from_numpy(self.nodeDof_host).to(dev)
-        self.nodeRowLen = torch.from_numpy(self.nodeRowLen_host).to(dev)
-        self.indptr = torch.from_numpy(self.indptr_host).to(dev)
-        self.indices = torch.from_numpy(self.indices_host).to(dev)
+        self.coords = _upload(coords, np.float64, dev)
+        self.nodeDof = _upload(self.nodeDof_host, np.int32, dev)
+        self.nodeRowLen = _upload(self.nodeRowLen_host, np.int32, dev)
+        self.indptr = _upload(self.indptr_host, np.int32, dev)
+        self.indices = _upload(self.indices_host, np.int32, dev)
         self.status = torch.zeros(4, dtype=torch.int32, device=dev)
         self.mesh = L.EfeMesh(
             self.dim, self.nNodes, self.nDof, self.nnz, self.coords.data_ptr(), self.nodeDof.data_ptr(),
@@ -127,11 +132,13 @@ class GPUAssembler:
         S = 12 + nm
         d = g._dev
         d["type"] = et
-        d["conn"] = torch.from_numpy(self._conns_host[self.groups.index(g)]).to(dev)
-        d["pairSlot"] = torch.from_numpy(self._slots_host[self.groups.index(g)]).to(dev)
-        d["props"] = torch.from_numpy(np.array(props, np.float64)).to(dev)
-        d["thickness"] = torch.from_numpy(np.array(th, np.float64)).to(dev)
+        d["conn"] = _upload(self._conns_host[self.groups.index(g)], np.int32, dev)
+        d["pairSlot"] = _upload(self._slots_host[self.groups.index(g)], np.int32, dev)
+        d["props"] = _upload(props, np.float64, dev)
+        d["thickness"] = _upload(th, np.float64, dev)
         d["geomG"] = torch.zeros((et.dim * et.nNodes, nPts), dtype=torch.float64, device=dev)
+        if self.kPrecision == L.EFE_K_FP32:
+            d["geomG32"] = torch.zeros((et.dim * et.nNodes, nPts), dtype=torch.float32, device=dev)
         d["geomS"] = torch.zeros(nPts, dtype=torch.float64, device=dev)
         d["stateRef"] = torch.zeros((S, nPts), dtype=torch.float64, device=dev)
         d["stateTemp"] = torch.zeros((S, nPts), dtype=torch.float64, device=dev)
@@ -139,11 +146,14 @@ class GPUAssembler:
             d["auxRef"] = torch.zeros((6, nPts), dtype=torch.float64, device=dev)
             d["auxTemp"] = torch.zeros((6, nPts), dtype=torch.float64, device=dev)
         d["offset"] = offset
+        for key, t in d.items():
+            if isinstance(t, torch.Tensor) and not t.is_contiguous():
+                raise AssertionError(f"{key} must be contiguous for the C ABI")
         return L.EfeGroup(
             et.shape, et.rule, et.kinematics, et.plane, mcode, props.shape[1], E, offset,
             d["conn"].data_ptr(), d["pairSlot"].data_ptr(), d["props"].data_ptr(),
             d["thickness"].data_ptr() if et.dim == 2 else None,
-            d["geomG"].data_ptr(), d["geomS"].data_ptr(), d["stateRef"].data_ptr(), d["stateTemp"].data_ptr(),
+            d["geomG"].data_ptr(), d["geomG32"].data_ptr() if "geomG32" in d else None, d["geomS"].data_ptr(), d["stateRef"].data_ptr(), d["stateTemp"].data_ptr(),
             d["auxRef"].data_ptr() if et.totalLagrangian else None,
             d["auxTemp"].data_ptr() if et.totalLagrangian else None,
         )  # fmt: skip

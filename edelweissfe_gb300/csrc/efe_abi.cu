@@ -219,19 +219,19 @@ int32_t efe_setup_geometry(const EfeMesh* mesh, const EfeGroup* g, int32_t* stat
   switch (g->shape) {
     case EFE_QUAD4:
       e = efe::geometry_quad4(g->rule, g->nElements, g->elementOffset, g->conn, mesh->coords, g->thickness, g->geomG,
-                              g->geomS, status, fix, st);
+                              g->geomG32, g->geomS, status, fix, st);
       break;
     case EFE_QUAD8:
       e = efe::geometry_quad8(g->rule, g->nElements, g->elementOffset, g->conn, mesh->coords, g->thickness, g->geomG,
-                              g->geomS, status, fix, st);
+                              g->geomG32, g->geomS, status, fix, st);
       break;
     case EFE_HEXA8:
       e = efe::geometry_hexa8(g->rule, g->nElements, g->elementOffset, g->conn, mesh->coords, nullptr, g->geomG,
-                              g->geomS, status, fix, st);
+                              g->geomG32, g->geomS, status, fix, st);
       break;
     case EFE_HEXA20:
       e = efe::geometry_hexa20(g->rule, g->nElements, g->elementOffset, g->conn, mesh->coords, nullptr, g->geomG,
-                               g->geomS, status, fix, st);
+                               g->geomG32, g->geomS, status, fix, st);
       break;
   }
   if (e != cudaSuccess) return cuda_fail(e, "efe_setup_geometry");
@@ -266,6 +266,7 @@ int32_t efe_compute_elements(const EfeMesh* mesh, const EfeGroup* groups, int32_
     a.props = gr.props;
     a.thickness = gr.thickness;
     a.geomG = gr.geomG;
+    a.geomG32 = gr.geomG32;
     a.geomS = gr.geomS;
     a.stateRef = gr.stateRef;
     a.stateTemp = gr.stateTemp;

@@ -210,11 +210,33 @@ __device__ __forceinline__ double tangent3_entry(const Tangent3& T, int i, int j
   return v - T.a * T.n[i] * T.n[j];
 }
 
+// Per-element constants of the von Mises / linear-elastic 3D update, formed once per element.
+struct VMConst {
+  Iso Ei;
+  double G, fy0, H, dfy, delta;
+};
+__device__ __forceinline__ VMConst vm_const(const double* props, bool vonMises) {
+  VMConst c;
+  c.Ei = iso3d(props[0], props[1]);
+  c.G = props[0] / (2.0 * (1.0 + props[1]));
+  c.fy0 = vonMises ? props[2] : 0.0;
+  c.H = vonMises ? props[3] : 0.0;
+  c.dfy = vonMises ? props[4] : 0.0;
+  c.delta = vonMises ? props[5] : 0.0;
+  return c;
+}
+// dfy * (1 - exp(-delta k)); identical to the reference's expression, and exactly 0 when dfy == 0
+__device__ __forceinline__ double vm_sat(const VMConst& c, double k) {
+  return c.dfy == 0.0 ? 0.0 : c.dfy * (1.0 - exp(-c.delta * k));
+}
+__device__ __forceinline__ double vm_dsat(const VMConst& c, double k) {
+  return c.dfy == 0.0 ? 0.0 : c.dfy * c.delta * exp(-c.delta * k);
+}
+
 // von Mises radial return (vonmises.py:186-254).  Updates sig and kappa in place.
 // Returns false when the scalar Newton does not converge in 15 iterations (CutbackRequest).
-__device__ inline bool von_mises_3d(const double* props, double sig[6], const double de[6], double& kappa, Tangent3& T) {
-  const double E = props[0], v = props[1], fy0 = props[2], H = props[3], dfy = props[4], delta = props[5];
-  const Iso Ei = iso3d(E, v);
+__device__ inline bool von_mises_3d(const VMConst& c, double sig[6], const double de[6], double& kappa, Tangent3& T) {
+  const Iso& Ei = c.Ei;
   T.c11 = Ei.c11;
   T.c12 = Ei.c12;
   T.c44 = Ei.c44;
@@ -223,14 +245,15 @@ __device__ inline bool von_mises_3d(const double* props, double sig[6], const do
   double nrm = 0.0;
   for (int i = 0; i < 6; ++i) nrm += de[i] * de[i];
   if (sqrt(nrm) < 1e-14) return true;  // zero increment: C = Ei (:211-213)
-  const double G = E / (2.0 * (1.0 + v));
+  const double G = c.G;
   double tr[6], ds[6];
   iso_apply(Ei, de, ds);
   for (int i = 0; i < 6; ++i) tr[i] = sig[i] + ds[i];
   double dev[6];
-  dev[0] = 2.0 / 3.0 * tr[0] - 1.0 / 3.0 * tr[1] - 1.0 / 3.0 * tr[2];
-  dev[1] = -1.0 / 3.0 * tr[0] + 2.0 / 3.0 * tr[1] - 1.0 / 3.0 * tr[2];
-  dev[2] = -1.0 / 3.0 * tr[0] - 1.0 / 3.0 * tr[1] + 2.0 / 3.0 * tr[2];
+  const double mean = (tr[0] + tr[1] + tr[2]) * (1.0 / 3.0);
+  dev[0] = tr[0] - mean;
+  dev[1] = tr[1] - mean;
+  dev[2] = tr[2] - mean;
   dev[3] = tr[3];
   dev[4] = tr[4];
   dev[5] = tr[5];
@@ -238,33 +261,34 @@ __device__ inline bool von_mises_3d(const double* props, double sig[6], const do
       sqrt(dev[0] * dev[0] + dev[1] * dev[1] + dev[2] * dev[2] + 2.0 * (dev[3] * dev[3] + dev[4] * dev[4] + dev[5] * dev[5]));
   const double k0 = kappa;
   const double sq23 = sqrt(2.0 / 3.0), sq6 = sqrt(6.0);
-  const double fy_k0 = fy0 + H * k0 + dfy * (1.0 - exp(-delta * k0));
+  const double fy_k0 = c.fy0 + c.H * k0 + vm_sat(c, k0);
   if (devNorm - sq23 * fy_k0 > 0.0) {
     double dK = 0.0;
     int counter = 0;
     bool ok = true;
     while (true) {
       const double k = k0 + dK;
-      const double R = devNorm - sq6 * G * dK - sq23 * (fy0 + H * k + dfy * (1.0 - exp(-delta * k)));
+      const double R = devNorm - sq6 * G * dK - sq23 * (c.fy0 + c.H * k + vm_sat(c, k));
       if (!(fabs(R) > 1e-12)) break;
       if (counter == 15) {
         ok = false;
         break;
       }
-      const double dR = -sq6 * G - sq23 * (H + dfy * delta * exp(-delta * k));
+      const double dR = -sq6 * G - sq23 * (c.H + vm_dsat(c, k));
       dK -= R / dR;
       ++counter;
     }
     const double dLambda = sqrt(1.5) * dK;
     kappa = k0 + dK;
     const double inv = 1.0 / devNorm;
+    const double g2 = 2.0 * G * dLambda;
     for (int i = 0; i < 6; ++i) {
       T.n[i] = dev[i] * inv;
-      sig[i] = tr[i] - 2.0 * G * dLambda * T.n[i];
+      sig[i] = tr[i] - g2 * T.n[i];
     }
-    const double dfyk = H + dfy * delta * exp(-delta * kappa);
-    const double beta = 4.0 * G * G * dLambda / devNorm;  // coefficient of IDevHalfShear
-    T.a = 2.0 * G * (1.0 / (1.0 + dfyk / (3.0 * G)) - 2.0 * G * dLambda / devNorm);
+    const double dfyk = c.H + vm_dsat(c, kappa);
+    const double beta = 2.0 * G * g2 * inv;  // 4 G^2 dLambda / devNorm, coefficient of IDevHalfShear
+    T.a = 2.0 * G * (1.0 / (1.0 + dfyk / (3.0 * G)) - g2 * inv);
     T.c11 = Ei.c11 - beta * (2.0 / 3.0);
     T.c12 = Ei.c12 + beta * (1.0 / 3.0);
     T.c44 = Ei.c44 - beta * 0.5;
@@ -274,15 +298,13 @@ __device__ inline bool von_mises_3d(const double* props, double sig[6], const do
   return true;
 }
 
-__device__ __forceinline__ void linear_elastic_3d(const double* props, double sig[6], const double de[6],
-                                                  Tangent3& T) {
-  const Iso Ei = iso3d(props[0], props[1]);
+__device__ __forceinline__ void linear_elastic_3d(const VMConst& c, double sig[6], const double de[6], Tangent3& T) {
   double ds[6];
-  iso_apply(Ei, de, ds);
+  iso_apply(c.Ei, de, ds);
   for (int i = 0; i < 6; ++i) sig[i] += ds[i];
-  T.c11 = Ei.c11;
-  T.c12 = Ei.c12;
-  T.c44 = Ei.c44;
+  T.c11 = c.Ei.c11;
+  T.c12 = c.Ei.c12;
+  T.c44 = c.Ei.c44;
   T.a = 0.0;
   for (int i = 0; i < 6; ++i) T.n[i] = 0.0;
 }
@@ -321,7 +343,7 @@ __device__ __forceinline__ void linear_elastic_plane_stress(const double* props,
 // local Newton on de[2]; every local step calls the 3D update with a zero stress vector and the
 // material state, so kappa accumulates the plastic increments of all local steps; the converged
 // 3D stress is added to sig.  Returns false on a cutback request.
-__device__ inline bool von_mises_plane_stress(const double* props, double sig[6], double de[6], double& kappa, Tangent2& C) {
+__device__ inline bool von_mises_plane_stress(const VMConst& vc, double sig[6], double de[6], double& kappa, Tangent2& C) {
   Tangent3 T;
   double s3[6];
   de[2] = -de[0] - de[1];
@@ -329,7 +351,7 @@ __device__ inline bool von_mises_plane_stress(const double* props, double sig[6]
   bool ok = true;
   while (true) {
     for (int i = 0; i < 6; ++i) s3[i] = 0.0;
-    if (!von_mises_3d(props, s3, de, kappa, T)) {
+    if (!von_mises_3d(vc, s3, de, kappa, T)) {
       ok = false;
       break;
     }

@@ -13,6 +13,8 @@
 //      (CSRGenerator.updateCSR, csrgenerator.pyx:100-115, without the VIJ vector).
 // KT is the type of the tangent (double, or float in the mixed mode).
 #pragma once
+#include <type_traits>
+
 #include "efe_device.cuh"
 
 namespace efe {
@@ -24,6 +26,7 @@ struct GroupArgs {
   const double* props;
   const double* thickness;
   const double* geomG;
+  const float* geomG32;  // optional FP32 copy of geomG, used for the FP32 tangent
   const double* geomS;
   const double* stateRef;
   double* stateTemp;
@@ -57,7 +60,8 @@ __device__ __forceinline__ void report(int32_t* status, int bits, int64_t global
 template <int SHAPE, int RULE>
 __global__ void geometry_kernel(int64_t nEl, int64_t elOffset, const int32_t* __restrict__ conn,
                                 const double* __restrict__ coords, const double* __restrict__ thickness,
-                                double* __restrict__ G, double* __restrict__ S, int32_t* status, Hexa20Fix fix) {
+                                double* __restrict__ G, float* __restrict__ G32, double* __restrict__ S,
+                                int32_t* status, Hexa20Fix fix) {
   constexpr int DIM = ShapeInfo<SHAPE>::DIM, NN = ShapeInfo<SHAPE>::NN, NQ = RuleInfo<RULE>::NQ;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nEl * NQ) return;
@@ -106,6 +110,7 @@ __global__ void geometry_kernel(int64_t nEl, int64_t elOffset, const int32_t* __
       double s = 0.0;
       for (int r = 0; r < DIM; ++r) s += iJ[c][r] * dN[r][a];
       G[(int64_t)(c * NN + a) * stride + t] = s;
+      if (G32) G32[(int64_t)(c * NN + a) * stride + t] = (float)s;
     }
   const double th = (DIM == 2 && thickness) ? thickness[e] : 1.0;
   S[t] = detJ * w * th;
@@ -130,7 +135,8 @@ struct Layout {
   static constexpr size_t r_off = u_off + sizeof(double) * EPB * NDOF;            // double [EPB][NQ][NDOF]
   static constexpr size_t sc_off = r_off + sizeof(double) * EPB * NQ * NDOF;      // KT [EPB][NQ][NSCAL]
   static constexpr size_t v_off = sc_off + sizeof(KT) * EPB * NQ * NSCAL;         // KT [EPB][NQ][NN][NVEC][DIM]
-  static constexpr size_t rl_off = v_off + sizeof(KT) * EPB * NQ * NN * NVEC * DIM;  // int [EPB][NN]
+  static constexpr size_t mc_off = (v_off + sizeof(KT) * EPB * NQ * NN * NVEC * DIM + 15) / 16 * 16;  // VMConst [EPB]
+  static constexpr size_t rl_off = mc_off + sizeof(VMConst) * EPB;                                     // int [EPB][NN]
   static constexpr size_t bytes = rl_off + sizeof(int) * EPB * NN;
 };
 
@@ -139,8 +145,8 @@ __device__ __forceinline__ void kadd(KT* p, KT v) {
   atomicAdd(p, v);
 }
 
-template <int SHAPE, int RULE, int FORM, typename KT, int EPB, int NT>
-__global__ void __launch_bounds__(NT) assemble_kernel(GroupArgs g) {
+template <int SHAPE, int RULE, int FORM, typename KT, int EPB, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) assemble_kernel(GroupArgs g) {
   using L = Layout<SHAPE, RULE, FORM, KT, EPB>;
   constexpr int DIM = L::DIM, NN = L::NN, NQ = L::NQ, NVEC = L::NVEC, NSCAL = L::NSCAL, NDOF = L::NDOF;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -149,6 +155,7 @@ __global__ void __launch_bounds__(NT) assemble_kernel(GroupArgs g) {
   KT* ssc = reinterpret_cast<KT*>(smem + L::sc_off);
   KT* sv = reinterpret_cast<KT*>(smem + L::v_off);
   int* srl = reinterpret_cast<int*>(smem + L::rl_off);
+  VMConst* smc = reinterpret_cast<VMConst*>(smem + L::mc_off);
 
   const int64_t e0 = (int64_t)blockIdx.x * EPB;
   const int64_t nEl = g.nElements;
@@ -164,6 +171,13 @@ __global__ void __launch_bounds__(NT) assemble_kernel(GroupArgs g) {
       const int32_t dof = g.nodeDof[node];
       for (int c = 0; c < DIM; ++c) su[(le * NN + a) * DIM + c] = Ux[dof + c];
       srl[le * NN + a] = g.nodeRowLen[node];
+    }
+  }
+  // per-element material constants, formed once per element instead of once per point
+  if constexpr (FORM != TLH) {
+    for (int le = threadIdx.x; le < EPB; le += NT) {
+      const int64_t e = e0 + le;
+      if (e < nEl) smc[le] = vm_const(g.props + e * g.nProps, g.material == EFE_MAT_VON_MISES);
     }
   }
   __syncthreads();
@@ -221,43 +235,56 @@ __global__ void __launch_bounds__(NT) assemble_kernel(GroupArgs g) {
       if constexpr (FORM == SS3) {
         Tangent3 T;
         if (g.material == EFE_MAT_VON_MISES)
-          ok = von_mises_3d(props, sig, de, kappa, T);
+          ok = von_mises_3d(smc[le], sig, de, kappa, T);
         else
-          linear_elastic_3d(props, sig, de, T);
+          linear_elastic_3d(smc[le], sig, de, T);
         // residual r_a = s * sigma . G_a   (small-strain Voigt order 11,22,33,12,13,23)
+        double ss[6];
+        for (int f = 0; f < 6; ++f) ss[f] = sig[f] * s;
         for (int a = 0; a < NN; ++a) {
           const double gx = Gm[0][a], gy = Gm[1][a], gz = Gm[2 % DIM][a];
-          rq[a * DIM + 0] = (sig[0] * gx + sig[3] * gy + sig[4] * gz) * s;
-          rq[a * DIM + 1] = (sig[3] * gx + sig[1] * gy + sig[5] * gz) * s;
-          rq[a * DIM + 2 % DIM] = (sig[4] * gx + sig[5] * gy + sig[2] * gz) * s;
+          rq[a * DIM + 0] = ss[0] * gx + ss[3] * gy + ss[4] * gz;
+          rq[a * DIM + 1] = ss[3] * gx + ss[1] * gy + ss[5] * gz;
+          rq[a * DIM + 2 % DIM] = ss[4] * gx + ss[5] * gy + ss[2] * gz;
         }
         sc[0] = (KT)(T.c12 * s);
         sc[1] = (KT)(T.c44 * s);
         sc[2] = (KT)(T.a * s);
-        const double* n = T.n;
+        // tangent vectors G_a and n.G_a in the tangent's precision (FP32 copy of G when present)
+        KT n[6];
+        for (int f = 0; f < 6; ++f) n[f] = (KT)T.n[f];
         for (int a = 0; a < NN; ++a) {
-          const double gx = Gm[0][a], gy = Gm[1][a], gz = Gm[2 % DIM][a];
+          KT gx, gy, gz;
+          if (std::is_same<KT, float>::value && g.geomG32) {
+            gx = (KT)g.geomG32[(int64_t)(0 * NN + a) * stride + pt];
+            gy = (KT)g.geomG32[(int64_t)(1 * NN + a) * stride + pt];
+            gz = (KT)g.geomG32[(int64_t)(2 * NN + a) * stride + pt];
+          } else {
+            gx = (KT)Gm[0][a];
+            gy = (KT)Gm[1][a];
+            gz = (KT)Gm[2 % DIM][a];
+          }
           KT* v = vq + a * NVEC * DIM;
-          v[0] = (KT)gx;
-          v[1] = (KT)gy;
-          v[2 % DIM] = (KT)gz;
-          v[DIM + 0] = (KT)(n[0] * gx + n[3] * gy + n[4] * gz);
-          v[DIM + 1] = (KT)(n[3] * gx + n[1] * gy + n[5] * gz);
-          v[DIM + 2 % DIM] = (KT)(n[4] * gx + n[5] * gy + n[2] * gz);
+          v[0] = gx;
+          v[1] = gy;
+          v[2 % DIM] = gz;
+          v[DIM + 0] = n[0] * gx + n[3] * gy + n[4] * gz;
+          v[DIM + 1] = n[3] * gx + n[1] * gy + n[5] * gz;
+          v[DIM + 2 % DIM] = n[4] * gx + n[5] * gy + n[2] * gz;
         }
       } else {
         Tangent2 C;
         if (g.plane == EFE_PLANE_STRESS) {
           if (g.material == EFE_MAT_VON_MISES)
-            ok = von_mises_plane_stress(props, sig, de, kappa, C);
+            ok = von_mises_plane_stress(smc[le], sig, de, kappa, C);
           else
             linear_elastic_plane_stress(props, sig, de, C);
         } else {
           Tangent3 T;
           if (g.material == EFE_MAT_VON_MISES)
-            ok = von_mises_3d(props, sig, de, kappa, T);
+            ok = von_mises_3d(smc[le], sig, de, kappa, T);
           else
-            linear_elastic_3d(props, sig, de, T);
+            linear_elastic_3d(smc[le], sig, de, T);
           tangent2_from3(T, C);
         }
         for (int a = 0; a < NN; ++a) {
@@ -375,9 +402,9 @@ __global__ void __launch_bounds__(NT) assemble_kernel(GroupArgs g) {
         if constexpr (FORM == TLV3) {
           Tangent3 T;
           if (g.material == EFE_MAT_VON_MISES)
-            ok = von_mises_3d(props, sig, de, kappa, T);
+            ok = von_mises_3d(smc[le], sig, de, kappa, T);
           else
-            linear_elastic_3d(props, sig, de, T);
+            linear_elastic_3d(smc[le], sig, de, T);
           // TL Voigt order 11,22,33,12,23,13
           const double Sm[3][3] = {{sig[0], sig[3], sig[5]}, {sig[3], sig[1], sig[4]}, {sig[5], sig[4], sig[2]}};
           const double Nm[3][3] = {{T.n[0], T.n[3], T.n[5]}, {T.n[3], T.n[1], T.n[4]}, {T.n[5], T.n[4], T.n[2]}};
@@ -407,15 +434,15 @@ __global__ void __launch_bounds__(NT) assemble_kernel(GroupArgs g) {
           Tangent2 C;
           if (g.plane == EFE_PLANE_STRESS) {
             if (g.material == EFE_MAT_VON_MISES)
-              ok = von_mises_plane_stress(props, sig, de, kappa, C);
+              ok = von_mises_plane_stress(smc[le], sig, de, kappa, C);
             else
               linear_elastic_plane_stress(props, sig, de, C);
           } else {
             Tangent3 T;
             if (g.material == EFE_MAT_VON_MISES)
-              ok = von_mises_3d(props, sig, de, kappa, T);
+              ok = von_mises_3d(smc[le], sig, de, kappa, T);
             else
-              linear_elastic_3d(props, sig, de, T);
+              linear_elastic_3d(smc[le], sig, de, T);
             tangent2_from3(T, C);
           }
           // stress entering P: indices [0,1,3] (plane strain) or [0,1,2] (plane stress, :278-281);
@@ -472,9 +499,17 @@ __global__ void __launch_bounds__(NT) assemble_kernel(GroupArgs g) {
 
   // ---- phase B: tangent blocks
   KT* K = reinterpret_cast<KT*>(g.Kdata);
-  for (int t = threadIdx.x; t < EPB * NN * NN; t += NT) {
-    const int le = t / (NN * NN), ab = t % (NN * NN);
-    const int a = ab / NN, b = ab % NN;
+  // the element tangents are symmetric (K_ab[j][k] = K_ba[k][j]): evaluate the pairs a <= b and
+  // scatter each block twice
+  constexpr int NPAIR = NN * (NN + 1) / 2;
+  for (int t = threadIdx.x; t < EPB * NPAIR; t += NT) {
+    const int le = t / NPAIR;
+    int r = t % NPAIR, a = 0;
+    while (r >= NN - a) {
+      r -= NN - a;
+      ++a;
+    }
+    const int b = a + r;
     const int64_t e = e0 + le;
     if (e >= nEl) continue;
     KT acc[DIM][DIM];
@@ -577,6 +612,14 @@ __global__ void __launch_bounds__(NT) assemble_kernel(GroupArgs g) {
     for (int j = 0; j < DIM; ++j)
 #pragma unroll
       for (int k = 0; k < DIM; ++k) kadd(K + slot + (int64_t)k * rl + j, acc[j][k]);
+    if (a != b) {  // Ke[(b,k),(a,j)] = Ke[(a,j),(b,k)] -> (row = dof(a,j), col = dof(b,k))
+      const int32_t slot2 = g.pairSlot[(e * NN + b) * NN + a];
+      const int rl2 = srl[le * NN + a];
+#pragma unroll
+      for (int j = 0; j < DIM; ++j)
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) kadd(K + slot2 + (int64_t)j * rl2 + k, acc[j][k]);
+    }
   }
 }
 

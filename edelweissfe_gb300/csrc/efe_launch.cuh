@@ -4,22 +4,26 @@
 
 namespace efe {
 
-// Elements per CTA: as many as fit in ~96 KB of shared memory (two CTAs per SM fit in 228 KB),
-// capped at 32.
+// Elements per CTA: about 128 material points per CTA (one per thread in phase A), limited to
+// 72 KB of shared memory so that three CTAs can share an SM.
 template <int SHAPE, int RULE, int FORM, typename KT>
 struct Tile {
+  static constexpr int NQ = RuleInfo<RULE>::NQ;
   static constexpr size_t per_element = Layout<SHAPE, RULE, FORM, KT, 1>::bytes;
-  static constexpr int fit = (int)((96 * 1024) / per_element);
-  static constexpr int EPB = fit < 1 ? 1 : (fit > 32 ? 32 : fit);
-  static constexpr int NT = (EPB * RuleInfo<RULE>::NQ >= 192) ? 256 : 128;
+  static constexpr int fit = (int)((72 * 1024) / per_element);
+  static constexpr int want = (128 + NQ - 1) / NQ;
+  static constexpr int e0 = fit < want ? fit : want;
+  static constexpr int EPB = e0 < 1 ? 1 : (e0 > 32 ? 32 : e0);
+  static constexpr int NT = 128;
   static constexpr size_t bytes = Layout<SHAPE, RULE, FORM, KT, EPB>::bytes;
+  static constexpr int MINB = bytes <= 72 * 1024 ? 3 : 1;
 };
 
 template <int SHAPE, int RULE, int FORM, typename KT>
 cudaError_t launch_assemble(const GroupArgs& g, cudaStream_t st) {
   using T = Tile<SHAPE, RULE, FORM, KT>;
   static_assert(T::bytes <= 200 * 1024, "tile does not fit in shared memory");
-  auto kern = assemble_kernel<SHAPE, RULE, FORM, KT, T::EPB, T::NT>;
+  auto kern = assemble_kernel<SHAPE, RULE, FORM, KT, T::EPB, T::NT, T::MINB>;
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::bytes);
   if (err != cudaSuccess) return err;
   const int64_t grid = (g.nElements + T::EPB - 1) / T::EPB;
@@ -30,13 +34,13 @@ cudaError_t launch_assemble(const GroupArgs& g, cudaStream_t st) {
 
 template <int SHAPE, int RULE>
 cudaError_t launch_geometry(int64_t nEl, int64_t elOffset, const int32_t* conn, const double* coords,
-                            const double* thickness, double* G, double* S, int32_t* status, const Hexa20Fix& fix,
-                            cudaStream_t st) {
+                            const double* thickness, double* G, float* G32, double* S, int32_t* status,
+                            const Hexa20Fix& fix, cudaStream_t st) {
   const int64_t n = nEl * RuleInfo<RULE>::NQ;
   if (n == 0) return cudaSuccess;
   const int nt = 128;
   geometry_kernel<SHAPE, RULE><<<(unsigned)((n + nt - 1) / nt), nt, 0, st>>>(nEl, elOffset, conn, coords, thickness,
-                                                                             G, S, status, fix);
+                                                                             G, G32, S, status, fix);
   return cudaGetLastError();
 }
 
@@ -73,8 +77,8 @@ cudaError_t assemble_hexa8(int rule, int form, int kprec, const GroupArgs& g, cu
 cudaError_t assemble_hexa20(int rule, int form, int kprec, const GroupArgs& g, cudaStream_t st);
 #define EFE_GEOMETRY_DECL(name)                                                                          \
   cudaError_t geometry_##name(int rule, int64_t nEl, int64_t off, const int32_t* conn, const double* coords, \
-                              const double* th, double* G, double* S, int32_t* status, const Hexa20Fix& fix,  \
-                              cudaStream_t st);
+                              const double* th, double* G, float* G32, double* S, int32_t* status,            \
+                              const Hexa20Fix& fix, cudaStream_t st);
 EFE_GEOMETRY_DECL(quad4)
 EFE_GEOMETRY_DECL(quad8)
 EFE_GEOMETRY_DECL(hexa8)

@@ -111,6 +111,8 @@ typedef struct EfeGroup {
   const double* props;       /* [nElements][nProps] material properties per element          */
   const double* thickness;   /* [nElements] (2D); NULL for solids                            */
   double* geomG;             /* [dim*nNodes][nElements*nInt]  dN_a/dX_c at row c*nNodes+a    */
+  float* geomG32;            /* optional FP32 copy of geomG (same layout), read by the FP32
+                                tangent of EFE_K_FP32; NULL to convert geomG on the fly      */
   double* geomS;             /* [nElements*nInt]  det J * weight * thickness                 */
   double* stateRef;          /* [12 + nMatState][nElements*nInt]  stress(6) strain(6) material;
                                 read by efe_compute_elements, written by efe_accept_state      */

@@ -76,3 +76,20 @@ def test_csr_output_matches_scipy_layout():
     assert At.layout == torch.sparse_csr
     y = (At @ U.unsqueeze(1)).squeeze(1).cpu().numpy()
     assert _rel(y, A @ call["U"]) <= 1e-12
+
+
+def test_shared_properties_many_elements():
+    """One property vector shared by all elements (a section without fields) on a multi-CTA mesh."""
+    case = gc.load("cfg2_c3d8_vm_3cube")
+    assert np.all(case["props"] == case["props"][0])
+    case = dict(case)
+    case["props"] = case["props"][0]
+    asm = _assembler(case, "fp64")
+    for call in gc.calls(case):
+        if call["accept_before"]:
+            asm.acceptLastState()
+        P, F, K = asm.constructDofVector(), asm.constructDofVector(), asm.constructSystemMatrix()
+        asm.computeElements(None, torch.tensor(call["U"], device=asm.device),
+                            torch.tensor(call["dU"], device=asm.device), P, K, F)  # fmt: skip
+        assert _rel(P.cpu().numpy(), call["P"]) <= RTOL
+        assert _rel(asm.group_state(0), call["state"]) <= RTOL
