@@ -32,6 +32,7 @@ EXPORTS = [
     "efe_setup_geometry",
     "efe_compute_elements",
     "efe_accept_state",
+    "efe_body_force",
     "efe_pattern_count",
     "efe_pattern_fill",
 ]
@@ -123,6 +124,8 @@ def load(build_if_missing=False):
         P,
         P,
     ]
+    lib.efe_body_force.restype = i32
+    lib.efe_body_force.argtypes = [ctypes.POINTER(EfeMesh), ctypes.POINTER(EfeGroup), P, i64, P, P, P]
     lib.efe_accept_state.restype = i32
     lib.efe_accept_state.argtypes = [ctypes.POINTER(EfeGroup), i32, P]
     lib.efe_pattern_count.restype = i64

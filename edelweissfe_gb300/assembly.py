@@ -253,6 +253,32 @@ class GPUAssembler:
             )
         return torch.sparse_csr_tensor(self.indptr, self.indices, K, size=(self.nDof, self.nDof))
 
+    def computeBodyForce(self, P, force, elements=None):
+        """Add the body force `force` [dim] of the given global element indices (default: all) to P
+        (NIST.computeBodyForces, nonlinearimplicitstatic.py:520-557)."""
+        force = (ctypes.c_double * 3)(*[float(f) for f in list(force)[: self.dim]], *([0.0] * (3 - self.dim)))
+        if elements is not None:
+            elements = np.asarray(elements, np.int64)
+        for i, g in enumerate(self.groups):
+            off, n = g._dev["offset"], len(g.conn)
+            if elements is None:
+                sel, ptr, cnt = None, None, n
+            else:
+                loc = elements[(elements >= off) & (elements < off + n)] - off
+                if len(loc) == 0:
+                    continue
+                sel = _upload(loc, np.int32, self.device)
+                ptr, cnt = ctypes.c_void_p(sel.data_ptr()), len(loc)
+            L.check(
+                self.lib.efe_body_force(
+                    ctypes.byref(self.mesh), ctypes.byref(self._groups_c[i]), ptr, cnt, force,
+                    ctypes.c_void_p(P.data_ptr()), self._stream(),
+                ),
+                "efe_body_force",
+            )
+            del sel
+        return P
+
     # ------------------------------------------------------------------ state
     def acceptLastState(self):
         """acceptLastState of every element (element.py:373-379; TL element.py:454-461)."""

@@ -296,6 +296,25 @@ int32_t efe_compute_elements(const EfeMesh* mesh, const EfeGroup* groups, int32_
   return EFE_OK;
 }
 
+int32_t efe_body_force(const EfeMesh* mesh, const EfeGroup* g, const int32_t* elements, int64_t nSelected,
+                       const double* force, double* P, void* stream) {
+  if (!mesh || !g || !force || !P || nSelected < 0) return fail(EFE_ERR_ARGUMENT, "null argument");
+  int32_t rc = check_group(mesh, *g);
+  if (rc) return rc;
+  if (!elements) nSelected = g->nElements;
+  if (!g->geomS || !g->conn || !mesh->nodeDof) return fail(EFE_ERR_ARGUMENT, "group without geometry");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaErrorInvalidValue;
+  switch (g->shape) {
+    case EFE_QUAD4: e = efe::body_force_quad4(g->rule, nSelected, elements, g->conn, mesh->nodeDof, g->geomS, force, P, st); break;
+    case EFE_QUAD8: e = efe::body_force_quad8(g->rule, nSelected, elements, g->conn, mesh->nodeDof, g->geomS, force, P, st); break;
+    case EFE_HEXA8: e = efe::body_force_hexa8(g->rule, nSelected, elements, g->conn, mesh->nodeDof, g->geomS, force, P, st); break;
+    case EFE_HEXA20: e = efe::body_force_hexa20(g->rule, nSelected, elements, g->conn, mesh->nodeDof, g->geomS, force, P, st); break;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "efe_body_force");
+  return EFE_OK;
+}
+
 int32_t efe_accept_state(const EfeGroup* groups, int32_t nGroups, void* stream) {
   if (!groups || nGroups < 0) return fail(EFE_ERR_ARGUMENT, "null argument");
   cudaStream_t st = (cudaStream_t)stream;

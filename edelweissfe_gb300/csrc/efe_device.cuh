@@ -108,6 +108,33 @@ __device__ void shape_derivatives(const double p[3], double dN[ShapeInfo<SHAPE>:
   }
 }
 
+// N_a at natural point p (computeNOperator, _elementcomputationmatrices.py:106-212)
+template <int SHAPE>
+__device__ void shape_values(const double p[3], double N[ShapeInfo<SHAPE>::NN]) {
+  constexpr int DIM = ShapeInfo<SHAPE>::DIM, NN = ShapeInfo<SHAPE>::NN;
+  constexpr bool quadratic = NN > (1 << DIM);
+  for (int a = 0; a < NN; ++a) {
+    int c[3];
+    node_natural(SHAPE, a, c);
+    int mid = -1;
+    for (int k = 0; k < DIM; ++k)
+      if (c[k] == 0) mid = k;
+    if (!quadratic || mid < 0) {
+      double base = 1.0, s = -(DIM - 1);
+      for (int k = 0; k < DIM; ++k) {
+        base *= 1.0 + c[k] * p[k];
+        s += c[k] * p[k];
+      }
+      N[a] = base / (1 << DIM) * (quadratic ? s : 1.0);
+    } else {
+      double prod = 1.0 - p[mid] * p[mid];
+      for (int k = 0; k < DIM; ++k)
+        if (k != mid) prod *= 1.0 + c[k] * p[k];
+      N[a] = prod / (1 << (DIM - 1));
+    }
+  }
+}
+
 // quadrature point q of a rule: library coordinates (xi, eta, zeta) and weight
 __device__ __forceinline__ void quadrature_point(int rule, int q, double& xi, double& eta, double& zeta, double& w) {
   const double g = 1.0 / sqrt(3.0);
@@ -214,6 +241,7 @@ __device__ __forceinline__ double tangent3_entry(const Tangent3& T, int i, int j
 struct VMConst {
   Iso Ei;
   double G, fy0, H, dfy, delta;
+  double tfac;  // 1 / (1 + H / (3G)): the tangent factor of vonmises.py:247 when dfy == 0
 };
 __device__ __forceinline__ VMConst vm_const(const double* props, bool vonMises) {
   VMConst c;
@@ -223,6 +251,7 @@ __device__ __forceinline__ VMConst vm_const(const double* props, bool vonMises) 
   c.H = vonMises ? props[3] : 0.0;
   c.dfy = vonMises ? props[4] : 0.0;
   c.delta = vonMises ? props[5] : 0.0;
+  c.tfac = 1.0 / (1.0 + c.H / (3.0 * c.G));
   return c;
 }
 // dfy * (1 - exp(-delta k)); identical to the reference's expression, and exactly 0 when dfy == 0
@@ -244,7 +273,7 @@ __device__ inline bool von_mises_3d(const VMConst& c, double sig[6], const doubl
   for (int i = 0; i < 6; ++i) T.n[i] = 0.0;
   double nrm = 0.0;
   for (int i = 0; i < 6; ++i) nrm += de[i] * de[i];
-  if (sqrt(nrm) < 1e-14) return true;  // zero increment: C = Ei (:211-213)
+  if (nrm < 1e-28) return true;  // zero increment, |dStrain| < 1e-14: C = Ei (:211-213)
   const double G = c.G;
   double tr[6], ds[6];
   iso_apply(Ei, de, ds);
@@ -286,9 +315,9 @@ __device__ inline bool von_mises_3d(const VMConst& c, double sig[6], const doubl
       T.n[i] = dev[i] * inv;
       sig[i] = tr[i] - g2 * T.n[i];
     }
-    const double dfyk = c.H + vm_dsat(c, kappa);
+    const double tfac = c.dfy == 0.0 ? c.tfac : 1.0 / (1.0 + (c.H + vm_dsat(c, kappa)) / (3.0 * G));
     const double beta = 2.0 * G * g2 * inv;  // 4 G^2 dLambda / devNorm, coefficient of IDevHalfShear
-    T.a = 2.0 * G * (1.0 / (1.0 + dfyk / (3.0 * G)) - g2 * inv);
+    T.a = 2.0 * G * (tfac - g2 * inv);
     T.c11 = Ei.c11 - beta * (2.0 / 3.0);
     T.c12 = Ei.c12 + beta * (1.0 / 3.0);
     T.c44 = Ei.c44 - beta * 0.5;

@@ -23,4 +23,14 @@ cudaError_t geometry_hexa8(int rule, int64_t nEl, int64_t off, const int32_t* co
   return cudaErrorInvalidValue;
 }
 
+cudaError_t body_force_hexa8(int rule, int64_t nSel, const int32_t* elems, const int32_t* conn, const int32_t* nodeDof,
+                              const double* S, const double* f, double* P, cudaStream_t st) {
+  switch (rule) {
+    case EFE_RULE_3D_1: return launch_body_force<EFE_HEXA8, EFE_RULE_3D_1>(nSel, elems, conn, nodeDof, S, f, P, st);
+    case EFE_RULE_3D_2X2X2: return launch_body_force<EFE_HEXA8, EFE_RULE_3D_2X2X2>(nSel, elems, conn, nodeDof, S, f, P, st);
+    case EFE_RULE_3D_3X3X3: return launch_body_force<EFE_HEXA8, EFE_RULE_3D_3X3X3>(nSel, elems, conn, nodeDof, S, f, P, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
 }  // namespace efe

@@ -116,6 +116,32 @@ __global__ void geometry_kernel(int64_t nEl, int64_t elOffset, const int32_t* __
   S[t] = detJ * w * th;
 }
 
+// ------------------------------------------------------------------ body force
+// P_e[(a,c)] += sum_q N_a(xi_q, eta_q, zeta_q) * f_c * detJ_q * t * w_q with N at the library point and
+// det J at the point the Jacobian is formed (DisplacementElement.computeBodyForce, element.py:348-371).
+template <int SHAPE, int RULE>
+__global__ void body_force_kernel(int64_t nSel, const int32_t* __restrict__ elems, const int32_t* __restrict__ conn,
+                                  const int32_t* __restrict__ nodeDof, const double* __restrict__ S, double f0,
+                                  double f1, double f2, double* P) {
+  constexpr int DIM = ShapeInfo<SHAPE>::DIM, NN = ShapeInfo<SHAPE>::NN, NQ = RuleInfo<RULE>::NQ;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nSel * NN) return;
+  const int64_t sel = t / NN;
+  const int a = (int)(t % NN);
+  const int64_t e = elems ? elems[sel] : sel;
+  double acc = 0.0;
+  for (int q = 0; q < NQ; ++q) {
+    double xi, eta, zeta, w, N[NN];
+    quadrature_point(RULE, q, xi, eta, zeta, w);
+    const double p[3] = {xi, eta, zeta};
+    shape_values<SHAPE>(p, N);
+    acc += N[a] * S[e * NQ + q];
+  }
+  const int32_t dof = nodeDof[conn[e * NN + a]];
+  const double f[3] = {f0, f1, f2};
+  for (int c = 0; c < DIM; ++c) atomicAdd(P + dof + c, acc * f[c]);
+}
+
 // ------------------------------------------------------------------ assembly
 enum Form { SS3 = 0, SS2 = 1, TLH = 2, TLV3 = 3, TLV2 = 4 };
 template <int FORM, int DIM> struct FormInfo;

@@ -44,6 +44,17 @@ cudaError_t launch_geometry(int64_t nEl, int64_t elOffset, const int32_t* conn, 
   return cudaGetLastError();
 }
 
+template <int SHAPE, int RULE>
+cudaError_t launch_body_force(int64_t nSel, const int32_t* elems, const int32_t* conn, const int32_t* nodeDof,
+                              const double* S, const double* f, double* P, cudaStream_t st) {
+  const int64_t n = nSel * ShapeInfo<SHAPE>::NN;
+  if (n == 0) return cudaSuccess;
+  const int nt = 128;
+  body_force_kernel<SHAPE, RULE><<<(unsigned)((n + nt - 1) / nt), nt, 0, st>>>(nSel, elems, conn, nodeDof, S, f[0], f[1],
+                                                                               ShapeInfo<SHAPE>::DIM == 3 ? f[2] : 0.0, P);
+  return cudaGetLastError();
+}
+
 // form selector: small strain 3D/2D, total Lagrangian hyperelastic, total Lagrangian hypoelastic 3D/2D
 template <int SHAPE, int RULE, typename KT>
 cudaError_t launch_form(int form, const GroupArgs& g, cudaStream_t st) {
@@ -75,6 +86,14 @@ cudaError_t assemble_quad4(int rule, int form, int kprec, const GroupArgs& g, cu
 cudaError_t assemble_quad8(int rule, int form, int kprec, const GroupArgs& g, cudaStream_t st);
 cudaError_t assemble_hexa8(int rule, int form, int kprec, const GroupArgs& g, cudaStream_t st);
 cudaError_t assemble_hexa20(int rule, int form, int kprec, const GroupArgs& g, cudaStream_t st);
+#define EFE_BODY_DECL(name)                                                                                \
+  cudaError_t body_force_##name(int rule, int64_t nSel, const int32_t* elems, const int32_t* conn,            \
+                                const int32_t* nodeDof, const double* S, const double* f, double* P, cudaStream_t st);
+EFE_BODY_DECL(quad4)
+EFE_BODY_DECL(quad8)
+EFE_BODY_DECL(hexa8)
+EFE_BODY_DECL(hexa20)
+#undef EFE_BODY_DECL
 #define EFE_GEOMETRY_DECL(name)                                                                          \
   cudaError_t geometry_##name(int rule, int64_t nEl, int64_t off, const int32_t* conn, const double* coords, \
                               const double* th, double* G, float* G32, double* S, int32_t* status,            \

@@ -1,0 +1,333 @@
+"""Newton-Raphson driver around the GPU element pass (the reference's NIST, restated for the device).
+
+`NISTGPU.solveStep` / `solveIncrement` follow `NIST.solveStep` / `NIST.solveIncrement`
+(`edelweissfe/solvers/nonlinearimplicitstatic.py:134-332, 334-458`): the same increment loop and
+cutback handling, Dirichlet treatment (prescribed increment in the first iteration, zeroed
+residual rows afterwards, identity rows in K, `:559-623`), Abaqus-like convergence test
+(`:625-725`: flux residual <= max(tol * spatially averaged flux, 1e-7) and correction < tol),
+growing-residual and maximum-iteration checks, and linear extrapolation of the last increment
+(`:947-986`).  `AdaptiveTimeStepper` restates `edelweissfe/timesteppers/adaptivetimestepper.py:38-183`.
+
+The element pass, the residual, the tangent and the loads stay on the GPU.  The linear solve is
+either SciPy's SuperLU on the host on the reference's row-modified CSR matrix (``"superlu"``, the
+reference's fallback solver, for parity runs) or a Jacobi-preconditioned conjugate-gradient solve on
+the device (``"pcg"``) on the equivalent symmetric system with the Dirichlet columns eliminated.
+"""
+
+from collections import namedtuple
+
+import numpy as np
+import torch
+
+from .exceptions import CutbackRequest
+
+TimeStep = namedtuple("TimeStep", "number stepProgressIncrement stepProgress timeIncrement stepTime totalTime")
+
+
+class ReachedMaxIterations(Exception):
+    pass
+
+
+class DivergingSolution(Exception):
+    pass
+
+
+class ReachedMinIncrementSize(Exception):
+    pass
+
+
+class ReachedMaxIncrements(Exception):
+    pass
+
+
+class StepFailed(Exception):
+    pass
+
+
+class AdaptiveTimeStepper:
+    """Increment generator of `timesteppers/adaptivetimestepper.py:38-183` (first increment is a zero
+    increment; the increment grows by `increaseFactor` after three good increments)."""
+
+    def __init__(self, currentTime=0.0, stepLength=1.0, startIncrement=1.0, maxIncrement=1.0, minIncrement=1e-4,
+                 maxNumberIncrements=1000, increaseFactor=1.1):  # fmt: skip
+        self.nPassedGoodIncrements = 0
+        self.incrementCounter = 0
+        self.maxIncrement = maxIncrement
+        self.minIncrement = minIncrement
+        self.maxNumberIncrements = maxNumberIncrements
+        self.finishedStepProgress = 0.0
+        self.increment = min(startIncrement, maxIncrement)
+        self.allowedToIncreasedNext = True
+        self.currentTime = currentTime
+        self.stepLength = stepLength
+        self.increaseFactor = increaseFactor
+
+    def generateTimeStep(self):
+        while self.finishedStepProgress < (1.0 - 1e-15):
+            remainder = 1.0 - self.finishedStepProgress
+            if remainder < self.increment:
+                self.increment = remainder
+            theIncrement = self.increment if self.incrementCounter > 0 else 0.0
+            dT = self.stepLength * theIncrement
+            self.finishedStepProgress += theIncrement
+            endInStep = self.stepLength * self.finishedStepProgress
+            yield TimeStep(self.incrementCounter, theIncrement, self.finishedStepProgress, dT, endInStep,
+                           self.currentTime + endInStep)  # fmt: skip
+            if self.incrementCounter > self.maxNumberIncrements:
+                raise ReachedMaxIncrements()
+            if self.nPassedGoodIncrements >= 3 and self.allowedToIncreasedNext:
+                self.increment *= self.increaseFactor
+                if self.increment > self.maxIncrement:
+                    self.increment = self.maxIncrement
+            self.allowedToIncreasedNext = True
+            self.incrementCounter += 1
+            self.nPassedGoodIncrements += 1
+
+    def preventIncrementIncrease(self):
+        self.allowedToIncreasedNext = False
+
+    def reduceNextIncrement(self, scaleFactor):
+        if self.increment == self.minIncrement:
+            raise ReachedMinIncrementSize()
+        new = self.increment * scaleFactor
+        self.increment = min(self.maxIncrement, max(self.minIncrement, new))
+
+    def discardAndChangeIncrement(self, scaleFactor):
+        if self.incrementCounter == 0:
+            raise ReachedMinIncrementSize()
+        self.finishedStepProgress -= self.increment
+        self.incrementCounter -= 1
+        self.nPassedGoodIncrements = 0
+        self.reduceNextIncrement(scaleFactor)
+
+
+def _linear(x):
+    return x
+
+
+class Dirichlet:
+    """Prescribed displacements: `values` are reached at the end of the step (stepactions/dirichlet.py:105-112)."""
+
+    def __init__(self, dofs, values, amplitude=_linear):
+        self.dofs = np.asarray(dofs, np.int64)
+        self.values = np.broadcast_to(np.asarray(values, float), self.dofs.shape).copy()
+        self.amplitude = amplitude
+
+    def getDelta(self, ts):
+        return self.values * (self.amplitude(ts.stepProgress) - self.amplitude(ts.stepProgress - ts.stepProgressIncrement))
+
+
+class NodeForces:
+    """Concentrated loads ramped over the step (stepactions/nodeforces.py:136-145)."""
+
+    def __init__(self, dofs, values, amplitude=_linear):
+        self.dofs = np.asarray(dofs, np.int64)
+        self.values = np.broadcast_to(np.asarray(values, float), self.dofs.shape).copy()
+        self.amplitude = amplitude
+
+    def getCurrentLoad(self, ts):
+        return self.values * self.amplitude(ts.stepProgress)
+
+
+class BodyForce:
+    """Body force per unit volume on a set of elements (global indices), ramped over the step
+    (stepactions/bodyforce.py:95-101)."""
+
+    def __init__(self, elements, force, amplitude=_linear):
+        self.elements = None if elements is None else np.asarray(elements, np.int64)
+        self.force = np.asarray(force, float)
+        self.amplitude = amplitude
+
+    def getCurrentLoad(self, ts):
+        return self.force * self.amplitude(ts.stepProgress)
+
+
+class NISTGPU:
+    """Nonlinear implicit static solver with the element pass, loads and (optionally) the linear
+    solve on the GPU.  `assembler` is a GPUAssembler."""
+
+    def __init__(self, assembler, linsolver="pcg", extrapolation="linear", maxIter=10, criticalIter=5,
+                 maxGrowingIter=10, fluxResidualTolerance=1e-8, fluxResidualToleranceAlternative=5e-3,
+                 fieldCorrectionTolerance=1e-8, pcgTolerance=1e-12, pcgMaxIter=20000):  # fmt: skip
+        self.asm = assembler
+        self.linsolver = linsolver
+        self.extrapolation = extrapolation
+        self.maxIter = maxIter
+        self.criticalIter = criticalIter
+        self.maxGrowingIter = maxGrowingIter
+        self.fluxTol = fluxResidualTolerance
+        self.fluxTolAlt = fluxResidualToleranceAlternative
+        self.corrTol = fieldCorrectionTolerance
+        self.pcgTolerance = pcgTolerance
+        self.pcgMaxIter = pcgMaxIter
+        self.nAccumulatedFluxes = sum(len(g.conn) * len(g.conn[0]) * assembler.dim for g in assembler.groups if len(g.conn))
+        dev = assembler.device
+        ip, ix = assembler.indptr_host, assembler.indices_host
+        rows = np.repeat(np.arange(assembler.nDof), np.diff(ip))
+        self._diag_pos = torch.from_numpy(np.nonzero(ix == rows)[0]).to(dev)
+        self.history = []  # one record per attempted increment
+        self.linearIterations = []
+
+    # ------------------------------------------------------------------ step
+    def solveStep(self, stepper, dirichlets=(), nodeforces=(), bodyforces=(), cutbackFactor=0.25, U=None):
+        asm = self.asm
+        U = asm.constructDofVector() if U is None else U
+        dU = asm.constructDofVector()
+        prev = None
+        try:
+            for ts in stepper.generateTimeStep():
+                try:
+                    U_new, dU, P, iters, res = self.solveIncrement(U, dU, dirichlets, nodeforces, bodyforces, ts, prev)
+                except CutbackRequest as e:
+                    stepper.discardAndChangeIncrement(max(e.cutbackSize, cutbackFactor))
+                    prev = None
+                    self.history.append(dict(timeStep=ts, iterations=None, error="CutbackRequest"))
+                except (ReachedMaxIterations, DivergingSolution) as e:
+                    stepper.discardAndChangeIncrement(cutbackFactor)
+                    prev = None
+                    self.history.append(dict(timeStep=ts, iterations=None, error=type(e).__name__))
+                else:
+                    prev = ts
+                    if iters >= self.criticalIter:
+                        stepper.preventIncrementIncrease()
+                    U = U_new
+                    asm.acceptLastState()  # FEModel.advanceToTime (models/femodel.py:245-258)
+                    self.history.append(dict(timeStep=ts, iterations=iters, error="", residuals=res))
+        except (ReachedMaxIncrements, ReachedMinIncrementSize):
+            raise StepFailed()
+        return U
+
+    # ------------------------------------------------------------------ increment
+    def _dirichlet_rhs(self, vec, dirichlets, ts):
+        for d in dirichlets:
+            vec[torch.from_numpy(d.dofs).to(vec.device)] = torch.from_numpy(d.getDelta(ts)).to(vec)
+        return vec
+
+    def solveIncrement(self, U_n, dU, dirichlets, nodeforces, bodyforces, ts, prevTimeStep):
+        asm = self.asm
+        dev = asm.device
+        dir_idx = (
+            torch.from_numpy(np.unique(np.concatenate([d.dofs for d in dirichlets]))).to(dev) if dirichlets else None
+        )
+        # extrapolateLastIncrement (:947-986)
+        if self.extrapolation == "linear" and prevTimeStep is not None and prevTimeStep.timeIncrement:
+            dU = dU * (ts.stepProgressIncrement / prevTimeStep.stepProgressIncrement)
+            dU = self._dirichlet_rhs(dU, dirichlets, ts)
+            extrapolated = True
+        else:
+            dU = torch.zeros_like(dU)
+            extrapolated = False
+        it = 0
+        ddU = None
+        prevFlux, nGrew = 0.0, 0
+        residuals = []
+        time = (ts.stepTime, ts.totalTime)
+        P, F, K = asm.constructDofVector(), asm.constructDofVector(), asm.constructSystemMatrix()
+        while True:
+            U_np = U_n + dU
+            P.zero_()
+            F.zero_()
+            K.zero_()
+            asm.status.zero_()
+            asm.launch(U_np, dU, P, K, F, time, ts.timeIncrement)
+            asm.check_status()
+            PExt = asm.constructDofVector()
+            for nf in nodeforces:
+                PExt.index_add_(0, torch.from_numpy(nf.dofs).to(dev), torch.from_numpy(nf.getCurrentLoad(ts)).to(PExt))
+            for bf in bodyforces:
+                asm.computeBodyForce(PExt, bf.getCurrentLoad(ts), bf.elements)
+            R = P + PExt
+            if it == 0 and not extrapolated and dirichlets:
+                R = self._dirichlet_rhs(R, dirichlets, ts)
+            else:
+                if dir_idx is not None:
+                    R[dir_idx] = 0.0
+                # checkConvergence (:625-725), one field
+                flux = float(R.abs().max())
+                avgFlux = max(1e-10, float(F.abs().sum()) / self.nAccumulatedFluxes)
+                corr = float(ddU.abs().max()) if ddU is not None else 0.0
+                tol = self.fluxTol if it < 15 else self.fluxTolAlt
+                converged = corr < self.corrTol and flux <= max(tol * avgFlux, 1e-7)
+                if flux > prevFlux:
+                    nGrew += 1
+                prevFlux = flux
+                residuals.append((flux, avgFlux, corr))
+                if converged:
+                    break
+                if nGrew > self.maxGrowingIter:
+                    raise DivergingSolution("Residual grew {:} times, cutting back".format(self.maxGrowingIter))
+                if it == self.maxIter:
+                    raise ReachedMaxIterations("Reached max. iterations in current increment, cutting back")
+            ddU = self.linearSolve(K, R, dir_idx)
+            if torch.isnan(ddU).any():
+                raise DivergingSolution("Obtained NaN in linear solve")
+            dU = dU + ddU
+            it += 1
+        return U_np, dU, P, it, residuals
+
+    # ------------------------------------------------------------------ linear solve
+    def linearSolve(self, K, R, dir_idx):
+        if self.linsolver == "superlu":
+            return self._solve_superlu(K, R, dir_idx)
+        return self._solve_pcg(K, R, dir_idx)
+
+    def _solve_superlu(self, K, R, dir_idx):
+        """assembleStiffnessCSR + applyDirichletK (:559-593) + SciPy SuperLU, on the host."""
+        import scipy.sparse.linalg as sla
+
+        A = self.asm.assembleStiffnessCSR(K, host=True)
+        if dir_idx is not None:
+            rows = dir_idx.cpu().numpy()
+            for r in rows:
+                A.data[A.indptr[r] : A.indptr[r + 1]] = 0.0
+            diag = A.diagonal()
+            diag[rows] = 1.0
+            A.setdiag(diag)
+            A.eliminate_zeros()
+        x = sla.spsolve(A, R.cpu().numpy(), use_umfpack=False)
+        return torch.from_numpy(np.asarray(x, np.float64)).to(self.asm.device)
+
+    def _solve_pcg(self, K, R, dir_idx):
+        """Jacobi-preconditioned CG on the device.  The reference's system has identity rows for the
+        Dirichlet DOFs; moving the known values to the right-hand side gives the same solution from a
+        symmetric positive-definite system on the free DOFs."""
+        asm = self.asm
+        Kd = K.double() if K.dtype != torch.float64 else K
+        A = torch.sparse_csr_tensor(asm.indptr, asm.indices, Kd, size=(asm.nDof, asm.nDof))
+        m = torch.ones(asm.nDof, dtype=torch.float64, device=asm.device)
+        if dir_idx is not None:
+            m[dir_idx] = 0.0
+        xd = (1.0 - m) * R
+        b = m * (R - (A @ xd.unsqueeze(1)).squeeze(1)) + xd
+
+        def op(v):
+            return m * (A @ (m * v).unsqueeze(1)).squeeze(1) + (1.0 - m) * v
+
+        d = Kd[self._diag_pos]
+        dinv = torch.where(m > 0, 1.0 / d, torch.ones_like(d))
+        x = xd.clone()
+        r = b - op(x)
+        z = dinv * r
+        p = z.clone()
+        rz = torch.dot(r, z)
+        bnorm = float(torch.linalg.vector_norm(b))
+        k = 0
+        if bnorm == 0.0 or float(torch.linalg.vector_norm(r)) <= self.pcgTolerance * bnorm:
+            self.linearIterations.append(0)
+            return x
+        for k in range(1, self.pcgMaxIter + 1):
+            Ap = op(p)
+            pAp = torch.dot(p, Ap)
+            if float(pAp) == 0.0:
+                break
+            alpha = rz / pAp
+            x += alpha * p
+            r -= alpha * Ap
+            if k % 10 == 0 and float(torch.linalg.vector_norm(r)) <= self.pcgTolerance * bnorm:
+                break
+            z = dinv * r
+            rz_new = torch.dot(r, z)
+            p = z + (rz_new / rz) * p
+            rz = rz_new
+        self.linearIterations.append(k)
+        return x

@@ -146,6 +146,15 @@ int32_t efe_compute_elements(const EfeMesh* mesh, const EfeGroup* groups, int32_
                              const double* dU, const double* time2, double dT, int32_t kPrecision, void* Kdata,
                              double* P, double* F, int32_t* status, void* stream);
 
+/* Body force of a set of elements of one group, added to P (NIST.computeBodyForces,
+   solvers/nonlinearimplicitstatic.py:520-557, element computeBodyForce,
+   elements/displacementelement/element.py:348-371 and displacementtlelement/element.py:429-452):
+   P[(a,c)] += sum_q N_a(q) * force[c] * detJ_q * w_q * t.  elements: device array of nSelected
+   element indices local to the group, or NULL for all nElements; force: HOST array [dim].
+   Needs efe_setup_geometry to have run for the group. */
+int32_t efe_body_force(const EfeMesh* mesh, const EfeGroup* group, const int32_t* elements, int64_t nSelected,
+                       const double* force, double* P, void* stream);
+
 /* acceptLastState: stateTemp -> stateRef and auxTemp -> auxRef for every group. */
 int32_t efe_accept_state(const EfeGroup* groups, int32_t nGroups, void* stream);
 
