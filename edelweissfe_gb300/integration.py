@@ -1,0 +1,138 @@
+"""Wiring the GPU element path into an EdelweissFE run.
+
+EdelweissFE extends its Newton solver by subclassing `NIST` and overriding `computeElements`
+(the pattern of `solvers/nonlinearimplicitstaticparallelmk2.pyx:50,111`), registered in
+`config/solvers.py:48-53` (`solverLibrary`) and selected with ``*solver, solver=<name>``.
+`make_nist_gpu` builds such a subclass around `GPUAssembler`; `arrays_from_reference` converts the
+reference's element objects and DofManager into the arrays the GPU path takes.
+
+The reference package is not imported here: the functions take its objects and read only their
+public state (element type tables, nodes, material parameters, section thickness, DOF indices).
+"""
+
+import numpy as np
+
+from . import library
+
+_MATERIALS = {
+    "LinearElasticMaterial": "linearelastic",
+    "VonMisesMaterial": "vonmises",
+    "NeoHookeanWaMaterial": "neohookewa",
+    "NeoHookeanWbMaterial": "neohookewb",
+    "NeoHookeanWcMaterial": "neohookewc",
+}
+
+
+def element_type_of(el):
+    """Library name of a reference element from its tables (class, nodes, dimension, points, plane flag)."""
+    tl = type(el).__name__ == "DisplacementTLElement"
+    if type(el).__name__ not in ("DisplacementElement", "DisplacementTLElement"):
+        raise NotImplementedError(f"{type(el).__name__} is not an edelweiss displacement element")
+    for name, et in library.ELEMENT_TYPES.items():
+        if et.totalLagrangian != tl or et.nNodes != el.nNodes or et.dim != el.nSpatialDimensions:
+            continue
+        if et.nInt != el._nInt:
+            continue
+        plane = {True: "pe", False: "ps", None: "solid"}[el.planeStrain]
+        if plane == {1: "pe", 2: "ps", 0: "solid"}[et.plane]:
+            return name
+    raise KeyError("no matching element type")
+
+
+def material_of(mat):
+    """(material name, property vector) of a reference material object (materials/*)."""
+    name = _MATERIALS.get(type(mat).__name__)
+    if name is None:
+        raise NotImplementedError(f"{type(mat).__name__} is not supported by the GPU element path")
+    if name == "linearelastic":
+        return name, [mat._E, mat._v]
+    if name == "vonmises":
+        return name, [mat._E, mat._v, mat.yieldStress, mat.HLin, mat.deltaYieldStress, mat.delta]
+    return name, list(np.asarray(mat.materialProperties, float)[:2])
+
+
+def arrays_from_reference(elements, dofManager):
+    """coords, nodeDof, nDof, groups for a list of reference elements (in the model's element order)."""
+    from .assembly import ElementGroup
+
+    elements = list(elements)
+    nodes = {}
+    for el in elements:
+        for n in el.nodes:
+            nodes.setdefault(id(n), n)
+    order = list(nodes.values())
+    pos = {id(n): i for i, n in enumerate(order)}
+    dim = elements[0].nSpatialDimensions
+    coords = np.array([n.coordinates for n in order], float)
+    nodeDof = -np.ones(len(order), np.int64)
+    recs = []
+    for el in elements:
+        idx = np.asarray(dofManager.idcsOfElementsInDofVector[el])
+        conn = [pos[id(n)] for n in el.nodes]
+        first = idx[0::dim]
+        if not np.array_equal(idx, (first[:, None] + np.arange(dim)).ravel()):
+            raise NotImplementedError("element DOFs are not node-major with interleaved components")
+        nodeDof[conn] = first
+        kind, props = material_of(el.material)
+        recs.append((element_type_of(el), kind, props, conn, float(getattr(el, "_t", 1.0))))
+    groups = []
+    start = 0
+    for e in range(1, len(recs) + 1):
+        if e == len(recs) or recs[e][:2] != recs[start][:2] or len(recs[e][2]) != len(recs[start][2]):
+            chunk = recs[start:e]
+            groups.append(ElementGroup(chunk[0][0], chunk[0][1], np.array([r[2] for r in chunk]),
+                                       np.array([r[3] for r in chunk]), np.array([r[4] for r in chunk])))  # fmt: skip
+            start = e
+    return coords, nodeDof, int(dofManager.nDof), groups
+
+
+def make_nist_gpu(NIST, precision="fp64"):
+    """A NIST subclass whose element loop and CSR assembly run on the GPU.
+
+    The reference's solveIncrement keeps its host DOF vectors: computeElements copies U_np and dU to
+    the device, runs the element pass, and adds P and |P_e| back into the host vectors; the
+    tangent stays on the device until assembleStiffnessCSR returns it as the scipy CSR matrix the
+    linear solvers expect.  Accepting a converged increment (FEModel.advanceToTime) also accepts
+    the device state."""
+    import torch
+
+    from .assembly import GPUAssembler
+
+    class NISTGPU(NIST):
+        identification = "NISTGPU"
+
+        def _gpu(self, elements):
+            if getattr(self, "_gpuAssembler", None) is None or self._gpuDofManager is not self.theDofManager:
+                coords, nodeDof, nDof, groups = arrays_from_reference(elements.values(), self.theDofManager)
+                self._gpuAssembler = GPUAssembler(coords, nodeDof, nDof, groups, precision=precision)
+                self._gpuDofManager = self.theDofManager
+            return self._gpuAssembler
+
+        def computeElements(self, elements, U_np, dU, P, K, F, timeStep):
+            asm = self._gpu(elements)
+            Pd, Fd = asm.constructDofVector(), asm.constructDofVector()
+            self._gpuK = asm.constructSystemMatrix()
+            asm.computeElements(elements, torch.as_tensor(np.asarray(U_np)), torch.as_tensor(np.asarray(dU)), Pd,
+                                self._gpuK, Fd, timeStep)  # fmt: skip
+            P += Pd.cpu().numpy()
+            F += Fd.cpu().numpy()
+            return P, K, F
+
+        def assembleStiffnessCSR(self, K):
+            return self._gpuAssembler.assembleStiffnessCSR(self._gpuK, host=True)
+
+        def solveStep(self, step, model, fieldOutputController, outputmanagers):
+            advance = model.advanceToTime
+
+            def advanceToTime(time):
+                advance(time)
+                if getattr(self, "_gpuAssembler", None) is not None:
+                    self._gpuAssembler.acceptLastState()
+
+            model.advanceToTime = advanceToTime
+            try:
+                return super().solveStep(step, model, fieldOutputController, outputmanagers)
+            finally:
+                model.advanceToTime = advance
+
+    return NISTGPU

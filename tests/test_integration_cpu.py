@@ -1,0 +1,81 @@
+"""The adapter from reference objects to the GPU path's arrays (edelweissfe_gb300.integration).
+
+Needs the reference source tree (EDELWEISSFE_ROOT, default ../reference next to this repository's
+parent); skipped when it is not present.  No GPU: the extracted arrays are checked against the
+reference's own DofManager and, through the oracle, against the reference's computeElements.
+"""
+
+import os
+import sys
+
+import numpy as np
+import pytest
+
+REF = os.environ.get("EDELWEISSFE_ROOT", "/root/reference")
+pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "edelweissfe")), reason="reference not present")
+
+
+@pytest.fixture(scope="module")
+def ref():
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    import make_golden
+
+    make_golden.setup_reference(REF)
+    return make_golden
+
+
+def _prepared(mg, dim, gen, lines, et, kind, props, jit, h, seed, lo, hi):
+    from edelweissfe.journal.journal import Journal
+    from edelweissfe.numerics.dofmanager import DofManager
+    from edelweissfe.sets.nodeset import NodeSet
+
+    model = mg.make_model(dim, gen, lines, et, jit, h, seed, lo, hi)
+    model.nodeSets["all"] = NodeSet("all", list(model.nodes.values()))
+    cls = mg.material_class(kind)
+    for el in model.elements.values():
+        el.setProperties(np.array([0.7]))
+        el.initializeElement()
+        el.setMaterial(cls(np.array(props, float)))
+    model._prepareVariablesAndFields(Journal(verbose=False))
+    dm = DofManager(model.nodeFields.values(), [], model.elements.values(), [], model.nodeSets.values())
+    return model, dm
+
+
+@pytest.mark.parametrize(
+    "dim,gen,lines,et,kind,props",
+    [
+        (3, "boxGen", ["nX=3", "nY=2", "nZ=2"], "C3D8", "vonmises", [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0]),
+        (2, "planeRectQuad", ["nX=4", "nY=3"], "CPE8RTL", "neohookewa", [1000.0, 10000.0]),
+        (3, "boxGen", ["nX=2", "nY=1", "nZ=1"], "C3D20", "linearelastic", [210000.0, 0.3]),
+    ],
+)
+def test_arrays_from_reference_reproduce_compute_elements(ref, dim, gen, lines, et, kind, props):
+    from edelweissfe.config.timing import createTimingDict
+    from edelweissfe.numerics.csrgenerator import CSRGenerator
+    from edelweissfe.solvers.nonlinearimplicitstatic import NIST
+    from edelweissfe.timesteppers.timestep import TimeStep
+
+    from edelweissfe_gb300.integration import arrays_from_reference
+    from oracle.assembly import Model
+
+    h = [1.0 / 3] * dim
+    model, dm = _prepared(ref, dim, gen, lines, et, kind, props, 0.1, h, 5, [0] * dim, [1] * dim)
+    coords, nodeDof, nDof, groups = arrays_from_reference(model.elements.values(), dm)
+    assert len(groups) == 1 and groups[0].elType == et and groups[0].material == kind
+    g = groups[0]
+    el_dofs = (nodeDof[g.conn][:, :, None] + np.arange(dim)).reshape(len(g.conn), -1)
+    assert np.array_equal(el_dofs, np.array([dm.idcsOfElementsInDofVector[el] for el in model.elements.values()]))
+    # the oracle on the extracted arrays reproduces the reference's element pass
+    rng = np.random.default_rng(0)
+    U = dm.constructDofVector()
+    U[:] = rng.uniform(-1, 1, nDof) * (0.02 if kind.startswith("neo") else 2e-3)
+    P, F, K = dm.constructDofVector(), dm.constructDofVector(), dm.constructVIJSystemMatrix()
+    s = type("S", (), {"computationTimes": createTimingDict()})()
+    P, K, F = NIST.computeElements(s, model.elements, U, U, P, K, F, TimeStep(1, 1.0, 1.0, 1.0, 1.0, 1.0))
+    Kc = CSRGenerator(K).updateCSR(K)
+    om = Model(coords, nodeDof, nDof, [dict(elType=g.elType, kind=g.material, props=g.props, conn=g.conn,
+                                            thickness=g.thickness, order=np.arange(len(g.conn)))])  # fmt: skip
+    r = om.compute_elements(np.asarray(U), np.asarray(U), om.initial_state())
+    assert np.array_equal(om.indptr, Kc.indptr) and np.array_equal(om.indices, Kc.indices)
+    assert np.abs(r["P"] - P).max() <= 1e-12 * np.abs(P).max()
+    assert np.abs(r["Kdata"] - Kc.data).max() <= 1e-12 * np.abs(Kc.data).max()
