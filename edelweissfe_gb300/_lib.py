@@ -33,6 +33,7 @@ EXPORTS = [
     "efe_compute_elements",
     "efe_accept_state",
     "efe_body_force",
+    "efe_adjoint_tl",
     "efe_pattern_count",
     "efe_pattern_fill",
 ]
@@ -126,6 +127,8 @@ def load(build_if_missing=False):
     ]
     lib.efe_body_force.restype = i32
     lib.efe_body_force.argtypes = [ctypes.POINTER(EfeMesh), ctypes.POINTER(EfeGroup), P, i64, P, P, P]
+    lib.efe_adjoint_tl.restype = i32
+    lib.efe_adjoint_tl.argtypes = [ctypes.POINTER(EfeMesh), ctypes.POINTER(EfeGroup), P, P, P, P, P]
     lib.efe_accept_state.restype = i32
     lib.efe_accept_state.argtypes = [ctypes.POINTER(EfeGroup), i32, P]
     lib.efe_pattern_count.restype = i64

@@ -279,6 +279,26 @@ class GPUAssembler:
             del sel
         return P
 
+    def adjointTL(self, U, lam):
+        """dL/dX [nNodes, dim] and per group dL/d(mu, K) [E, 2] for L = lam^T P(X, U, mu, K) of the
+        total-Lagrangian Neo-Hooke groups (efe_adjoint_tl); lam must be zero on prescribed DOFs."""
+        U = self._as_device(U)
+        lam = self._as_device(lam)
+        gX = torch.zeros((self.nNodes, self.dim), dtype=torch.float64, device=self.device)
+        gP = []
+        for i, g in enumerate(self.groups):
+            gp = torch.zeros((len(g.conn), 2), dtype=torch.float64, device=self.device)
+            L.check(
+                self.lib.efe_adjoint_tl(
+                    ctypes.byref(self.mesh), ctypes.byref(self._groups_c[i]), ctypes.c_void_p(U.data_ptr()),
+                    ctypes.c_void_p(lam.data_ptr()), ctypes.c_void_p(gX.data_ptr()), ctypes.c_void_p(gp.data_ptr()),
+                    self._stream(),
+                ),
+                "efe_adjoint_tl",
+            )
+            gP.append(gp)
+        return gX, gP
+
     # ------------------------------------------------------------------ state
     def acceptLastState(self):
         """acceptLastState of every element (element.py:373-379; TL element.py:454-461)."""

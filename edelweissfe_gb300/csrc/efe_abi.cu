@@ -315,6 +315,30 @@ int32_t efe_body_force(const EfeMesh* mesh, const EfeGroup* g, const int32_t* el
   return EFE_OK;
 }
 
+int32_t efe_adjoint_tl(const EfeMesh* mesh, const EfeGroup* g, const double* U, const double* lambda, double* gX,
+                       double* gParams, void* stream) {
+  if (!mesh || !g || !U || !lambda || !gX || !gParams) return fail(EFE_ERR_ARGUMENT, "null argument");
+  int32_t rc = check_group(mesh, *g);
+  if (rc) return rc;
+  if (g->kinematics != EFE_TOTAL_LAGRANGIAN || !hyperelastic(g->material))
+    return fail(EFE_ERR_UNSUPPORTED, "the adjoint covers total-Lagrangian Neo-Hooke groups");
+  if (!mesh->coords || !mesh->nodeDof || !g->conn || !g->props) return fail(EFE_ERR_ARGUMENT, "null group buffer");
+  if (mesh->dim == 2 && !g->thickness) return fail(EFE_ERR_ARGUMENT, "2D elements need a thickness array");
+  static const efe::Hexa20Fix fix = hexa20_fix();
+  efe::AdjointArgs a{g->nElements, g->conn,      mesh->nodeDof, mesh->coords, U,   lambda, g->props,
+                     g->nProps,   g->material,  g->thickness,  fix,          gX,  gParams};
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaErrorInvalidValue;
+  switch (g->shape) {
+    case EFE_QUAD4: e = efe::adjoint_tl_quad4(g->rule, a, st); break;
+    case EFE_QUAD8: e = efe::adjoint_tl_quad8(g->rule, a, st); break;
+    case EFE_HEXA8: e = efe::adjoint_tl_hexa8(g->rule, a, st); break;
+    case EFE_HEXA20: e = efe::adjoint_tl_hexa20(g->rule, a, st); break;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "efe_adjoint_tl");
+  return EFE_OK;
+}
+
 int32_t efe_accept_state(const EfeGroup* groups, int32_t nGroups, void* stream) {
   if (!groups || nGroups < 0) return fail(EFE_ERR_ARGUMENT, "null argument");
   cudaStream_t st = (cudaStream_t)stream;

@@ -1,0 +1,217 @@
+// efe_adjoint.cuh -- adjoint of the total-Lagrangian hyperelastic element residual.
+//
+// For L = lambda^T P(X, U, mu, K), with P the element residual of DisplacementTLElement with a
+// Neo-Hooke material (displacementtlelement/element.py:389-414: P_a -= s tau h_a, s = det J w t,
+// h_a = F^-T dN_a/dX, tau the Kirchhoff stress), the kernel returns dL/dX (nodal reference
+// coordinates) and dL/dmu, dL/dK per element, by reverse-mode differentiation written out by hand:
+//
+//   L = -s phi,  phi = tau : M,  M = Lambda F^-1,  Lambda = sum_a lambda_a (x) dN_a/dX
+//   dphi/dF  = c1 (M F + M^T F) + (c2 tr M + c3 M:B) F^-T + c4 tr(M) F - F^-T Lambda^T tau F^-T
+//   dphi/dLambda = tau F^-T
+//   then through F = I + sum_a U_a (x) G_a and Lambda to G = dN/dX = J^-1 dN/dxi, and through
+//   J = dN/dxi . X (with the Hexa20 third-row term of the reference) and s = det J w t to X.
+// Parameter derivatives use dtau/dmu, dtau/dK of each variant.
+#pragma once
+#include "efe_launch.cuh"
+
+namespace efe {
+
+// d tau / d mu and d tau / d K of the three Neo-Hooke variants (same formulas as neo_hooke()).
+__device__ inline void neo_hooke_param_derivatives(int material, double mu, double K, const double F[3][3],
+                                                   double dmu[3][3], double dK[3][3]) {
+  double B[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) B[i][j] = F[i][0] * F[j][0] + F[i][1] * F[j][1] + F[i][2] * F[j][2];
+  const double J = det3(F);
+  const double I1 = B[0][0] + B[1][1] + B[2][2];
+  double aB = 0.0, aI = 0.0, bI = 0.0;  // dtau/dmu = aB B + aI I, dtau/dK = bI I
+  if (material == EFE_MAT_NEOHOOKE_WA) {
+    aB = 1.0;
+    aI = -(2.0 / 3.0) * (J * J - J) - 1.0;
+    bI = J * J - J;
+  } else if (material == EFE_MAT_NEOHOOKE_WB) {
+    const double J23 = pow(J, 2.0 / 3.0);
+    aB = 1.0 / J23;
+    aI = -I1 / (3.0 * J23);
+    bI = (J * J - 1.0 / (J * J)) / 4.0;
+  } else {
+    const double p = pow(J, 2.0 / 3.0 - K / mu);
+    const double lnJ = log(J);
+    aB = 1.0;
+    aI = -p * (1.0 + (K / mu) * lnJ);
+    bI = p * lnJ;
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      dmu[i][j] = aB * B[i][j] + (i == j ? aI : 0.0);
+      dK[i][j] = (i == j ? bI : 0.0);
+    }
+}
+
+// One thread per (element, quadrature point).  gX is [nNodes][dim], gP is [nElements][2] (mu, K);
+// both are accumulated into (the caller zeroes them).
+template <int SHAPE, int RULE>
+__global__ void adjoint_tl_kernel(int64_t nEl, const int32_t* __restrict__ conn, const int32_t* __restrict__ nodeDof,
+                                  const double* __restrict__ coords, const double* __restrict__ U,
+                                  const double* __restrict__ lam, const double* __restrict__ props, int nProps,
+                                  int material, const double* __restrict__ thickness, Hexa20Fix fix, double* gX,
+                                  double* gP) {
+  constexpr int DIM = ShapeInfo<SHAPE>::DIM, NN = ShapeInfo<SHAPE>::NN, NQ = RuleInfo<RULE>::NQ;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nEl * NQ) return;
+  const int64_t e = t / NQ;
+  const int q = (int)(t % NQ);
+  double xi, eta, zeta, w;
+  quadrature_point(RULE, q, xi, eta, zeta, w);
+  const double p[3] = {eta, xi, zeta};
+  double D[DIM][NN];
+  shape_derivatives<SHAPE>(p, D);
+  double X[NN][DIM], Ua[NN][DIM], La[NN][DIM];
+  for (int a = 0; a < NN; ++a) {
+    const int32_t n = conn[e * NN + a];
+    const int32_t dof = nodeDof[n];
+    for (int c = 0; c < DIM; ++c) {
+      X[a][c] = coords[(int64_t)n * DIM + c];
+      Ua[a][c] = U[dof + c];
+      La[a][c] = lam[dof + c];
+    }
+  }
+  // Jacobian table row 2 of Hexa20 carries (zeta - xi) * inv(A)[5] (the reference's _J3D20)
+  const double quirk = (SHAPE == EFE_HEXA20) ? (zeta - xi) : 0.0;
+  double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 1}};
+  for (int r = 0; r < DIM; ++r)
+    for (int c = 0; c < DIM; ++c) {
+      double s = 0.0;
+      for (int a = 0; a < NN; ++a) s += (D[r][a] + (r == 2 ? quirk * fix.r[a % 20] : 0.0)) * X[a][c];
+      J[r][c] = s;
+    }
+  double detJ, iJ[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 1}};
+  if constexpr (DIM == 2) {
+    detJ = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    iJ[0][0] = J[1][1] / detJ;
+    iJ[0][1] = -J[0][1] / detJ;
+    iJ[1][0] = -J[1][0] / detJ;
+    iJ[1][1] = J[0][0] / detJ;
+  } else {
+    detJ = det3(J);
+    inv3(J, detJ, iJ);
+  }
+  double G[DIM][NN];
+  for (int c = 0; c < DIM; ++c)
+    for (int a = 0; a < NN; ++a) {
+      double s = 0.0;
+      for (int r = 0; r < DIM; ++r) s += iJ[c][r] * D[r][a];
+      G[c][a] = s;
+    }
+  const double th = (DIM == 2 && thickness) ? thickness[e] : 1.0;
+  const double s = detJ * w * th;
+  double F[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  for (int i = 0; i < DIM; ++i)
+    for (int j = 0; j < DIM; ++j) {
+      double h = 0.0;
+      for (int a = 0; a < NN; ++a) h += Ua[a][i] * G[j][a];
+      F[i][j] += h;
+    }
+  const double Jf = det3(F);
+  double iF[3][3];
+  inv3(F, Jf, iF);
+  const double mu = props[e * nProps + 0], Kb = props[e * nProps + 1];
+  NeoHookeOut o;
+  neo_hooke(material, mu, Kb, F, o);
+  double Lam[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int i = 0; i < DIM; ++i)
+    for (int k = 0; k < DIM; ++k) {
+      double v = 0.0;
+      for (int a = 0; a < NN; ++a) v += La[a][i] * G[k][a];
+      Lam[i][k] = v;
+    }
+  double M[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) M[i][j] = Lam[i][0] * iF[0][j] + Lam[i][1] * iF[1][j] + Lam[i][2] * iF[2][j];
+  double phi = 0.0, trM = M[0][0] + M[1][1] + M[2][2], MB = 0.0;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      phi += o.tau[i][j] * M[i][j];
+      MB += M[i][j] * o.Bm[i][j];
+    }
+  // parameter derivatives
+  {
+    double dmu[3][3], dK[3][3];
+    neo_hooke_param_derivatives(material, mu, Kb, F, dmu, dK);
+    double gm = 0.0, gk = 0.0;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        gm += dmu[i][j] * M[i][j];
+        gk += dK[i][j] * M[i][j];
+      }
+    atomicAdd(gP + 2 * e + 0, -s * gm);
+    atomicAdd(gP + 2 * e + 1, -s * gk);
+  }
+  // dphi/dF and dphi/dLambda, scaled by dL/dphi = -s
+  double MF[3][3], MtF[3][3], T1[3][3], Fbar[3][3], Lbar[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      MF[i][j] = M[i][0] * F[0][j] + M[i][1] * F[1][j] + M[i][2] * F[2][j];
+      MtF[i][j] = M[0][i] * F[0][j] + M[1][i] * F[1][j] + M[2][i] * F[2][j];
+    }
+  // T1 = Lambda^T tau ; Fbar -= iF^T T1 iF^T
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) T1[i][j] = Lam[0][i] * o.tau[0][j] + Lam[1][i] * o.tau[1][j] + Lam[2][i] * o.tau[2][j];
+  double T2[3][3];  // T1 iF^T
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) T2[i][j] = T1[i][0] * iF[j][0] + T1[i][1] * iF[j][1] + T1[i][2] * iF[j][2];
+  const double cI = o.c2 * trM + o.c3 * MB;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      const double iFt_T2 = iF[0][i] * T2[0][j] + iF[1][i] * T2[1][j] + iF[2][i] * T2[2][j];
+      const double v = o.c1 * (MF[i][j] + MtF[i][j]) + cI * iF[j][i] + o.c4 * trM * F[i][j] - iFt_T2;
+      Fbar[i][j] = -s * v;
+      Lbar[i][j] = -s * (o.tau[i][0] * iF[j][0] + o.tau[i][1] * iF[j][1] + o.tau[i][2] * iF[j][2]);
+    }
+  const double sbar = -phi;
+  // Gbar[k][a] = sum_i Fbar[i][k] U[a][i] + Lbar[i][k] lambda[a][i]
+  double Gbar[DIM][NN];
+  for (int k = 0; k < DIM; ++k)
+    for (int a = 0; a < NN; ++a) {
+      double v = 0.0;
+      for (int i = 0; i < DIM; ++i) v += Fbar[i][k] * Ua[a][i] + Lbar[i][k] * La[a][i];
+      Gbar[k][a] = v;
+    }
+  // G = iJ D: iJbar[c][r] = sum_a Gbar[c][a] D[r][a]
+  double iJbar[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int c = 0; c < DIM; ++c)
+    for (int r = 0; r < DIM; ++r) {
+      double v = 0.0;
+      for (int a = 0; a < NN; ++a) v += Gbar[c][a] * D[r][a];
+      iJbar[c][r] = v;
+    }
+  // Jbar = -iJ^T iJbar iJ^T + sbar * w * t * detJ * iJ^T
+  double Jbar[3][3];
+  for (int r = 0; r < DIM; ++r)
+    for (int c = 0; c < DIM; ++c) {
+      double v = 0.0;
+      for (int k = 0; k < DIM; ++k)
+        for (int l = 0; l < DIM; ++l) v += iJ[k][r] * iJbar[k][l] * iJ[c][l];
+      Jbar[r][c] = -v + sbar * w * th * detJ * iJ[c][r];
+    }
+  for (int a = 0; a < NN; ++a) {
+    const int32_t n = conn[e * NN + a];
+    for (int c = 0; c < DIM; ++c) {
+      double v = 0.0;
+      for (int r = 0; r < DIM; ++r) v += Jbar[r][c] * (D[r][a] + (r == 2 ? quirk * fix.r[a % 20] : 0.0));
+      atomicAdd(gX + (int64_t)n * DIM + c, v);
+    }
+  }
+}
+
+template <int SHAPE, int RULE>
+cudaError_t launch_adjoint_tl(const AdjointArgs& a, cudaStream_t st) {
+  const int64_t n = a.nEl * RuleInfo<RULE>::NQ;
+  if (n == 0) return cudaSuccess;
+  const int nt = 64;
+  adjoint_tl_kernel<SHAPE, RULE><<<(unsigned)((n + nt - 1) / nt), nt, 0, st>>>(
+      a.nEl, a.conn, a.nodeDof, a.coords, a.U, a.lam, a.props, a.nProps, a.material, a.thickness, a.fix, a.gX, a.gP);
+  return cudaGetLastError();
+}
+
+}  // namespace efe

@@ -1,5 +1,5 @@
 // efe_hexa20.cu -- kernel instantiations for the hexa20 element shape (one translation unit per shape).
-#include "efe_launch.cuh"
+#include "efe_adjoint.cuh"
 
 namespace efe {
 
@@ -26,6 +26,14 @@ cudaError_t body_force_hexa20(int rule, int64_t nSel, const int32_t* elems, cons
   switch (rule) {
     case EFE_RULE_3D_2X2X2: return launch_body_force<EFE_HEXA20, EFE_RULE_3D_2X2X2>(nSel, elems, conn, nodeDof, S, f, P, st);
     case EFE_RULE_3D_3X3X3: return launch_body_force<EFE_HEXA20, EFE_RULE_3D_3X3X3>(nSel, elems, conn, nodeDof, S, f, P, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t adjoint_tl_hexa20(int rule, const AdjointArgs& a, cudaStream_t st) {
+  switch (rule) {
+    case EFE_RULE_3D_2X2X2: return launch_adjoint_tl<EFE_HEXA20, EFE_RULE_3D_2X2X2>(a, st);
+    case EFE_RULE_3D_3X3X3: return launch_adjoint_tl<EFE_HEXA20, EFE_RULE_3D_3X3X3>(a, st);
   }
   return cudaErrorInvalidValue;
 }

@@ -55,6 +55,24 @@ cudaError_t launch_body_force(int64_t nSel, const int32_t* elems, const int32_t*
   return cudaGetLastError();
 }
 
+struct AdjointArgs {
+  int64_t nEl;
+  const int32_t* conn;
+  const int32_t* nodeDof;
+  const double* coords;
+  const double* U;
+  const double* lam;
+  const double* props;
+  int nProps, material;
+  const double* thickness;
+  Hexa20Fix fix;
+  double* gX;
+  double* gP;
+};
+
+template <int SHAPE, int RULE>
+cudaError_t launch_adjoint_tl(const AdjointArgs& a, cudaStream_t st);
+
 // form selector: small strain 3D/2D, total Lagrangian hyperelastic, total Lagrangian hypoelastic 3D/2D
 template <int SHAPE, int RULE, typename KT>
 cudaError_t launch_form(int form, const GroupArgs& g, cudaStream_t st) {
@@ -94,6 +112,10 @@ EFE_BODY_DECL(quad8)
 EFE_BODY_DECL(hexa8)
 EFE_BODY_DECL(hexa20)
 #undef EFE_BODY_DECL
+cudaError_t adjoint_tl_quad4(int rule, const AdjointArgs& a, cudaStream_t st);
+cudaError_t adjoint_tl_quad8(int rule, const AdjointArgs& a, cudaStream_t st);
+cudaError_t adjoint_tl_hexa8(int rule, const AdjointArgs& a, cudaStream_t st);
+cudaError_t adjoint_tl_hexa20(int rule, const AdjointArgs& a, cudaStream_t st);
 #define EFE_GEOMETRY_DECL(name)                                                                          \
   cudaError_t geometry_##name(int rule, int64_t nEl, int64_t off, const int32_t* conn, const double* coords, \
                               const double* th, double* G, float* G32, double* S, int32_t* status,            \

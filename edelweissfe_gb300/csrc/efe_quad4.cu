@@ -1,5 +1,5 @@
 // efe_quad4.cu -- kernel instantiations for the quad4 element shape (one translation unit per shape).
-#include "efe_launch.cuh"
+#include "efe_adjoint.cuh"
 
 namespace efe {
 
@@ -29,6 +29,15 @@ cudaError_t body_force_quad4(int rule, int64_t nSel, const int32_t* elems, const
     case EFE_RULE_2D_1: return launch_body_force<EFE_QUAD4, EFE_RULE_2D_1>(nSel, elems, conn, nodeDof, S, f, P, st);
     case EFE_RULE_2D_2X2: return launch_body_force<EFE_QUAD4, EFE_RULE_2D_2X2>(nSel, elems, conn, nodeDof, S, f, P, st);
     case EFE_RULE_2D_3X3: return launch_body_force<EFE_QUAD4, EFE_RULE_2D_3X3>(nSel, elems, conn, nodeDof, S, f, P, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t adjoint_tl_quad4(int rule, const AdjointArgs& a, cudaStream_t st) {
+  switch (rule) {
+    case EFE_RULE_2D_1: return launch_adjoint_tl<EFE_QUAD4, EFE_RULE_2D_1>(a, st);
+    case EFE_RULE_2D_2X2: return launch_adjoint_tl<EFE_QUAD4, EFE_RULE_2D_2X2>(a, st);
+    case EFE_RULE_2D_3X3: return launch_adjoint_tl<EFE_QUAD4, EFE_RULE_2D_3X3>(a, st);
   }
   return cudaErrorInvalidValue;
 }

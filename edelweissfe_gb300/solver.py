@@ -148,7 +148,7 @@ class NISTGPU:
 
     def __init__(self, assembler, linsolver="pcg", extrapolation="linear", maxIter=10, criticalIter=5,
                  maxGrowingIter=10, fluxResidualTolerance=1e-8, fluxResidualToleranceAlternative=5e-3,
-                 fieldCorrectionTolerance=1e-8, pcgTolerance=1e-12, pcgMaxIter=20000):  # fmt: skip
+                 fieldCorrectionTolerance=1e-8, pcgTolerance=1e-12, pcgMaxIter=20000, fluxResidualFloor=1e-7):  # fmt: skip
         self.asm = assembler
         self.linsolver = linsolver
         self.extrapolation = extrapolation
@@ -160,6 +160,7 @@ class NISTGPU:
         self.corrTol = fieldCorrectionTolerance
         self.pcgTolerance = pcgTolerance
         self.pcgMaxIter = pcgMaxIter
+        self.fluxFloor = fluxResidualFloor
         self.nAccumulatedFluxes = sum(len(g.conn) * len(g.conn[0]) * assembler.dim for g in assembler.groups if len(g.conn))
         dev = assembler.device
         ip, ix = assembler.indptr_host, assembler.indices_host
@@ -247,7 +248,7 @@ class NISTGPU:
                 avgFlux = max(1e-10, float(F.abs().sum()) / self.nAccumulatedFluxes)
                 corr = float(ddU.abs().max()) if ddU is not None else 0.0
                 tol = self.fluxTol if it < 15 else self.fluxTolAlt
-                converged = corr < self.corrTol and flux <= max(tol * avgFlux, 1e-7)
+                converged = corr < self.corrTol and flux <= max(tol * avgFlux, self.fluxFloor)
                 if flux > prevFlux:
                     nGrew += 1
                 prevFlux = flux
@@ -264,6 +265,15 @@ class NISTGPU:
             dU = dU + ddU
             it += 1
         return U_np, dU, P, it, residuals
+
+    def tangentAt(self, U):
+        """The tangent K (CSR data) at total displacement U with a zero increment (no state change)."""
+        asm = self.asm
+        P, F, K = asm.constructDofVector(), asm.constructDofVector(), asm.constructSystemMatrix()
+        asm.status.zero_()
+        asm.launch(U, torch.zeros_like(U), P, K, F)
+        asm.check_status()
+        return K
 
     # ------------------------------------------------------------------ linear solve
     def linearSolve(self, K, R, dir_idx):

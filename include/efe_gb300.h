@@ -155,6 +155,17 @@ int32_t efe_compute_elements(const EfeMesh* mesh, const EfeGroup* groups, int32_
 int32_t efe_body_force(const EfeMesh* mesh, const EfeGroup* group, const int32_t* elements, int64_t nSelected,
                        const double* force, double* P, void* stream);
 
+/* Adjoint of the total-Lagrangian hyperelastic element residual (no reference counterpart: the
+   reference has no derivatives; this differentiates the residual of
+   elements/displacementtlelement/element.py:389-414 with the Neo-Hooke materials of
+   materials/neohooke/).  For L = lambda^T P(X, U, mu, K) it adds dL/dX to gX ([nNodes][dim], node
+   order of the mesh coordinates) and dL/dmu, dL/dK to gParams ([nElements][2]).  With K lambda =
+   dJ/dU (lambda = 0 on prescribed DOFs), these are the gradients dJ/dX and dJ/d(mu, K) of an
+   objective J(U) at equilibrium.  U, lambda: device DOF vectors.  Total-Lagrangian groups with
+   EFE_MAT_NEOHOOKE_* only. */
+int32_t efe_adjoint_tl(const EfeMesh* mesh, const EfeGroup* group, const double* U, const double* lambda, double* gX,
+                       double* gParams, void* stream);
+
 /* acceptLastState: stateTemp -> stateRef and auxTemp -> auxRef for every group. */
 int32_t efe_accept_state(const EfeGroup* groups, int32_t nGroups, void* stream);
 
