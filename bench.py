@@ -146,7 +146,7 @@ def run_gpu(args, rank, world):
     results = {}
     state = {}
     sampler.start()
-    for precision in (("fp64", "mixed") if args.precision == "both" else (args.precision,)):
+    for precision in (("fp64", "mixed", "mixed-ff") if args.precision == "both" else (args.precision,)):
         asm = GPUAssembler(coords, nodeDof, nDof, [ElementGroup("C3D8", "vonmises", VM, conn)], precision=precision,
                            device=dev)  # fmt: skip
         P, F, K = asm.constructDofVector(), asm.constructDofVector(), asm.constructSystemMatrix()
@@ -199,6 +199,10 @@ def run_gpu(args, rank, world):
     if len(state) < 2:
         return results, {}, clocks, nEl, nDof, len(coords)
     errs = {
+        "R_rel_mixed_ff_vs_fp64": float((state["mixed-ff"]["P"] - state["fp64"]["P"]).abs().max()
+                                        / state["fp64"]["P"].abs().max()),
+        "state_rel_mixed_ff_vs_fp64": float(np.abs(state["mixed-ff"]["st"] - state["fp64"]["st"]).max()
+                                            / np.abs(state["fp64"]["st"]).max()),
         "R_rel_mixed_vs_fp64": float((state["mixed"]["P"] - state["fp64"]["P"]).abs().max()
                                      / state["fp64"]["P"].abs().max()),
         "K_rel_mixed_vs_fp64": float((state["mixed"]["K"] - state["fp64"]["K"]).abs().max()
@@ -334,7 +338,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_CUBE, help="elements per cube edge")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64"],
+    ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64", "mixed-ff"],
                     help="profiling aid: run one mode only (the JSON line needs both)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
@@ -390,6 +394,8 @@ def main():
         },
         "fp64": {"value": world * nEl / (fp64["ms"] * 1e-3), "ms_per_step": fp64["ms"], "kernel_ms": fp64["kernel_ms"]},
         "mixed_over_fp64": fp64["ms"] / mixed["ms"],
+        "mixed_ff": {"value": world * nEl / (results["mixed-ff"]["ms"] * 1e-3), "ms_per_step": results["mixed-ff"]["ms"],
+                     "kernel_ms": results["mixed-ff"]["kernel_ms"]},
         "errors": errs,
         "roofline": {
             "bound": "hbm",

@@ -18,7 +18,7 @@ EFE_SMALL_STRAIN, EFE_TOTAL_LAGRANGIAN = 0, 1
 EFE_SOLID, EFE_PLANE_STRAIN, EFE_PLANE_STRESS = 0, 1, 2
 EFE_MAT_LINEAR_ELASTIC, EFE_MAT_VON_MISES = 0, 1
 EFE_MAT_NEOHOOKE_WA, EFE_MAT_NEOHOOKE_WB, EFE_MAT_NEOHOOKE_WC = 2, 3, 4
-EFE_K_FP64, EFE_K_FP32 = 0, 1
+EFE_K_FP64, EFE_K_FP32, EFE_K_FP32_FF = 0, 1, 2
 EFE_STATUS_CUTBACK, EFE_STATUS_BAD_JACOBIAN, EFE_STATUS_NONFINITE = 1, 2, 4
 EFE_OK, EFE_ERR_ARGUMENT, EFE_ERR_UNSUPPORTED, EFE_ERR_CUDA, EFE_ERR_PATTERN = 0, 1, 2, 3, 4
 
@@ -67,6 +67,7 @@ class EfeGroup(ctypes.Structure):
         ("thickness", ctypes.c_void_p),
         ("geomG", ctypes.c_void_p),
         ("geomG32", ctypes.c_void_p),
+        ("geomGlo", ctypes.c_void_p),
         ("geomS", ctypes.c_void_p),
         ("stateRef", ctypes.c_void_p),
         ("stateTemp", ctypes.c_void_p),

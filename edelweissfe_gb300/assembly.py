@@ -58,7 +58,9 @@ class GPUAssembler:
     coords: [nNodes, dim] reference coordinates; nodeDof: [nNodes] first DOF of each node
     (-1 for nodes without DOFs; DofManager numbering, `numerics/dofmanager.py:259-300`);
     nDof: size of the DOF vectors; groups: ElementGroup list in the reference's element order.
-    precision: "fp64" (everything FP64) or "mixed" (FP32 tangent, FP64 residual and state)."""
+    precision: "fp64" (everything FP64), "mixed" (FP32 tangent, FP64 residual and state) or
+    "mixed-ff" (as "mixed", with the small-strain strain increment and element residual in
+    float-float arithmetic; the return map, state and global residual accumulation stay FP64)."""
 
     def __init__(self, coords, nodeDof, nDof, groups, precision="fp64", device=None):
         self.lib = L.load()
@@ -75,7 +77,7 @@ class GPUAssembler:
         self.nodeDof_host = np.ascontiguousarray(nodeDof, np.int32)
         self.groups = list(groups)
         self.precision = precision
-        self.kPrecision = {"fp64": L.EFE_K_FP64, "mixed": L.EFE_K_FP32}[precision]
+        self.kPrecision = {"fp64": L.EFE_K_FP64, "mixed": L.EFE_K_FP32, "mixed-ff": L.EFE_K_FP32_FF}[precision]
         self.kdtype = torch.float64 if precision == "fp64" else torch.float32
         self._build_pattern()
         dev = self.device
@@ -137,8 +139,10 @@ class GPUAssembler:
         d["props"] = _upload(props, np.float64, dev)
         d["thickness"] = _upload(th, np.float64, dev)
         d["geomG"] = torch.zeros((et.dim * et.nNodes, nPts), dtype=torch.float64, device=dev)
-        if self.kPrecision == L.EFE_K_FP32:
+        if self.kPrecision in (L.EFE_K_FP32, L.EFE_K_FP32_FF):
             d["geomG32"] = torch.zeros((et.dim * et.nNodes, nPts), dtype=torch.float32, device=dev)
+        if self.kPrecision == L.EFE_K_FP32_FF:
+            d["geomGlo"] = torch.zeros((et.dim * et.nNodes, nPts), dtype=torch.float32, device=dev)
         d["geomS"] = torch.zeros(nPts, dtype=torch.float64, device=dev)
         d["stateRef"] = torch.zeros((S, nPts), dtype=torch.float64, device=dev)
         d["stateTemp"] = torch.zeros((S, nPts), dtype=torch.float64, device=dev)
@@ -153,7 +157,8 @@ class GPUAssembler:
             et.shape, et.rule, et.kinematics, et.plane, mcode, props.shape[1], E, offset,
             d["conn"].data_ptr(), d["pairSlot"].data_ptr(), d["props"].data_ptr(),
             d["thickness"].data_ptr() if et.dim == 2 else None,
-            d["geomG"].data_ptr(), d["geomG32"].data_ptr() if "geomG32" in d else None, d["geomS"].data_ptr(), d["stateRef"].data_ptr(), d["stateTemp"].data_ptr(),
+            d["geomG"].data_ptr(), d["geomG32"].data_ptr() if "geomG32" in d else None,
+            d["geomGlo"].data_ptr() if "geomGlo" in d else None, d["geomS"].data_ptr(), d["stateRef"].data_ptr(), d["stateTemp"].data_ptr(),
             d["auxRef"].data_ptr() if et.totalLagrangian else None,
             d["auxTemp"].data_ptr() if et.totalLagrangian else None,
         )  # fmt: skip

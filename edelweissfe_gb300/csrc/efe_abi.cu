@@ -219,19 +219,19 @@ int32_t efe_setup_geometry(const EfeMesh* mesh, const EfeGroup* g, int32_t* stat
   switch (g->shape) {
     case EFE_QUAD4:
       e = efe::geometry_quad4(g->rule, g->nElements, g->elementOffset, g->conn, mesh->coords, g->thickness, g->geomG,
-                              g->geomG32, g->geomS, status, fix, st);
+                              g->geomG32, g->geomGlo, g->geomS, status, fix, st);
       break;
     case EFE_QUAD8:
       e = efe::geometry_quad8(g->rule, g->nElements, g->elementOffset, g->conn, mesh->coords, g->thickness, g->geomG,
-                              g->geomG32, g->geomS, status, fix, st);
+                              g->geomG32, g->geomGlo, g->geomS, status, fix, st);
       break;
     case EFE_HEXA8:
       e = efe::geometry_hexa8(g->rule, g->nElements, g->elementOffset, g->conn, mesh->coords, nullptr, g->geomG,
-                              g->geomG32, g->geomS, status, fix, st);
+                              g->geomG32, g->geomGlo, g->geomS, status, fix, st);
       break;
     case EFE_HEXA20:
       e = efe::geometry_hexa20(g->rule, g->nElements, g->elementOffset, g->conn, mesh->coords, nullptr, g->geomG,
-                               g->geomG32, g->geomS, status, fix, st);
+                               g->geomG32, g->geomGlo, g->geomS, status, fix, st);
       break;
   }
   if (e != cudaSuccess) return cuda_fail(e, "efe_setup_geometry");
@@ -245,7 +245,8 @@ int32_t efe_compute_elements(const EfeMesh* mesh, const EfeGroup* groups, int32_
   (void)dT;
   if (!mesh || !groups || nGroups < 0 || !Kdata || !P || !F || !status)
     return fail(EFE_ERR_ARGUMENT, "null argument");
-  if (kPrecision != EFE_K_FP64 && kPrecision != EFE_K_FP32) return fail(EFE_ERR_ARGUMENT, "unknown K precision");
+  if (kPrecision != EFE_K_FP64 && kPrecision != EFE_K_FP32 && kPrecision != EFE_K_FP32_FF)
+    return fail(EFE_ERR_ARGUMENT, "unknown K precision");
   if (!mesh->nodeDof || !mesh->nodeRowLen) return fail(EFE_ERR_ARGUMENT, "mesh without DOF map");
   cudaStream_t st = (cudaStream_t)stream;
   for (int32_t i = 0; i < nGroups; ++i) {
@@ -258,6 +259,8 @@ int32_t efe_compute_elements(const EfeMesh* mesh, const EfeGroup* groups, int32_
       return fail(EFE_ERR_ARGUMENT, "null group buffer");
     if (tl && (!U || !gr.auxTemp)) return fail(EFE_ERR_ARGUMENT, "total-Lagrangian group needs U and auxTemp");
     if (!tl && !dU) return fail(EFE_ERR_ARGUMENT, "small-strain group needs dU");
+    if (kPrecision == EFE_K_FP32_FF && form_of(gr) == efe::SS3 && (!gr.geomG32 || !gr.geomGlo))
+      return fail(EFE_ERR_ARGUMENT, "EFE_K_FP32_FF needs geomG32 and geomGlo");
     efe::GroupArgs a;
     a.nElements = gr.nElements;
     a.elementOffset = gr.elementOffset;
@@ -267,6 +270,7 @@ int32_t efe_compute_elements(const EfeMesh* mesh, const EfeGroup* groups, int32_
     a.thickness = gr.thickness;
     a.geomG = gr.geomG;
     a.geomG32 = gr.geomG32;
+    a.geomGlo = gr.geomGlo;
     a.geomS = gr.geomS;
     a.stateRef = gr.stateRef;
     a.stateTemp = gr.stateTemp;

@@ -203,6 +203,39 @@ __device__ __forceinline__ void inv3(const double A[3][3], double d, double B[3]
   B[2][2] = (A[0][0] * A[1][1] - A[0][1] * A[1][0]) * id;
 }
 
+// ------------------------------------------------------------------ float-float arithmetic
+// A value x is carried as hi + lo with hi = fl32(x), lo = fl32(x - hi) (~48 significant bits).
+// Error-free product (FMA) and sum (Knuth's two-sum) use the _rn intrinsics so that the compiler
+// cannot contract or reorder them.
+struct ff {
+  float h, l;
+};
+__device__ __forceinline__ ff ff_split(double x) {
+  const float h = __double2float_rn(x);
+  return ff{h, __double2float_rn(x - (double)h)};
+}
+__device__ __forceinline__ double ff_to_double(ff a) { return (double)a.h + (double)a.l; }
+// acc += a * b
+__device__ __forceinline__ void ff_fma(ff& acc, ff a, ff b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  const float s = __fadd_rn(acc.h, p);
+  const float bb = __fsub_rn(s, acc.h);
+  const float err = __fadd_rn(__fsub_rn(acc.h, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  acc.l = __fadd_rn(acc.l, __fadd_rn(err, e));
+  acc.h = s;
+}
+// acc += a
+__device__ __forceinline__ void ff_add(ff& acc, ff a) {
+  const float s = __fadd_rn(acc.h, a.h);
+  const float bb = __fsub_rn(s, acc.h);
+  const float err = __fadd_rn(__fsub_rn(acc.h, __fsub_rn(s, bb)), __fsub_rn(a.h, bb));
+  acc.l = __fadd_rn(acc.l, __fadd_rn(err, a.l));
+  acc.h = s;
+}
+
 // ------------------------------------------------------------------ materials
 // Isotropic elasticity matrix entries, formed like the reference: f = E/((1+v)(1-2v)),
 // C11 = f(1-v), C12 = f v, C44 = f (1-2v)/2   (linearelastic.py:95-117, vonmises.py:126-149)

@@ -27,6 +27,7 @@ struct GroupArgs {
   const double* thickness;
   const double* geomG;
   const float* geomG32;  // optional FP32 copy of geomG, used for the FP32 tangent
+  const float* geomGlo;  // optional fl32(G - geomG32): with geomG32 the float-float form of G
   const double* geomS;
   const double* stateRef;
   double* stateTemp;
@@ -60,8 +61,8 @@ __device__ __forceinline__ void report(int32_t* status, int bits, int64_t global
 template <int SHAPE, int RULE>
 __global__ void geometry_kernel(int64_t nEl, int64_t elOffset, const int32_t* __restrict__ conn,
                                 const double* __restrict__ coords, const double* __restrict__ thickness,
-                                double* __restrict__ G, float* __restrict__ G32, double* __restrict__ S,
-                                int32_t* status, Hexa20Fix fix) {
+                                double* __restrict__ G, float* __restrict__ G32, float* __restrict__ Glo,
+                                double* __restrict__ S, int32_t* status, Hexa20Fix fix) {
   constexpr int DIM = ShapeInfo<SHAPE>::DIM, NN = ShapeInfo<SHAPE>::NN, NQ = RuleInfo<RULE>::NQ;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nEl * NQ) return;
@@ -111,6 +112,7 @@ __global__ void geometry_kernel(int64_t nEl, int64_t elOffset, const int32_t* __
       for (int r = 0; r < DIM; ++r) s += iJ[c][r] * dN[r][a];
       G[(int64_t)(c * NN + a) * stride + t] = s;
       if (G32) G32[(int64_t)(c * NN + a) * stride + t] = (float)s;
+      if (Glo) Glo[(int64_t)(c * NN + a) * stride + t] = (float)(s - (double)(float)s);
     }
   const double th = (DIM == 2 && thickness) ? thickness[e] : 1.0;
   S[t] = detJ * w * th;
@@ -171,7 +173,9 @@ __device__ __forceinline__ void kadd(KT* p, KT v) {
   atomicAdd(p, v);
 }
 
-template <int SHAPE, int RULE, int FORM, typename KT, int EPB, int NT, int MINB>
+// FF: the strain increment and the residual of the small-strain 3D form are formed in float-float
+// arithmetic from the float-float geometry (geomG32 + geomGlo); the return map stays FP64.
+template <int SHAPE, int RULE, int FORM, typename KT, int EPB, int NT, int MINB, bool FF = false>
 __global__ void __launch_bounds__(NT, MINB) assemble_kernel(GroupArgs g) {
   using L = Layout<SHAPE, RULE, FORM, KT, EPB>;
   constexpr int DIM = L::DIM, NN = L::NN, NQ = L::NQ, NVEC = L::NVEC, NSCAL = L::NSCAL, NDOF = L::NDOF;
@@ -195,7 +199,14 @@ __global__ void __launch_bounds__(NT, MINB) assemble_kernel(GroupArgs g) {
     if (e < nEl) {
       const int32_t node = g.conn[e * NN + a];
       const int32_t dof = g.nodeDof[node];
-      for (int c = 0; c < DIM; ++c) su[(le * NN + a) * DIM + c] = Ux[dof + c];
+      if constexpr (FF) {
+        // displacement relative to node 0 (sum_a dN_a/dX = 0): no cancellation in the strain sum
+        const int32_t dof0 = g.nodeDof[g.conn[e * NN]];
+        ff* sf = reinterpret_cast<ff*>(su);
+        for (int c = 0; c < DIM; ++c) sf[(le * NN + a) * DIM + c] = ff_split(Ux[dof + c] - Ux[dof0 + c]);
+      } else {
+        for (int c = 0; c < DIM; ++c) su[(le * NN + a) * DIM + c] = Ux[dof + c];
+      }
       srl[le * NN + a] = g.nodeRowLen[node];
     }
   }
@@ -216,10 +227,12 @@ __global__ void __launch_bounds__(NT, MINB) assemble_kernel(GroupArgs g) {
     if (e >= nEl) continue;
     const int64_t pt = e * NQ + q;
     double Gm[DIM][NN];
+    if constexpr (!FF) {
 #pragma unroll
-    for (int c = 0; c < DIM; ++c)
+      for (int c = 0; c < DIM; ++c)
 #pragma unroll
-      for (int a = 0; a < NN; ++a) Gm[c][a] = g.geomG[(int64_t)(c * NN + a) * stride + pt];
+        for (int a = 0; a < NN; ++a) Gm[c][a] = g.geomG[(int64_t)(c * NN + a) * stride + pt];
+    }
     const double s = g.geomS[pt];
     const double* u = su + le * NN * DIM;
     const double* props = g.props + e * g.nProps;
@@ -238,16 +251,36 @@ __global__ void __launch_bounds__(NT, MINB) assemble_kernel(GroupArgs g) {
     if constexpr (FORM == SS3 || FORM == SS2) {
       // ------------------------------------------------ small strain (element.py:318-346)
       double de[6] = {0, 0, 0, 0, 0, 0};
-      if constexpr (DIM == 3) {
+      ff Gf[DIM][NN];
+      if constexpr (FF) {
+        const ff* uf = reinterpret_cast<const ff*>(su) + le * NN * DIM;
+        ff acc[6] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}};
+        for (int a = 0; a < NN; ++a) {
+          for (int c = 0; c < DIM; ++c)
+            Gf[c][a] = ff{g.geomG32[(int64_t)(c * NN + a) * stride + pt], g.geomGlo[(int64_t)(c * NN + a) * stride + pt]};
+          const ff ux = uf[a * 3 + 0], uy = uf[a * 3 + 1], uz = uf[a * 3 + 2 % DIM];
+          ff_fma(acc[0], Gf[0][a], ux);
+          ff_fma(acc[1], Gf[1][a], uy);
+          ff_fma(acc[2], Gf[2 % DIM][a], uz);
+          ff_fma(acc[3], Gf[1][a], ux);
+          ff_fma(acc[3], Gf[0][a], uy);
+          ff_fma(acc[4], Gf[2 % DIM][a], ux);
+          ff_fma(acc[4], Gf[0][a], uz);
+          ff_fma(acc[5], Gf[2 % DIM][a], uy);
+          ff_fma(acc[5], Gf[1][a], uz);
+        }
+        for (int f = 0; f < 6; ++f) de[f] = ff_to_double(acc[f]);
+      } else if constexpr (DIM == 3) {
         for (int a = 0; a < NN; ++a) {
           const double ux = u[a * 3 + 0], uy = u[a * 3 + 1], uz = u[a * 3 + 2];
           const double gx = Gm[0][a], gy = Gm[1][a], gz = Gm[2][a];
-          de[0] += gx * ux;
-          de[1] += gy * uy;
-          de[2] += gz * uz;
-          de[3] += gy * ux + gx * uy;
-          de[4] += gz * ux + gx * uz;
-          de[5] += gz * uy + gy * uz;
+          // one FMA per product (B . dU, element.py:322)
+          de[0] = fma(gx, ux, de[0]);
+          de[1] = fma(gy, uy, de[1]);
+          de[2] = fma(gz, uz, de[2]);
+          de[3] = fma(gx, uy, fma(gy, ux, de[3]));
+          de[4] = fma(gx, uz, fma(gz, ux, de[4]));
+          de[5] = fma(gy, uz, fma(gz, uy, de[5]));
         }
       } else {
         for (int a = 0; a < NN; ++a) {
@@ -267,11 +300,32 @@ __global__ void __launch_bounds__(NT, MINB) assemble_kernel(GroupArgs g) {
         // residual r_a = s * sigma . G_a   (small-strain Voigt order 11,22,33,12,13,23)
         double ss[6];
         for (int f = 0; f < 6; ++f) ss[f] = sig[f] * s;
-        for (int a = 0; a < NN; ++a) {
-          const double gx = Gm[0][a], gy = Gm[1][a], gz = Gm[2 % DIM][a];
-          rq[a * DIM + 0] = ss[0] * gx + ss[3] * gy + ss[4] * gz;
-          rq[a * DIM + 1] = ss[3] * gx + ss[1] * gy + ss[5] * gz;
-          rq[a * DIM + 2 % DIM] = ss[4] * gx + ss[5] * gy + ss[2] * gz;
+        if constexpr (FF) {
+          ff sf[6];
+          for (int f = 0; f < 6; ++f) sf[f] = ff_split(ss[f]);
+          ff* rf = reinterpret_cast<ff*>(rq);
+          for (int a = 0; a < NN; ++a) {
+            ff r0{0, 0}, r1{0, 0}, r2{0, 0};
+            ff_fma(r0, sf[0], Gf[0][a]);
+            ff_fma(r0, sf[3], Gf[1][a]);
+            ff_fma(r0, sf[4], Gf[2 % DIM][a]);
+            ff_fma(r1, sf[3], Gf[0][a]);
+            ff_fma(r1, sf[1], Gf[1][a]);
+            ff_fma(r1, sf[5], Gf[2 % DIM][a]);
+            ff_fma(r2, sf[4], Gf[0][a]);
+            ff_fma(r2, sf[5], Gf[1][a]);
+            ff_fma(r2, sf[2], Gf[2 % DIM][a]);
+            rf[a * DIM + 0] = r0;
+            rf[a * DIM + 1] = r1;
+            rf[a * DIM + 2 % DIM] = r2;
+          }
+        } else {
+          for (int a = 0; a < NN; ++a) {
+            const double gx = Gm[0][a], gy = Gm[1][a], gz = Gm[2 % DIM][a];
+            rq[a * DIM + 0] = ss[0] * gx + ss[3] * gy + ss[4] * gz;
+            rq[a * DIM + 1] = ss[3] * gx + ss[1] * gy + ss[5] * gz;
+            rq[a * DIM + 2 % DIM] = ss[4] * gx + ss[5] * gy + ss[2] * gz;
+          }
         }
         sc[0] = (KT)(T.c12 * s);
         sc[1] = (KT)(T.c44 * s);
@@ -281,7 +335,11 @@ __global__ void __launch_bounds__(NT, MINB) assemble_kernel(GroupArgs g) {
         for (int f = 0; f < 6; ++f) n[f] = (KT)T.n[f];
         for (int a = 0; a < NN; ++a) {
           KT gx, gy, gz;
-          if (std::is_same<KT, float>::value && g.geomG32) {
+          if constexpr (FF) {
+            gx = (KT)Gf[0][a].h;
+            gy = (KT)Gf[1][a].h;
+            gz = (KT)Gf[2 % DIM][a].h;
+          } else if (std::is_same<KT, float>::value && g.geomG32) {
             gx = (KT)g.geomG32[(int64_t)(0 * NN + a) * stride + pt];
             gy = (KT)g.geomG32[(int64_t)(1 * NN + a) * stride + pt];
             gz = (KT)g.geomG32[(int64_t)(2 * NN + a) * stride + pt];
@@ -515,7 +573,14 @@ __global__ void __launch_bounds__(NT, MINB) assemble_kernel(GroupArgs g) {
     const int64_t e = e0 + le;
     if (e >= nEl) continue;
     double pe = 0.0;
-    for (int q = 0; q < NQ; ++q) pe -= sr[(le * NQ + q) * NDOF + k];
+    if constexpr (FF) {
+      const ff* rf = reinterpret_cast<const ff*>(sr);
+      ff acc{0, 0};
+      for (int q = 0; q < NQ; ++q) ff_add(acc, rf[(le * NQ + q) * NDOF + k]);
+      pe = -ff_to_double(acc);
+    } else {
+      for (int q = 0; q < NQ; ++q) pe -= sr[(le * NQ + q) * NDOF + k];
+    }
     const int a = k / DIM, c = k % DIM;
     const int32_t node = g.conn[e * NN + a];
     const int32_t dof = g.nodeDof[node] + c;

@@ -19,11 +19,11 @@ struct Tile {
   static constexpr int MINB = bytes <= 72 * 1024 ? 3 : 1;
 };
 
-template <int SHAPE, int RULE, int FORM, typename KT>
+template <int SHAPE, int RULE, int FORM, typename KT, bool FF = false>
 cudaError_t launch_assemble(const GroupArgs& g, cudaStream_t st) {
   using T = Tile<SHAPE, RULE, FORM, KT>;
   static_assert(T::bytes <= 200 * 1024, "tile does not fit in shared memory");
-  auto kern = assemble_kernel<SHAPE, RULE, FORM, KT, T::EPB, T::NT, T::MINB>;
+  auto kern = assemble_kernel<SHAPE, RULE, FORM, KT, T::EPB, T::NT, T::MINB, FF>;
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::bytes);
   if (err != cudaSuccess) return err;
   const int64_t grid = (g.nElements + T::EPB - 1) / T::EPB;
@@ -34,13 +34,13 @@ cudaError_t launch_assemble(const GroupArgs& g, cudaStream_t st) {
 
 template <int SHAPE, int RULE>
 cudaError_t launch_geometry(int64_t nEl, int64_t elOffset, const int32_t* conn, const double* coords,
-                            const double* thickness, double* G, float* G32, double* S, int32_t* status,
-                            const Hexa20Fix& fix, cudaStream_t st) {
+                            const double* thickness, double* G, float* G32, float* Glo, double* S,
+                            int32_t* status, const Hexa20Fix& fix, cudaStream_t st) {
   const int64_t n = nEl * RuleInfo<RULE>::NQ;
   if (n == 0) return cudaSuccess;
   const int nt = 128;
   geometry_kernel<SHAPE, RULE><<<(unsigned)((n + nt - 1) / nt), nt, 0, st>>>(nEl, elOffset, conn, coords, thickness,
-                                                                             G, G32, S, status, fix);
+                                                                             G, G32, Glo, S, status, fix);
   return cudaGetLastError();
 }
 
@@ -74,12 +74,12 @@ template <int SHAPE, int RULE>
 cudaError_t launch_adjoint_tl(const AdjointArgs& a, cudaStream_t st);
 
 // form selector: small strain 3D/2D, total Lagrangian hyperelastic, total Lagrangian hypoelastic 3D/2D
-template <int SHAPE, int RULE, typename KT>
+template <int SHAPE, int RULE, typename KT, bool FF = false>
 cudaError_t launch_form(int form, const GroupArgs& g, cudaStream_t st) {
   constexpr int DIM = ShapeInfo<SHAPE>::DIM;
   if constexpr (DIM == 3) {
     switch (form) {
-      case SS3: return launch_assemble<SHAPE, RULE, SS3, KT>(g, st);
+      case SS3: return launch_assemble<SHAPE, RULE, SS3, KT, FF>(g, st);
       case TLH: return launch_assemble<SHAPE, RULE, TLH, KT>(g, st);
       case TLV3: return launch_assemble<SHAPE, RULE, TLV3, KT>(g, st);
     }
@@ -95,6 +95,7 @@ cudaError_t launch_form(int form, const GroupArgs& g, cudaStream_t st) {
 
 template <int SHAPE, int RULE>
 cudaError_t launch_rule(int form, int kprec, const GroupArgs& g, cudaStream_t st) {
+  if (kprec == EFE_K_FP32_FF) return launch_form<SHAPE, RULE, float, true>(form, g, st);
   return kprec == EFE_K_FP32 ? launch_form<SHAPE, RULE, float>(form, g, st)
                              : launch_form<SHAPE, RULE, double>(form, g, st);
 }
@@ -118,8 +119,8 @@ cudaError_t adjoint_tl_hexa8(int rule, const AdjointArgs& a, cudaStream_t st);
 cudaError_t adjoint_tl_hexa20(int rule, const AdjointArgs& a, cudaStream_t st);
 #define EFE_GEOMETRY_DECL(name)                                                                          \
   cudaError_t geometry_##name(int rule, int64_t nEl, int64_t off, const int32_t* conn, const double* coords, \
-                              const double* th, double* G, float* G32, double* S, int32_t* status,            \
-                              const Hexa20Fix& fix, cudaStream_t st);
+                              const double* th, double* G, float* G32, float* Glo, double* S,                 \
+                              int32_t* status, const Hexa20Fix& fix, cudaStream_t st);
 EFE_GEOMETRY_DECL(quad4)
 EFE_GEOMETRY_DECL(quad8)
 EFE_GEOMETRY_DECL(hexa8)

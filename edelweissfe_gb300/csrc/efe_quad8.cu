@@ -12,11 +12,11 @@ cudaError_t assemble_quad8(int rule, int form, int kprec, const GroupArgs& g, cu
 }
 
 cudaError_t geometry_quad8(int rule, int64_t nEl, int64_t off, const int32_t* conn, const double* coords,
-                             const double* th, double* G, float* G32, double* S, int32_t* status,
-                             const Hexa20Fix& fix, cudaStream_t st) {
+                             const double* th, double* G, float* G32, float* Glo, double* S,
+                             int32_t* status, const Hexa20Fix& fix, cudaStream_t st) {
   switch (rule) {
-    case EFE_RULE_2D_2X2: return launch_geometry<EFE_QUAD8, EFE_RULE_2D_2X2>(nEl, off, conn, coords, th, G, G32, S, status, fix, st);
-    case EFE_RULE_2D_3X3: return launch_geometry<EFE_QUAD8, EFE_RULE_2D_3X3>(nEl, off, conn, coords, th, G, G32, S, status, fix, st);
+    case EFE_RULE_2D_2X2: return launch_geometry<EFE_QUAD8, EFE_RULE_2D_2X2>(nEl, off, conn, coords, th, G, G32, Glo, S, status, fix, st);
+    case EFE_RULE_2D_3X3: return launch_geometry<EFE_QUAD8, EFE_RULE_2D_3X3>(nEl, off, conn, coords, th, G, G32, Glo, S, status, fix, st);
   }
   return cudaErrorInvalidValue;
 }

@@ -71,8 +71,12 @@ enum {
 /* precision of the assembled tangent (CSR data) */
 enum {
   EFE_K_FP64 = 0, /* everything in FP64 (Kdata is double*)                                   */
-  EFE_K_FP32 = 1  /* tangent formed and accumulated in FP32 (Kdata is float*); residual, state
+  EFE_K_FP32 = 1, /* tangent formed and accumulated in FP32 (Kdata is float*); residual, state
                      and the return map stay FP64                                              */
+  EFE_K_FP32_FF = 2 /* as EFE_K_FP32, and for small-strain solids the strain increment and the
+                     element residual are formed in float-float arithmetic (~48-bit significand,
+                     needs geomG32 and geomGlo); the return map, state and the global residual
+                     accumulation stay FP64                                                    */
 };
 /* status words (int32[3], zeroed by the caller): status[0] = OR of EFE_STATUS_* bits,
    status[1] = INT32_MAX - (global index of the first failing element), 0 if none,
@@ -113,6 +117,8 @@ typedef struct EfeGroup {
   double* geomG;             /* [dim*nNodes][nElements*nInt]  dN_a/dX_c at row c*nNodes+a    */
   float* geomG32;            /* optional FP32 copy of geomG (same layout), read by the FP32
                                 tangent of EFE_K_FP32; NULL to convert geomG on the fly      */
+  float* geomGlo;            /* optional fl32(geomG - geomG32): geomG32 + geomGlo is geomG in
+                                float-float form (EFE_K_FP32_FF)                              */
   double* geomS;             /* [nElements*nInt]  det J * weight * thickness                 */
   double* stateRef;          /* [12 + nMatState][nElements*nInt]  stress(6) strain(6) material;
                                 read by efe_compute_elements, written by efe_accept_state      */
