@@ -31,6 +31,7 @@ EXPORTS = [
     "efe_shape_nodes",
     "efe_setup_geometry",
     "efe_compute_elements",
+    "efe_compute_elements_persistent",
     "efe_accept_state",
     "efe_body_force",
     "efe_adjoint_tl",
@@ -73,6 +74,19 @@ class EfeGroup(ctypes.Structure):
         ("stateTemp", ctypes.c_void_p),
         ("auxRef", ctypes.c_void_p),
         ("auxTemp", ctypes.c_void_p),
+        ("tileVariant", ctypes.c_int32),
+    ]
+
+
+class EfeWorkItem(ctypes.Structure):
+    _fields_ = [
+        ("mesh", ctypes.c_void_p),
+        ("group", ctypes.c_void_p),
+        ("U", ctypes.c_void_p),
+        ("dU", ctypes.c_void_p),
+        ("Kdata", ctypes.c_void_p),
+        ("P", ctypes.c_void_p),
+        ("F", ctypes.c_void_p),
     ]
 
 
@@ -130,6 +144,8 @@ def load(build_if_missing=False):
     lib.efe_body_force.argtypes = [ctypes.POINTER(EfeMesh), ctypes.POINTER(EfeGroup), P, i64, P, P, P]
     lib.efe_adjoint_tl.restype = i32
     lib.efe_adjoint_tl.argtypes = [ctypes.POINTER(EfeMesh), ctypes.POINTER(EfeGroup), P, P, P, P, P]
+    lib.efe_compute_elements_persistent.restype = i32
+    lib.efe_compute_elements_persistent.argtypes = [ctypes.POINTER(EfeWorkItem), i32, i32, P, P, P]
     lib.efe_accept_state.restype = i32
     lib.efe_accept_state.argtypes = [ctypes.POINTER(EfeGroup), i32, P]
     lib.efe_pattern_count.restype = i64

@@ -1,0 +1,126 @@
+"""Batches of independent meshes of uneven size and mixed element types in one element pass.
+
+Meshes of one dimension are concatenated into one block-diagonal system (`MeshBatch`): their
+nodes, DOFs and CSR rows are stacked, so one group spans every mesh of a batch and each mesh's
+DOF vectors and CSR data are contiguous slices of the batch's.  `BatchedPass` runs the element
+pass of up to two batches (e.g. the 2D and the 3D meshes) either as one persistent launch
+(`efe_compute_elements_persistent`: the resident CTAs take tiles of both batches from one work
+counter) or as one launch per batch, and can capture the whole pass (zeroing of P, F, K and the
+launches) in a CUDA graph.
+"""
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from .assembly import ElementGroup, GPUAssembler
+
+
+class MeshBatch:
+    """meshes: list of dicts with coords [n, d], conn [E, nN], nodeDof [n], nDof, props [nP] or [E, nP],
+    thickness (2D); all of one element type and material."""
+
+    def __init__(self, meshes, elType, material, precision="mixed", device=None):
+        node_off = np.cumsum([0] + [len(m["coords"]) for m in meshes])
+        dof_off = np.cumsum([0] + [int(m["nDof"]) for m in meshes])
+        el_off = np.cumsum([0] + [len(m["conn"]) for m in meshes])
+        coords = np.concatenate([m["coords"] for m in meshes])
+        nodeDof = np.concatenate([np.where(m["nodeDof"] >= 0, m["nodeDof"] + dof_off[i], -1)
+                                  for i, m in enumerate(meshes)])  # fmt: skip
+        conn = np.concatenate([m["conn"] + node_off[i] for i, m in enumerate(meshes)])
+        props = np.concatenate([np.broadcast_to(np.asarray(m["props"], float), (len(m["conn"]), len(m["props"]) if
+                                np.ndim(m["props"]) == 1 else np.shape(m["props"])[1])) for m in meshes])  # fmt: skip
+        thickness = np.concatenate([np.broadcast_to(np.asarray(m.get("thickness", 1.0), float), (len(m["conn"]),))
+                                    for m in meshes])  # fmt: skip
+        self.asm = GPUAssembler(coords, nodeDof, int(dof_off[-1]),
+                                [ElementGroup(elType, material, props, conn, thickness)],
+                                precision=precision, device=device)  # fmt: skip
+        self.nMeshes = len(meshes)
+        self.dof_offsets = dof_off
+        self.element_offsets = el_off
+        ip = self.asm.indptr_host
+        self.nnz_offsets = np.array([ip[d] for d in dof_off])
+        self.nElements = int(el_off[-1])
+        self.U = self.asm.constructDofVector()
+        self.dU = self.asm.constructDofVector()
+        self.P = self.asm.constructDofVector()
+        self.F = self.asm.constructDofVector()
+        self.K = self.asm.constructSystemMatrix()
+
+    def mesh_slice(self, i):
+        """(DOF slice, CSR-data slice) of mesh i in the batch vectors."""
+        return (slice(int(self.dof_offsets[i]), int(self.dof_offsets[i + 1])),
+                slice(int(self.nnz_offsets[i]), int(self.nnz_offsets[i + 1])))  # fmt: skip
+
+
+class BatchedPass:
+    """The element pass of one or two MeshBatch objects."""
+
+    def __init__(self, batches, persistent=True):
+        self.batches = list(batches)
+        self.lib = L.load()
+        self.persistent = persistent and len(self.batches) == 2
+        dev = self.batches[0].asm.device
+        self.counter = torch.zeros(1, dtype=torch.int64, device=dev)
+        self.status = torch.zeros(4, dtype=torch.int32, device=dev)
+        self.graph = None
+        if len(self.batches) == 2:
+            self._items = (L.EfeWorkItem * 2)(*[
+                L.EfeWorkItem(ctypes.addressof(b.asm.mesh), ctypes.addressof(b.asm._groups_c[0]), b.U.data_ptr(),
+                              b.dU.data_ptr(), b.K.data_ptr(), b.P.data_ptr(), b.F.data_ptr())
+                for b in self.batches
+            ])  # fmt: skip
+            prec = {torch.float32: L.EFE_K_FP32, torch.float64: L.EFE_K_FP64}[self.batches[0].K.dtype]
+            self._prec = prec
+
+    def _launch(self):
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        if self.persistent:
+            L.check(self.lib.efe_compute_elements_persistent(self._items, 2, self._prec,
+                                                             ctypes.c_void_p(self.counter.data_ptr()),
+                                                             ctypes.c_void_p(self.status.data_ptr()), stream),
+                    "efe_compute_elements_persistent")  # fmt: skip
+        else:
+            for b in self.batches:
+                a = b.asm
+                L.check(self.lib.efe_compute_elements(ctypes.byref(a.mesh), a._groups_c, len(a.groups),
+                                                      ctypes.c_void_p(b.U.data_ptr()), ctypes.c_void_p(b.dU.data_ptr()),
+                                                      None, 0.0, a.kPrecision, ctypes.c_void_p(b.K.data_ptr()),
+                                                      ctypes.c_void_p(b.P.data_ptr()), ctypes.c_void_p(b.F.data_ptr()),
+                                                      ctypes.c_void_p(self.status.data_ptr()), stream),
+                        "efe_compute_elements")  # fmt: skip
+
+    def step(self):
+        """One pass over every element of every batch: zero the accumulators, run the kernels."""
+        for b in self.batches:
+            b.P.zero_()
+            b.F.zero_()
+            b.K.zero_()
+        self.status.zero_()
+        self._launch()
+
+    def capture(self):
+        """Capture step() in a CUDA graph (warm-up on a side stream first, as torch requires)."""
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            self.step()
+        torch.cuda.current_stream().wait_stream(s)
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.step()
+        return self.graph
+
+    def replay(self):
+        self.graph.replay()
+
+    def check_status(self):
+        st = self.status.cpu().numpy()
+        if st[0] & L.EFE_STATUS_CUTBACK:
+            from .exceptions import CutbackRequest
+
+            raise CutbackRequest("material point failed in the batch", 0.5)
+        return st

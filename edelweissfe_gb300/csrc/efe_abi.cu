@@ -138,6 +138,47 @@ int32_t check_group(const EfeMesh* mesh, const EfeGroup& g) {
   return EFE_OK;
 }
 
+efe::GroupArgs make_args(const EfeMesh* mesh, const EfeGroup& gr, const double* U, const double* dU, void* Kdata,
+                         double* P, double* F, int32_t* status) {
+  efe::GroupArgs a;
+  a.nElements = gr.nElements;
+  a.elementOffset = gr.elementOffset;
+  a.conn = gr.conn;
+  a.pairSlot = gr.pairSlot;
+  a.props = gr.props;
+  a.thickness = gr.thickness;
+  a.geomG = gr.geomG;
+  a.geomG32 = gr.geomG32;
+  a.geomGlo = gr.geomGlo;
+  a.geomS = gr.geomS;
+  a.stateRef = gr.stateRef;
+  a.stateTemp = gr.stateTemp;
+  a.auxRef = gr.auxRef;
+  a.auxTemp = gr.auxTemp;
+  a.nProps = gr.nProps;
+  a.material = gr.material;
+  a.plane = gr.plane;
+  a.tileVariant = gr.tileVariant;
+  a.nodeDof = mesh->nodeDof;
+  a.nodeRowLen = mesh->nodeRowLen;
+  a.U = U;
+  a.dU = dU;
+  a.Kdata = Kdata;
+  a.P = P;
+  a.F = F;
+  a.status = status;
+  return a;
+}
+
+int32_t check_item_buffers(const EfeGroup& gr, const double* U, const double* dU) {
+  const bool tl = gr.kinematics == EFE_TOTAL_LAGRANGIAN;
+  if (!gr.conn || !gr.pairSlot || !gr.props || !gr.geomG || !gr.geomS || !gr.stateRef || !gr.stateTemp)
+    return fail(EFE_ERR_ARGUMENT, "null group buffer");
+  if (tl && (!U || !gr.auxTemp)) return fail(EFE_ERR_ARGUMENT, "total-Lagrangian group needs U and auxTemp");
+  if (!tl && !dU) return fail(EFE_ERR_ARGUMENT, "small-strain group needs dU");
+  return EFE_OK;
+}
+
 template <typename F>
 void parallel_for(int64_t n, F&& f) {
   unsigned nt = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
@@ -261,32 +302,7 @@ int32_t efe_compute_elements(const EfeMesh* mesh, const EfeGroup* groups, int32_
     if (!tl && !dU) return fail(EFE_ERR_ARGUMENT, "small-strain group needs dU");
     if (kPrecision == EFE_K_FP32_FF && form_of(gr) == efe::SS3 && (!gr.geomG32 || !gr.geomGlo))
       return fail(EFE_ERR_ARGUMENT, "EFE_K_FP32_FF needs geomG32 and geomGlo");
-    efe::GroupArgs a;
-    a.nElements = gr.nElements;
-    a.elementOffset = gr.elementOffset;
-    a.conn = gr.conn;
-    a.pairSlot = gr.pairSlot;
-    a.props = gr.props;
-    a.thickness = gr.thickness;
-    a.geomG = gr.geomG;
-    a.geomG32 = gr.geomG32;
-    a.geomGlo = gr.geomGlo;
-    a.geomS = gr.geomS;
-    a.stateRef = gr.stateRef;
-    a.stateTemp = gr.stateTemp;
-    a.auxRef = gr.auxRef;
-    a.auxTemp = gr.auxTemp;
-    a.nProps = gr.nProps;
-    a.material = gr.material;
-    a.plane = gr.plane;
-    a.nodeDof = mesh->nodeDof;
-    a.nodeRowLen = mesh->nodeRowLen;
-    a.U = U;
-    a.dU = dU;
-    a.Kdata = Kdata;
-    a.P = P;
-    a.F = F;
-    a.status = status;
+    const efe::GroupArgs a = make_args(mesh, gr, U, dU, Kdata, P, F, status);
     const int form = form_of(gr);
     cudaError_t e = cudaErrorInvalidValue;
     switch (gr.shape) {
@@ -340,6 +356,31 @@ int32_t efe_adjoint_tl(const EfeMesh* mesh, const EfeGroup* g, const double* U, 
     case EFE_HEXA20: e = efe::adjoint_tl_hexa20(g->rule, a, st); break;
   }
   if (e != cudaSuccess) return cuda_fail(e, "efe_adjoint_tl");
+  return EFE_OK;
+}
+
+int32_t efe_compute_elements_persistent(const EfeWorkItem* items, int32_t nItems, int32_t kPrecision,
+                                        uint64_t* workCounter, int32_t* status, void* stream) {
+  if (!items || nItems != 2 || !workCounter || !status) return fail(EFE_ERR_ARGUMENT, "two work items expected");
+  if (kPrecision != EFE_K_FP64 && kPrecision != EFE_K_FP32) return fail(EFE_ERR_ARGUMENT, "unknown K precision");
+  efe::GroupArgs args[2];
+  int forms[2];
+  for (int i = 0; i < 2; ++i) {
+    const EfeWorkItem& it = items[i];
+    if (!it.mesh || !it.group || !it.Kdata || !it.P || !it.F) return fail(EFE_ERR_ARGUMENT, "null work item buffer");
+    int32_t rc = check_group(it.mesh, *it.group);
+    if (rc) return rc;
+    rc = check_item_buffers(*it.group, it.U, it.dU);
+    if (rc) return rc;
+    args[i] = make_args(it.mesh, *it.group, it.U, it.dU, it.Kdata, it.P, it.F, status);
+    forms[i] = form_of(*it.group);
+  }
+  cudaError_t e = efe::persistent_pair(items[0].group->shape, items[0].group->rule, forms[0], items[1].group->shape,
+                                       items[1].group->rule, forms[1], kPrecision, args[0], args[1],
+                                       (unsigned long long*)workCounter, (cudaStream_t)stream);
+  if (e == cudaErrorNotSupported)
+    return fail(EFE_ERR_UNSUPPORTED, "no persistent kernel for this pair of element types");
+  if (e != cudaSuccess) return cuda_fail(e, "efe_compute_elements_persistent");
   return EFE_OK;
 }
 

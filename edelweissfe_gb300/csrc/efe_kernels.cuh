@@ -33,7 +33,7 @@ struct GroupArgs {
   double* stateTemp;
   const double* auxRef;
   double* auxTemp;
-  int32_t nProps, material, plane;
+  int32_t nProps, material, plane, tileVariant;
   // mesh
   const int32_t* nodeDof;
   const int32_t* nodeRowLen;
@@ -175,11 +175,12 @@ __device__ __forceinline__ void kadd(KT* p, KT v) {
 
 // FF: the strain increment and the residual of the small-strain 3D form are formed in float-float
 // arithmetic from the float-float geometry (geomG32 + geomGlo); the return map stays FP64.
-template <int SHAPE, int RULE, int FORM, typename KT, int EPB, int NT, int MINB, bool FF = false>
-__global__ void __launch_bounds__(NT, MINB) assemble_kernel(GroupArgs g) {
+// One tile: the EPB elements starting at e0, processed by the NT threads of the calling CTA
+// (every thread of the CTA must call it: it synchronises the CTA).
+template <int SHAPE, int RULE, int FORM, typename KT, int EPB, int NT, bool FF>
+__device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t e0, unsigned char* smem) {
   using L = Layout<SHAPE, RULE, FORM, KT, EPB>;
   constexpr int DIM = L::DIM, NN = L::NN, NQ = L::NQ, NVEC = L::NVEC, NSCAL = L::NSCAL, NDOF = L::NDOF;
-  extern __shared__ __align__(16) unsigned char smem[];
   double* su = reinterpret_cast<double*>(smem + L::u_off);
   double* sr = reinterpret_cast<double*>(smem + L::r_off);
   KT* ssc = reinterpret_cast<KT*>(smem + L::sc_off);
@@ -187,7 +188,6 @@ __global__ void __launch_bounds__(NT, MINB) assemble_kernel(GroupArgs g) {
   int* srl = reinterpret_cast<int*>(smem + L::rl_off);
   VMConst* smc = reinterpret_cast<VMConst*>(smem + L::mc_off);
 
-  const int64_t e0 = (int64_t)blockIdx.x * EPB;
   const int64_t nEl = g.nElements;
   const bool tl = (FORM == TLH || FORM == TLV3 || FORM == TLV2);
   const double* Ux = tl ? g.U : g.dU;
@@ -711,6 +711,35 @@ __global__ void __launch_bounds__(NT, MINB) assemble_kernel(GroupArgs g) {
 #pragma unroll
         for (int k = 0; k < DIM; ++k) kadd(K + slot2 + (int64_t)j * rl2 + k, acc[j][k]);
     }
+  }
+}
+
+template <int SHAPE, int RULE, int FORM, typename KT, int EPB, int NT, int MINB, bool FF = false>
+__global__ void __launch_bounds__(NT, MINB) assemble_kernel(GroupArgs g) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  assemble_tile<SHAPE, RULE, FORM, KT, EPB, NT, FF>(g, (int64_t)blockIdx.x * EPB, smem);
+}
+
+// Persistent form: a grid sized to the resident CTAs pulls tiles of two element types from one
+// work counter (scratch, zeroed before the launch), heavier type first, until both are done.
+template <int SA, int RA, int FA, int EA, int SB, int RB, int FB, int EB, typename KT, int NT>
+__global__ void __launch_bounds__(NT, 1)
+    assemble_persistent_kernel(GroupArgs ga, GroupArgs gb, int64_t tilesA, int64_t tilesB,
+                               unsigned long long* counter) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ long long tile;
+  while (true) {
+    if (threadIdx.x == 0) tile = (long long)atomicAdd(counter, 1ULL);
+    __syncthreads();
+    const long long t = tile;
+    __syncthreads();
+    if (t < tilesA)
+      assemble_tile<SA, RA, FA, KT, EA, NT, false>(ga, (int64_t)t * EA, smem);
+    else if (t < tilesA + tilesB)
+      assemble_tile<SB, RB, FB, KT, EB, NT, false>(gb, (int64_t)(t - tilesA) * EB, smem);
+    else
+      break;
+    __syncthreads();
   }
 }
 

@@ -4,24 +4,28 @@
 
 namespace efe {
 
-// Elements per CTA: about 128 material points per CTA (one per thread in phase A), limited to
-// 72 KB of shared memory so that three CTAs can share an SM.
-template <int SHAPE, int RULE, int FORM, typename KT>
+// Tile shapes of the element pass.  Variant 0: about 128 material points per CTA (one per
+// thread in phase A), 128 threads, at most 72 KB of shared memory so that three CTAs share an SM.
+// Variant 1: about 256 points and 256 threads per CTA, up to 110 KB (one or two CTAs per SM).
+// The autotuner (edelweissfe_gb300/autotune.py) picks one per group by timing both.
+template <int SHAPE, int RULE, int FORM, typename KT, int VARIANT = 0>
 struct Tile {
   static constexpr int NQ = RuleInfo<RULE>::NQ;
   static constexpr size_t per_element = Layout<SHAPE, RULE, FORM, KT, 1>::bytes;
-  static constexpr int fit = (int)((72 * 1024) / per_element);
-  static constexpr int want = (128 + NQ - 1) / NQ;
+  static constexpr size_t budget = VARIANT == 0 ? 72 * 1024 : 110 * 1024;
+  static constexpr int points = VARIANT == 0 ? 128 : 256;
+  static constexpr int fit = (int)(budget / per_element);
+  static constexpr int want = (points + NQ - 1) / NQ;
   static constexpr int e0 = fit < want ? fit : want;
   static constexpr int EPB = e0 < 1 ? 1 : (e0 > 32 ? 32 : e0);
-  static constexpr int NT = 128;
+  static constexpr int NT = VARIANT == 0 ? 128 : 256;
   static constexpr size_t bytes = Layout<SHAPE, RULE, FORM, KT, EPB>::bytes;
-  static constexpr int MINB = bytes <= 72 * 1024 ? 3 : 1;
+  static constexpr int MINB = VARIANT == 0 ? (bytes <= 72 * 1024 ? 3 : 1) : 1;
 };
 
-template <int SHAPE, int RULE, int FORM, typename KT, bool FF = false>
-cudaError_t launch_assemble(const GroupArgs& g, cudaStream_t st) {
-  using T = Tile<SHAPE, RULE, FORM, KT>;
+template <int SHAPE, int RULE, int FORM, typename KT, bool FF, int VARIANT>
+cudaError_t launch_assemble_variant(const GroupArgs& g, cudaStream_t st) {
+  using T = Tile<SHAPE, RULE, FORM, KT, VARIANT>;
   static_assert(T::bytes <= 200 * 1024, "tile does not fit in shared memory");
   auto kern = assemble_kernel<SHAPE, RULE, FORM, KT, T::EPB, T::NT, T::MINB, FF>;
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::bytes);
@@ -30,6 +34,12 @@ cudaError_t launch_assemble(const GroupArgs& g, cudaStream_t st) {
   if (grid == 0) return cudaSuccess;
   kern<<<(unsigned)grid, T::NT, T::bytes, st>>>(g);
   return cudaGetLastError();
+}
+
+template <int SHAPE, int RULE, int FORM, typename KT, bool FF = false>
+cudaError_t launch_assemble(const GroupArgs& g, cudaStream_t st) {
+  if (g.tileVariant == 1) return launch_assemble_variant<SHAPE, RULE, FORM, KT, FF, 1>(g, st);
+  return launch_assemble_variant<SHAPE, RULE, FORM, KT, FF, 0>(g, st);
 }
 
 template <int SHAPE, int RULE>
@@ -113,6 +123,8 @@ EFE_BODY_DECL(quad8)
 EFE_BODY_DECL(hexa8)
 EFE_BODY_DECL(hexa20)
 #undef EFE_BODY_DECL
+cudaError_t persistent_pair(int shapeA, int ruleA, int formA, int shapeB, int ruleB, int formB, int kprec,
+                            const GroupArgs& a, const GroupArgs& b, unsigned long long* counter, cudaStream_t st);
 cudaError_t adjoint_tl_quad4(int rule, const AdjointArgs& a, cudaStream_t st);
 cudaError_t adjoint_tl_quad8(int rule, const AdjointArgs& a, cudaStream_t st);
 cudaError_t adjoint_tl_hexa8(int rule, const AdjointArgs& a, cudaStream_t st);

@@ -127,7 +127,20 @@ typedef struct EfeGroup {
                                 [6][nElements*nInt] as (11,22,33,12,23,13); may be NULL for
                                 hyperelastic materials                                        */
   double* auxTemp;           /* TL only: Green-Lagrange strain of this call                  */
+  int32_t tileVariant;       /* CTA shape of the element pass: 0 = 128 threads, 3 CTAs/SM;
+                                1 = 256 threads, larger tiles (chosen by the autotuner)       */
 } EfeGroup;
+
+/* One (mesh, group) pair of a persistent launch, with its own DOF vectors and CSR data. */
+typedef struct EfeWorkItem {
+  const EfeMesh* mesh;
+  const EfeGroup* group;
+  const double* U;
+  const double* dU;
+  void* Kdata;
+  double* P;
+  double* F;
+} EfeWorkItem;
 
 int32_t efe_abi_version(void);
 const char* efe_last_error(void);
@@ -171,6 +184,15 @@ int32_t efe_body_force(const EfeMesh* mesh, const EfeGroup* group, const int32_t
    EFE_MAT_NEOHOOKE_* only. */
 int32_t efe_adjoint_tl(const EfeMesh* mesh, const EfeGroup* group, const double* U, const double* lambda, double* gX,
                        double* gParams, void* stream);
+
+/* The element pass of two groups, possibly of different meshes and dimensions (e.g. a batch of
+   2D meshes and a batch of 3D meshes), in ONE persistent launch: the resident CTAs take tiles of
+   both groups from the work counter until both are done (same results as efe_compute_elements on
+   each item).  workCounter: one device uint64 of scratch, zeroed by this call.  Implemented for
+   the pair (Hexa20 3x3x3, Quad8 2x2) total-Lagrangian Neo-Hooke in either order and precision
+   EFE_K_FP64 / EFE_K_FP32; other pairs return EFE_ERR_UNSUPPORTED. */
+int32_t efe_compute_elements_persistent(const EfeWorkItem* items, int32_t nItems, int32_t kPrecision,
+                                        uint64_t* workCounter, int32_t* status, void* stream);
 
 /* acceptLastState: stateTemp -> stateRef and auxTemp -> auxRef for every group. */
 int32_t efe_accept_state(const EfeGroup* groups, int32_t nGroups, void* stream);
