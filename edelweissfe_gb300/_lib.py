@@ -32,6 +32,7 @@ EXPORTS = [
     "efe_setup_geometry",
     "efe_compute_elements",
     "efe_compute_elements_persistent",
+    "efe_compute_elements_persistent_noalloc",
     "efe_accept_state",
     "efe_body_force",
     "efe_adjoint_tl",
@@ -146,6 +147,8 @@ def load(build_if_missing=False):
     lib.efe_adjoint_tl.argtypes = [ctypes.POINTER(EfeMesh), ctypes.POINTER(EfeGroup), P, P, P, P, P]
     lib.efe_compute_elements_persistent.restype = i32
     lib.efe_compute_elements_persistent.argtypes = [ctypes.POINTER(EfeWorkItem), i32, i32, P, P, P]
+    lib.efe_compute_elements_persistent_noalloc.restype = i32
+    lib.efe_compute_elements_persistent_noalloc.argtypes = [ctypes.POINTER(EfeWorkItem), i32, i32, P, P]
     lib.efe_accept_state.restype = i32
     lib.efe_accept_state.argtypes = [ctypes.POINTER(EfeGroup), i32, P]
     lib.efe_pattern_count.restype = i64

@@ -384,6 +384,40 @@ int32_t efe_compute_elements_persistent(const EfeWorkItem* items, int32_t nItems
   return EFE_OK;
 }
 
+// Same validation and kernels as efe_compute_elements_persistent; the work counter comes from the
+// library's static scratch array (efe_batch.cu), so nothing here allocates device memory.
+int32_t efe_compute_elements_persistent_noalloc(const EfeWorkItem* items, int32_t nItems, int32_t kPrecision,
+                                                int32_t* status, void* stream) {
+  if (!items || nItems != 2 || !status) return fail(EFE_ERR_ARGUMENT, "two work items expected");
+  if (kPrecision != EFE_K_FP64 && kPrecision != EFE_K_FP32) return fail(EFE_ERR_ARGUMENT, "unknown K precision");
+  efe::GroupArgs args[2];
+  int forms[2];
+  for (int i = 0; i < 2; ++i) {
+    const EfeWorkItem& it = items[i];
+    if (!it.mesh || !it.group || !it.Kdata || !it.P || !it.F) return fail(EFE_ERR_ARGUMENT, "null work item buffer");
+    int32_t rc = check_group(it.mesh, *it.group);
+    if (rc) return rc;
+    rc = check_item_buffers(*it.group, it.U, it.dU);
+    if (rc) return rc;
+    args[i] = make_args(it.mesh, *it.group, it.U, it.dU, it.Kdata, it.P, it.F, status);
+    forms[i] = form_of(*it.group);
+  }
+  int64_t needed = 0;
+  cudaError_t e = efe::persistent_pair_noalloc(items[0].group->shape, items[0].group->rule, forms[0],
+                                               items[1].group->shape, items[1].group->rule, forms[1], kPrecision,
+                                               args[0], args[1], &needed, (cudaStream_t)stream);
+  if (e == cudaErrorNotSupported)
+    return fail(EFE_ERR_UNSUPPORTED, "no persistent kernel for this pair of element types");
+  if (needed > EFE_NOALLOC_MAX_TILES) {
+    return fail(EFE_ERR_ARGUMENT, "efe_compute_elements_persistent_noalloc: the batch needs " + std::to_string(needed) +
+                                      " tile indices, the 32-bit work counter in the static scratch allows at most " +
+                                      std::to_string((long long)EFE_NOALLOC_MAX_TILES) +
+                                      "; split the batch or use efe_compute_elements_persistent");
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "efe_compute_elements_persistent_noalloc");
+  return EFE_OK;
+}
+
 int32_t efe_accept_state(const EfeGroup* groups, int32_t nGroups, void* stream) {
   if (!groups || nGroups < 0) return fail(EFE_ERR_ARGUMENT, "null argument");
   cudaStream_t st = (cudaStream_t)stream;

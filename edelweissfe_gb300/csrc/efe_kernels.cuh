@@ -722,14 +722,14 @@ __global__ void __launch_bounds__(NT, MINB) assemble_kernel(GroupArgs g) {
 
 // Persistent form: a grid sized to the resident CTAs pulls tiles of two element types from one
 // work counter (scratch, zeroed before the launch), heavier type first, until both are done.
-template <int SA, int RA, int FA, int EA, int SB, int RB, int FB, int EB, typename KT, int NT>
+template <int SA, int RA, int FA, int EA, int SB, int RB, int FB, int EB, typename KT, int NT,
+          typename CT = unsigned long long>
 __global__ void __launch_bounds__(NT, 1)
-    assemble_persistent_kernel(GroupArgs ga, GroupArgs gb, int64_t tilesA, int64_t tilesB,
-                               unsigned long long* counter) {
+    assemble_persistent_kernel(GroupArgs ga, GroupArgs gb, int64_t tilesA, int64_t tilesB, CT* counter) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ long long tile;
   while (true) {
-    if (threadIdx.x == 0) tile = (long long)atomicAdd(counter, 1ULL);
+    if (threadIdx.x == 0) tile = (long long)atomicAdd(counter, (CT)1);
     __syncthreads();
     const long long t = tile;
     __syncthreads();

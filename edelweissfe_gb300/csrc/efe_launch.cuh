@@ -125,6 +125,10 @@ EFE_BODY_DECL(hexa20)
 #undef EFE_BODY_DECL
 cudaError_t persistent_pair(int shapeA, int ruleA, int formA, int shapeB, int ruleB, int formB, int kprec,
                             const GroupArgs& a, const GroupArgs& b, unsigned long long* counter, cudaStream_t st);
+// same pass with the work counter in the library's static scratch array; *needed = tile indices
+// the counter runs through (written before the range check)
+cudaError_t persistent_pair_noalloc(int shapeA, int ruleA, int formA, int shapeB, int ruleB, int formB, int kprec,
+                                    const GroupArgs& a, const GroupArgs& b, int64_t* needed, cudaStream_t st);
 cudaError_t adjoint_tl_quad4(int rule, const AdjointArgs& a, cudaStream_t st);
 cudaError_t adjoint_tl_quad8(int rule, const AdjointArgs& a, cudaStream_t st);
 cudaError_t adjoint_tl_hexa8(int rule, const AdjointArgs& a, cudaStream_t st);

@@ -194,6 +194,28 @@ int32_t efe_adjoint_tl(const EfeMesh* mesh, const EfeGroup* group, const double*
 int32_t efe_compute_elements_persistent(const EfeWorkItem* items, int32_t nItems, int32_t kPrecision,
                                         uint64_t* workCounter, int32_t* status, void* stream);
 
+/* Allocation-free form of efe_compute_elements_persistent.  No counterpart in the reference: it
+   exists for callers that must not allocate device memory -- a host program whose device memory
+   belongs to another runtime's pool or arena (a solver framework, a game or simulation engine
+   that hands this library pre-sized buffers), or one that cannot afford a cudaMalloc's implicit
+   device synchronisation in its time step.  The caller passes the same inputs and outputs
+   (work items, status); the work counter lives in a static device array of the library
+   (EFE_NOALLOC_SCRATCH_BYTES per GPU that loads the library, held until the process exits)
+   instead of a caller-provided buffer.  The call makes no cudaMalloc/cudaFree and calls no
+   allocating library routine.
+   - The first call on a device looks up the array's device address on that device (with it
+     current); make that first call before any stream capture on the device.
+   - The counter is zeroed by every call, on `stream`, before its launch; status is NOT zeroed
+     (the caller zeroes it, as for the other passes).
+   - All calls on one device share the array: calls whose launches may overlap on the GPU (other
+     streams, other host threads) race on the counter and give wrong results; serialise them.
+   - Limit: the counter is 32-bit; a batch whose tile indices (element tiles of both groups plus
+     one per resident CTA) exceed EFE_NOALLOC_MAX_TILES is rejected with EFE_ERR_ARGUMENT. */
+#define EFE_NOALLOC_SCRATCH_BYTES 256
+#define EFE_NOALLOC_MAX_TILES 2147483647LL
+int32_t efe_compute_elements_persistent_noalloc(const EfeWorkItem* items, int32_t nItems, int32_t kPrecision,
+                                                int32_t* status, void* stream);
+
 /* acceptLastState: stateTemp -> stateRef and auxTemp -> auxRef for every group. */
 int32_t efe_accept_state(const EfeGroup* groups, int32_t nGroups, void* stream);
 
