@@ -411,6 +411,187 @@ def run_batched(args):
     }, default=str))  # fmt: skip
 
 
+# ------------------------------------------------------------------ Newton iteration counts (64^3 J2)
+def run_newton(args):
+    """The 64^3 von Mises cube under uniaxial displacement: bottom u_y = 0, left u_x = 0, back u_z = 0,
+    top u_y -> 0.005 in 20 increments (maxIncrement 0.05, no extrapolation), Newton to a flux
+    residual of 1e-10 x the average flux (no absolute floor) with the device PCG, in FP64 and in
+    mixed precision.  Reports the iterations per increment of both and the difference of the
+    final displacement fields."""
+    import torch
+
+    from edelweissfe_gb300 import ElementGroup, GPUAssembler
+    from edelweissfe_gb300.solver import AdaptiveTimeStepper, Dirichlet, NISTGPU
+
+    coords, conn, nodeDof, nDof, _, _ = workload(args.n)
+    x, y, z = coords[:, 0], coords[:, 1], coords[:, 2]
+    dirichlets = [Dirichlet(nodeDof[y < 1e-9] + 1, 0.0), Dirichlet(nodeDof[x < 1e-9] + 0, 0.0),
+                  Dirichlet(nodeDof[z < 1e-9] + 2, 0.0), Dirichlet(nodeDof[y > 1 - 1e-9] + 1, 0.005)]  # fmt: skip
+    out = {}
+    for precision in ("fp64", "mixed"):
+        asm = GPUAssembler(coords, nodeDof, nDof, [ElementGroup("C3D8", "vonmises", VM, conn)], precision=precision)
+        solver = NISTGPU(asm, linsolver="pcg", extrapolation="off", maxIter=15, fluxResidualTolerance=1e-10,
+                         fieldCorrectionTolerance=1e-10, fluxResidualFloor=0.0, pcgTolerance=1e-13)  # fmt: skip
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        U = solver.solveStep(AdaptiveTimeStepper(maxIncrement=0.05, startIncrement=0.05), dirichlets)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t
+        its = [h["iterations"] for h in solver.history]
+        out[precision] = dict(U=U.cpu().numpy(), iterations=its, wall_s=wall, pcg_iterations=sum(solver.linearIterations),
+                              final_flux=[h["residuals"][-1][0] / h["residuals"][-1][1] for h in solver.history
+                                          if h["iterations"] is not None][-1],
+                              plastic_fraction=float((asm.group_state(0, "ref")[..., 12] > 0).mean()))  # fmt: skip
+        del asm, solver
+        torch.cuda.empty_cache()
+    f, m = out["fp64"], out["mixed"]
+    extra = [b - a for a, b in zip(f["iterations"], m["iterations"]) if a is not None and b is not None]
+    print(json.dumps({
+        "metric": "Newton iterations per increment to 1e-10, FP64 vs mixed (FP32 tangent) element pass",
+        "value": max(extra) if extra else None, "unit": "max extra iterations per increment (mixed - fp64)",
+        "higher_is_better": False, "data": "synthetic",
+        "config": {"workload": f"C3D8 von Mises J2 {args.n}^3 unit cube (jitter 5%), 20 uniaxial increments to "
+                               "0.5% strain, device Jacobi-PCG (rel. tol 1e-13)", "dofs": nDof, "elements": len(conn)},
+        "fp64": {k: v for k, v in f.items() if k != "U"},
+        "mixed": {k: v for k, v in m.items() if k != "U"},
+        "U_rel_diff_mixed_vs_fp64": float(np.abs(m["U"] - f["U"]).max() / np.abs(f["U"]).max()),
+        "gpu_launches": None,
+    }))
+
+
+# ------------------------------------------------------------------ adjoint gradients (32^3 Neo-Hooke)
+def adjoint_setup(n=32, seed=4):
+    """boxGen C3D8TL n^3 unit cube, per-element E log-normal (median 1000, sigma 0.3, seed 4),
+    nu = 0.3 (Neo-Hooke (a): mu = E/2.6, K = E/1.2); bottom fixed, top u_y = -0.01 in 5 increments;
+    1000 sensor nodes off the bottom face (seed 5); targets = the solution for E x (1 + 0.1 N(0,1))
+    (seed 6)."""
+    from edelweissfe_gb300 import meshes
+
+    coords, conn, nodeDof, nDof = meshes.box(n, n, n, nNodes=8)
+    E = 1000.0 * np.exp(0.3 * np.random.default_rng(seed).normal(size=len(conn)))
+    y = coords[:, 1]
+    bottom = np.nonzero(y < 1e-9)[0]
+    top = np.nonzero(y > 1 - 1e-9)[0]
+    bdofs = (nodeDof[bottom][:, None] + np.arange(3)).ravel()
+    tdofs = nodeDof[top] + 1
+    cand = np.nonzero(y > 1e-9)[0]
+    sensors = np.random.default_rng(seed + 1).choice(cand, min(1000, len(cand)), replace=False)
+    sdofs = (nodeDof[sensors][:, None] + np.arange(3)).ravel()
+    Epert = E * (1 + 0.1 * np.random.default_rng(seed + 2).normal(size=len(conn)))
+    return coords, conn, nodeDof, nDof, E, Epert, bdofs, tdofs, sdofs
+
+
+def run_adjoint(args):
+    """dJ/dE (per element) and dJ/dX (nodal coordinates) of J = 1/2 sum_sensors |u - u*|^2 through
+    TLEquilibrium (torch.autograd), timed as gradient evaluations per second: one gradient = the
+    tangent at the solution + the adjoint kernel (lambda^T dP/dp); the adjoint linear solve is timed
+    separately.  Checked against central differences (h = 1e-6) of J through full Newton solves on
+    --fd-directions random directions in (E, X)."""
+    import torch
+
+    from edelweissfe_gb300 import ElementGroup, GPUAssembler
+    from edelweissfe_gb300.adjoint import TLAdjoint, TLEquilibrium, TLProblem, young_to_lame
+    from edelweissfe_gb300.solver import AdaptiveTimeStepper, Dirichlet
+
+    n = args.n if args.n != N_CUBE else 32
+    coords, conn, nodeDof, nDof, E0, Epert, bdofs, tdofs, sdofs = adjoint_setup(n)
+    dev = torch.device("cuda", 0)
+    asm = GPUAssembler(coords, nodeDof, nDof, [ElementGroup("C3D8TL", "neohookewa",
+                       young_to_lame(torch.tensor(E0), 0.3).numpy(), conn)], precision="fp64")  # fmt: skip
+    problem = TLProblem(asm, [Dirichlet(bdofs, 0.0), Dirichlet(tdofs, -0.01)],
+                        lambda: AdaptiveTimeStepper(maxIncrement=0.2, startIncrement=0.2), linsolver="pcg",
+                        extrapolation="linear", maxIter=25, fluxResidualTolerance=1e-12,
+                        fieldCorrectionTolerance=1e-13, fluxResidualFloor=0.0, pcgTolerance=1e-14)  # fmt: skip
+    X = torch.tensor(coords, device=dev)
+    sd = torch.as_tensor(sdofs, device=dev)
+    with torch.no_grad():
+        target = TLEquilibrium.apply(young_to_lame(torch.tensor(Epert, device=dev), 0.3), X, problem)[sd].clone()
+
+    def J(E, Xc):
+        U = TLEquilibrium.apply(young_to_lame(E, 0.3), Xc, problem)
+        return 0.5 * ((U[sd] - target) ** 2).sum()
+
+    E = torch.tensor(E0, device=dev, requires_grad=True)
+    Xg = X.clone().requires_grad_(True)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    J0 = J(E, Xg)
+    torch.cuda.synchronize()
+    forward_s = time.perf_counter() - t
+    newton = [h["iterations"] for h in problem.solver.history]
+    t = time.perf_counter()
+    J0.backward()
+    torch.cuda.synchronize()
+    backward_s = time.perf_counter() - t
+    gE, gX = E.grad.clone(), Xg.grad.clone()
+
+    # timed gradient evaluations at the solution (tangent + adjoint kernel), solve timed apart
+    with torch.no_grad():
+        U = problem.solve(young_to_lame(E.detach(), 0.3), X)
+        dJdU = torch.zeros(nDof, dtype=torch.float64, device=dev)
+        dJdU[sd] = U[sd] - target
+        adj = TLAdjoint(problem.solver)
+        K = problem.solver.tangentAt(U)
+        t = time.perf_counter()
+        lam = adj.solve_adjoint(U, dJdU, problem.dirichletDofs, K)
+        torch.cuda.synchronize()
+        solve_ms = (time.perf_counter() - t) * 1e3
+        pcg_its = adj.lastLinearIterations
+
+        def grad_eval(ev=None):
+            Kt = problem.solver.tangentAt(U) if ev is None else None
+            if ev is not None:
+                ev[0].record()
+                Kt = problem.solver.tangentAt(U)
+                ev[1].record()
+            gXk, gPk = asm.adjointTL(U, lam)
+            if ev is not None:
+                ev[2].record()
+            return Kt, gXk, gPk
+
+        for _ in range(args.warmup):
+            grad_eval()
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for k in range(args.steps):
+            grad_eval(evs[k])
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / args.steps
+        tangent_ms = sum(e[0].elapsed_time(e[1]) for e in evs) / args.steps
+        adjoint_ms = sum(e[1].elapsed_time(e[2]) for e in evs) / args.steps
+
+    # central differences on random joint directions (E, X)
+    rng = np.random.default_rng(7)
+    errs = []
+    with torch.no_grad():
+        for _ in range(args.fd_directions):
+            dE = torch.as_tensor(rng.normal(0, 1, len(conn)) * E0, device=dev)
+            dX = torch.as_tensor(rng.normal(0, 1, coords.shape) / n, device=dev)
+            h = 1e-6
+            fd = (float(J(E.detach() + h * dE, X + h * dX)) - float(J(E.detach() - h * dE, X - h * dX))) / (2 * h)
+            ad = float((gE * dE).sum() + (gX * dX).sum())
+            errs.append(abs(ad - fd) / abs(fd))
+    nEl = len(conn)
+    print(json.dumps({
+        "metric": "adjoint grads/s (dJ/dE per element + dJ/dX), excluding the adjoint linear solve",
+        "value": 1e3 / ms, "unit": "grad/s", "ms_per_step": ms, "steps": args.steps, "warmup": args.warmup,
+        "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"C3D8TL Neo-Hooke (a) {n}^3 unit cube, lognormal E (median 1000, sigma 0.3), "
+                               "1000 sensor nodes, bottom fixed, top -0.01 in 5 increments",
+                   "elements": nEl, "dofs": nDof, "nnz": int(asm.nnz)},
+        "tangent_ms": tangent_ms, "adjoint_kernel_ms": adjoint_ms,
+        "adjoint_kernel_elem_per_s": nEl / (adjoint_ms * 1e-3),
+        "adjoint_solve_ms": solve_ms, "adjoint_pcg_iterations": pcg_its,
+        "forward_newton_s": forward_s, "forward_newton_iterations": newton, "autograd_backward_s": backward_s,
+        "fd_check": {"directions": args.fd_directions, "h": 1e-6, "max_rel_err": max(errs) if errs else None,
+                     "median_rel_err": float(np.median(errs)) if errs else None},
+        "gpu_launches": 2 * args.steps,
+    }))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -419,8 +600,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_CUBE, help="elements per cube edge")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="cube", choices=["cube", "batched"],
-                    help="cube: the 64^3 von Mises headline; batched: the uneven-mesh batch")
+    ap.add_argument("--workload", default="cube", choices=["cube", "batched", "newton", "adjoint"],
+                    help="cube: the 64^3 von Mises headline; batched: the uneven-mesh batch; newton: Newton "
+                         "iterations FP64 vs mixed on the 64^3 cube; adjoint: 32^3 Neo-Hooke gradients")
+    ap.add_argument("--fd-directions", type=int, default=3)
     ap.add_argument("--batch-meshes", type=int, default=512)
     ap.add_argument("--batch-scale", type=float, default=1.0)
     ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64", "mixed-ff"],
@@ -432,9 +615,9 @@ def main():
         if rank == 0:
             run_reference(args)
         return
-    if args.workload == "batched":
+    if args.workload in ("batched", "newton", "adjoint"):
         if rank == 0:
-            run_batched(args)
+            {"batched": run_batched, "newton": run_newton, "adjoint": run_adjoint}[args.workload](args)
         return
     if world > 1:
         import torch

@@ -9,6 +9,10 @@ R_f(U, p) = P_f(U, p) + PExt_f vanishes, and dR_f/dU_f = -K_ff, so for any param
 The adjoint system is solved with the same device CG as the Newton steps (K is symmetric for
 hyperelastic materials); lambda^T dP/dp is the hand-written reverse-mode kernel `efe_adjoint_tl`.
 The hyperelastic state does not depend on the load path, so no history is needed.
+
+`TLEquilibrium` puts the solve and its adjoint behind torch.autograd: U = TLEquilibrium.apply(
+params, coords, problem) is differentiable in params ([E, 2] = (mu, K) per element) and coords
+([nNodes, dim]), so any torch objective of U back-propagates through the Newton solution.
 """
 
 import torch
@@ -19,6 +23,11 @@ def young_to_lame_chain(gP, nu):
     return gP[:, 0] / (2.0 * (1.0 + nu)) + gP[:, 1] / (3.0 * (1.0 - 2.0 * nu))
 
 
+def young_to_lame(E, nu):
+    """(mu, K) per element from Young's modulus E (a torch tensor; differentiable)."""
+    return torch.stack([E / (2.0 * (1.0 + nu)), E / (3.0 * (1.0 - 2.0 * nu))], 1)
+
+
 class TLAdjoint:
     """solver: NISTGPU around an FP64 GPUAssembler whose groups are total-Lagrangian Neo-Hooke."""
 
@@ -27,19 +36,67 @@ class TLAdjoint:
         self.asm = solver.asm
         self.lastLinearIterations = None
 
-    def gradient(self, U, dJdU, dirichletDofs):
-        """(dJ/dX [nNodes, dim], [dJ/d(mu, K) per group [E, 2]]) at the equilibrium U."""
+    def solve_adjoint(self, U, dJdU, dirichletDofs, K=None):
+        """lambda with K_ff lambda_f = dJ/dU_f and lambda = 0 on the prescribed DOFs."""
         asm = self.asm
-        U = U.to(asm.device, torch.float64)
         g = dJdU.to(asm.device, torch.float64).clone()
         dir_idx = None
         if dirichletDofs is not None and len(dirichletDofs):
             dir_idx = torch.as_tensor(dirichletDofs, dtype=torch.int64, device=asm.device)
             g[dir_idx] = 0.0
-        K = self.solver.tangentAt(U)
+        if K is None:
+            K = self.solver.tangentAt(U.to(asm.device, torch.float64))
         n0 = len(self.solver.linearIterations)
         lam = self.solver._solve_pcg(K, g, dir_idx)
         self.lastLinearIterations = self.solver.linearIterations[n0:]
         if dir_idx is not None:
             lam[dir_idx] = 0.0
-        return asm.adjointTL(U, lam)
+        return lam
+
+    def gradient(self, U, dJdU, dirichletDofs):
+        """(dJ/dX [nNodes, dim], [dJ/d(mu, K) per group [E, 2]]) at the equilibrium U."""
+        U = U.to(self.asm.device, torch.float64)
+        lam = self.solve_adjoint(U, dJdU, dirichletDofs)
+        return self.asm.adjointTL(U, lam)
+
+
+class TLProblem:
+    """A quasi-static total-Lagrangian Neo-Hooke problem on one GPUAssembler (one group) with fixed
+    Dirichlet conditions: solve(params, coords) resets the model, sets the per-element (mu, K) and
+    the nodal coordinates, and runs the Newton step (NISTGPU.solveStep) to the final load."""
+
+    def __init__(self, asm, dirichlets, stepper_factory, **solver_options):
+        import numpy as np
+
+        from .solver import NISTGPU
+
+        self.asm = asm
+        self.dirichlets = list(dirichlets)
+        self.stepper_factory = stepper_factory
+        self.solver = NISTGPU(asm, **solver_options)
+        self.dirichletDofs = np.unique(np.concatenate([d.dofs for d in self.dirichlets])) if self.dirichlets else None
+
+    def solve(self, params, coords):
+        self.asm.setProperties(0, params.detach())
+        self.asm.setCoordinates(coords.detach())
+        self.asm.resetState()
+        self.solver.history = []
+        return self.solver.solveStep(self.stepper_factory(), self.dirichlets)
+
+
+class TLEquilibrium(torch.autograd.Function):
+    """U(params, coords) at equilibrium; backward: one adjoint solve + efe_adjoint_tl."""
+
+    @staticmethod
+    def forward(ctx, params, coords, problem):
+        U = problem.solve(params, coords)
+        ctx.problem = problem
+        ctx.save_for_backward(U)
+        return U.clone()
+
+    @staticmethod
+    def backward(ctx, gU):
+        (U,) = ctx.saved_tensors
+        problem = ctx.problem
+        gX, gP = TLAdjoint(problem.solver).gradient(U, gU, problem.dirichletDofs)
+        return gP[0], gX, None

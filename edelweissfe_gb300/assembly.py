@@ -180,6 +180,29 @@ class GPUAssembler:
         if st[0] & L.EFE_STATUS_BAD_JACOBIAN:
             raise ValueError(f"element {0x7FFFFFFF - int(st[1])} has a non-positive Jacobian determinant")
 
+    # ------------------------------------------------------------------ parameters
+    def setCoordinates(self, coords):
+        """Move the nodes (same topology and DOF numbering) and recompute the element geometry
+        (the reference re-runs setNodes + initializeElement, element.py:164-205)."""
+        c = torch.as_tensor(coords, dtype=torch.float64).to(self.device).reshape(self.nNodes, self.dim)
+        self.coords.copy_(c)
+        self._setup_geometry()
+
+    def setProperties(self, group, props):
+        """Replace the material properties of one group: [nProps] shared or [E, nProps] per element."""
+        d = self.groups[group]._dev["props"]
+        p = torch.as_tensor(props, dtype=torch.float64).to(self.device)
+        if p.dim() == 1:
+            p = p[: d.shape[1]].expand_as(d)
+        d.copy_(p[:, : d.shape[1]])
+
+    def resetState(self):
+        """Zero the quadrature-point history of every group (a fresh, undeformed model)."""
+        for g in self.groups:
+            for key in ("stateRef", "stateTemp", "auxRef", "auxTemp"):
+                if key in g._dev:
+                    g._dev[key].zero_()
+
     # ------------------------------------------------------------------ buffers
     def constructDofVector(self):
         """Zero DOF vector on the device (DofManager.constructDofVector, dofmanager.py)."""

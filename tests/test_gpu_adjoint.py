@@ -125,3 +125,43 @@ def test_objective_gradient_matches_finite_differences():
         dX = rng.normal(0, 1, coords.shape)
         fd = (J(Efield, coords + H * dX)[0] - J(Efield, coords - H * dX)[0]) / (2 * H)
         assert abs(float(np.sum(gX * dX)) - fd) <= RTOL * abs(fd), ("X", k, float(np.sum(gX * dX)), fd)
+
+
+def test_autograd_function_matches_finite_differences():
+    """TLEquilibrium behind torch.autograd: J(U(E, X)) backpropagates to E and X; checked against
+    central differences of the same objective along one random direction each."""
+    from edelweissfe_gb300 import ElementGroup, GPUAssembler, meshes
+    from edelweissfe_gb300.adjoint import TLEquilibrium, TLProblem, young_to_lame
+    from edelweissfe_gb300.solver import AdaptiveTimeStepper, Dirichlet
+
+    coords, conn, nodeDof, nDof = meshes.box(3, 2, 2, nNodes=8)
+    coords = meshes.jitter(coords, 0.1, [1 / 3, 0.5, 0.5], 21, [0, 0, 0], [1, 1, 1])
+    rng = np.random.default_rng(22)
+    E0 = 1000.0 * np.exp(0.3 * rng.normal(size=len(conn)))
+    asm = GPUAssembler(coords, nodeDof, nDof, [ElementGroup("C3D8TL", "neohookewa", young_to_lame(
+        torch.tensor(E0), 0.3).numpy(), conn)])  # fmt: skip
+    bdofs, tdofs = _boundary_dofs(coords, nodeDof)
+    problem = TLProblem(asm, [Dirichlet(bdofs, 0.0), Dirichlet(tdofs, -0.01)],
+                        lambda: AdaptiveTimeStepper(maxIncrement=0.25), linsolver="pcg", extrapolation="off",
+                        maxIter=25, fluxResidualTolerance=1e-12, fieldCorrectionTolerance=1e-13,
+                        fluxResidualFloor=0.0, pcgTolerance=1e-14)  # fmt: skip
+    sdofs = torch.as_tensor(rng.choice(np.setdiff1d(np.arange(nDof), np.concatenate([bdofs, tdofs])), 12,
+                                       replace=False), device=asm.device)  # fmt: skip
+    target = torch.as_tensor(rng.normal(0, 1e-3, 12), device=asm.device)
+
+    def J(E, X):
+        U = TLEquilibrium.apply(young_to_lame(E, 0.3), X, problem)
+        return 0.5 * ((U[sdofs] - target) ** 2).sum()
+
+    E = torch.tensor(E0, device=asm.device, requires_grad=True)
+    X = torch.tensor(coords, device=asm.device, requires_grad=True)
+    J(E, X).backward()
+    with torch.no_grad():
+        dE = torch.as_tensor(rng.normal(0, 1, len(conn)) * E0, device=asm.device)
+        fd = (float(J(E + H * dE, X)) - float(J(E - H * dE, X))) / (2 * H)
+        ad = float((E.grad * dE).sum())
+        assert abs(ad - fd) <= RTOL * abs(fd), ("E", ad, fd)
+        dX = torch.as_tensor(rng.normal(0, 1, coords.shape), device=asm.device)
+        fd = (float(J(E, X + H * dX)) - float(J(E, X - H * dX))) / (2 * H)
+        ad = float((X.grad * dX).sum())
+        assert abs(ad - fd) <= RTOL * abs(fd), ("X", ad, fd)
