@@ -36,6 +36,7 @@ EXPORTS = [
     "efe_accept_state",
     "efe_body_force",
     "efe_adjoint_tl",
+    "efe_adjoint_small_strain",
     "efe_pattern_count",
     "efe_pattern_fill",
 ]
@@ -145,6 +146,8 @@ def load(build_if_missing=False):
     lib.efe_body_force.argtypes = [ctypes.POINTER(EfeMesh), ctypes.POINTER(EfeGroup), P, i64, P, P, P]
     lib.efe_adjoint_tl.restype = i32
     lib.efe_adjoint_tl.argtypes = [ctypes.POINTER(EfeMesh), ctypes.POINTER(EfeGroup), P, P, P, P, P]
+    lib.efe_adjoint_small_strain.restype = i32
+    lib.efe_adjoint_small_strain.argtypes = [ctypes.POINTER(EfeMesh), ctypes.POINTER(EfeGroup), P, P, P, P, P, P, P, P]
     lib.efe_compute_elements_persistent.restype = i32
     lib.efe_compute_elements_persistent.argtypes = [ctypes.POINTER(EfeWorkItem), i32, i32, P, P, P]
     lib.efe_compute_elements_persistent_noalloc.restype = i32

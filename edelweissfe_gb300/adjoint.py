@@ -100,3 +100,100 @@ class TLEquilibrium(torch.autograd.Function):
         problem = ctx.problem
         gX, gP = TLAdjoint(problem.solver).gradient(U, gU, problem.dirichletDofs)
         return gP[0], gX, None
+
+
+class PathAdjoint:
+    """Gradients of a function of the final increment of a plastic (path-dependent) small-strain
+    solution with respect to the material properties of every element.
+
+    The reference has no derivatives; this is new.  Attach it to a NISTGPU before solveStep: every
+    accepted increment n checkpoints the quadrature-point history before it (s_{n-1}), its total
+    displacement u_n and its increment du_n (host-side checkpoint list, device tensors).  The
+    discrete adjoint then runs backward over the increments, recomputing each increment from its
+    checkpoint:
+
+      K_n          the consistent tangent of increment n (element pass from s_{n-1} with du_n),
+      a            = (ds_n/du_n)^T sbar_n + (dP_n/du_n)^T cP_n        (efe_adjoint_small_strain)
+      K_n lam_n    = a + ubar_n  on the free DOFs, lam_n = 0 on the prescribed ones
+      b            = (dP_n/du_n)^T lam_n;   ubar_{n-1} = -(a + b);   sbar_{n-1}, dJ/dprops from both
+                     passes,
+
+    for J = cP . P_N + cU . u_N (cP: weights of the final residual, e.g. -1 on the DOFs whose
+    reaction is wanted; cU: weights of the final displacement).  With an FP32 tangent the adjoint
+    systems are refined against the exact FP64 operator (K v = -(dP/du)^T v from the reverse
+    kernel), so the gradient is that of the FP64 path.
+
+    Checkpoints hold one state array per group and increment (13 doubles per point for von Mises),
+    i.e. history memory grows with the number of increments; nothing else is stored."""
+
+    def __init__(self, solver, refine_steps=2):
+        self.solver = solver
+        self.asm = solver.asm
+        self.refine_steps = refine_steps
+        self.checkpoints = []
+        solver.onAccept = self._record
+
+    def _record(self, ts, U_old, U_new, dU):
+        states = [g._dev["stateRef"].clone() for g in self.asm.groups]
+        self.checkpoints.append(dict(ts=ts, U=U_new.clone(), dU=dU.clone(), states=states))
+
+    def _exact_Kv(self, ck, v):
+        """K v with the FP64 consistent tangent of checkpointed increment ck, matrix-free."""
+        asm = self.asm
+        out = asm.constructDofVector()
+        for gi in range(len(asm.groups)):
+            asm.adjointSmallStrain(gi, ck["states"][gi], ck["dU"], out, Pbar=v)
+        return -out
+
+    def gradient(self, dirichletDofs, cP=None, cU=None):
+        """dJ/dprops per group ([E, nProps] tensors) for J = cP . P_N + cU . u_N."""
+        asm = self.asm
+        solver = self.solver
+        dev = asm.device
+        dir_idx = None
+        if dirichletDofs is not None and len(dirichletDofs):
+            dir_idx = torch.as_tensor(dirichletDofs, dtype=torch.int64, device=dev)
+        saved = [g._dev["stateRef"].clone() for g in asm.groups]
+        sbar = [torch.zeros_like(g._dev["stateRef"]) for g in asm.groups]
+        gP = [torch.zeros((len(g.conn), g._dev["props"].shape[1]), dtype=torch.float64, device=dev)
+              for g in asm.groups]  # fmt: skip
+        carry = asm.constructDofVector()
+        self.linearIterations = []
+        N = len(self.checkpoints)
+        for n in reversed(range(N)):
+            ck = self.checkpoints[n]
+            last = n == N - 1
+            # recompute increment n from its checkpoint: the tangent K_n
+            for gi, g in enumerate(asm.groups):
+                g._dev["stateRef"].copy_(ck["states"][gi])
+            K = solver.tangentAt_increment(ck["U"], ck["dU"])
+            a = asm.constructDofVector()
+            sprev = [torch.zeros_like(s) for s in sbar]
+            for gi in range(len(asm.groups)):
+                asm.adjointSmallStrain(gi, ck["states"][gi], ck["dU"], a, Pbar=cP if last else None,
+                                       stateBarIn=sbar[gi], stateBarOut=sprev[gi], gProps=gP[gi])  # fmt: skip
+            rhs = a + carry
+            if last and cU is not None:
+                rhs = rhs + cU
+            if dir_idx is not None:
+                rhs[dir_idx] = 0.0
+            n0 = len(solver.linearIterations)
+            lam = solver.linearSolve(K, rhs, dir_idx)
+            if K.dtype != torch.float64:
+                for _ in range(self.refine_steps):
+                    r = rhs - self._exact_Kv(ck, lam)
+                    if dir_idx is not None:
+                        r[dir_idx] = 0.0
+                    lam = lam + solver.linearSolve(K, r, dir_idx)
+            if dir_idx is not None:
+                lam[dir_idx] = 0.0
+            self.linearIterations.append(solver.linearIterations[n0:])
+            b = asm.constructDofVector()
+            for gi in range(len(asm.groups)):
+                asm.adjointSmallStrain(gi, ck["states"][gi], ck["dU"], b, Pbar=lam, stateBarOut=sprev[gi],
+                                       gProps=gP[gi])  # fmt: skip
+            carry = -(a + b)
+            sbar = sprev
+        for gi, g in enumerate(asm.groups):
+            g._dev["stateRef"].copy_(saved[gi])
+        return gP

@@ -359,6 +359,48 @@ int32_t efe_adjoint_tl(const EfeMesh* mesh, const EfeGroup* g, const double* U, 
   return EFE_OK;
 }
 
+int32_t efe_adjoint_small_strain(const EfeMesh* mesh, const EfeGroup* g, const double* stateBefore, const double* dU,
+                                 const double* Pbar, const double* stateBarIn, double* stateBarOut, double* dUbar,
+                                 double* gProps, void* stream) {
+  if (!mesh || !g || !stateBefore || !dU || !dUbar) return fail(EFE_ERR_ARGUMENT, "null argument");
+  int32_t rc = check_group(mesh, *g);
+  if (rc) return rc;
+  if (g->kinematics != EFE_SMALL_STRAIN)
+    return fail(EFE_ERR_UNSUPPORTED, "efe_adjoint_small_strain covers small-strain groups");
+  if (g->material != EFE_MAT_LINEAR_ELASTIC && g->material != EFE_MAT_VON_MISES)
+    return fail(EFE_ERR_UNSUPPORTED, "efe_adjoint_small_strain covers linear elastic and von Mises groups");
+  if (mesh->dim == 2 && g->plane != EFE_PLANE_STRAIN)
+    return fail(EFE_ERR_UNSUPPORTED, "efe_adjoint_small_strain covers solids and plane strain");
+  if (!mesh->nodeDof || !g->conn || !g->props || !g->geomG || !g->geomS)
+    return fail(EFE_ERR_ARGUMENT, "null group buffer (has efe_setup_geometry run?)");
+  efe::SSAdjointArgs a;
+  a.nEl = g->nElements;
+  a.nProps = g->nProps;
+  a.material = g->material;
+  a.conn = g->conn;
+  a.nodeDof = mesh->nodeDof;
+  a.props = g->props;
+  a.geomG = g->geomG;
+  a.geomS = g->geomS;
+  a.stateBefore = stateBefore;
+  a.dU = dU;
+  a.Pbar = Pbar;
+  a.barIn = stateBarIn;
+  a.barOut = stateBarOut;
+  a.dUbar = dUbar;
+  a.gProps = gProps;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaErrorInvalidValue;
+  switch (g->shape) {
+    case EFE_QUAD4: e = efe::adjoint_ss_quad4(g->rule, a, st); break;
+    case EFE_QUAD8: e = efe::adjoint_ss_quad8(g->rule, a, st); break;
+    case EFE_HEXA8: e = efe::adjoint_ss_hexa8(g->rule, a, st); break;
+    case EFE_HEXA20: e = efe::adjoint_ss_hexa20(g->rule, a, st); break;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "efe_adjoint_small_strain");
+  return EFE_OK;
+}
+
 int32_t efe_compute_elements_persistent(const EfeWorkItem* items, int32_t nItems, int32_t kPrecision,
                                         uint64_t* workCounter, int32_t* status, void* stream) {
   if (!items || nItems != 2 || !workCounter || !status) return fail(EFE_ERR_ARGUMENT, "two work items expected");

@@ -1,0 +1,270 @@
+// efe_adjoint_ss.cuh -- reverse mode of one small-strain element pass (linear elastic, von Mises).
+//
+// Forward, per quadrature point (displacementelement/element.py:318-346, vonmises.py:186-254):
+//   de = B dU_e,  (sig, kappa) = update(sig0, kappa0, de; props),  eps = eps0 + de,
+//   P_e -= s B^T sig   (s = det J w t).
+// Given adjoint seeds of the outputs -- sigBar, epsBar, kappaBar of the new state and PBar of the
+// element residual -- the kernel accumulates the adjoints of the inputs: dUBar (DOF vector),
+// sig0Bar, eps0Bar, kappa0Bar (state before the increment) and the material properties
+// (E, nu, fy0, H, dfy, delta).  The return map is differentiated through its converged scalar
+// equation R(dK) = q - sqrt(6) G dK - sqrt(2/3) fy(kappa0 + dK) = 0 (implicit function theorem),
+// so the derivatives are those of the exact return map, consistent with the reference's
+// consistent tangent (vonmises.py:241-251).
+//
+// Tile layout as the forward pass: EPB elements per CTA; phase 0 gathers dU_e and PBar_e, phase A
+// runs one thread per point, phase C reduces the per-point contributions per DOF (one atomic per
+// element DOF) and per property (plain stores: one thread owns an element's property).
+#pragma once
+#include "efe_launch.cuh"
+
+namespace efe {
+
+// Adjoint of the hypoelastic 3D update.  Accumulates into sig0Bar, k0Bar, deBar, pBar[6].
+__device__ inline void hypo3d_reverse(const VMConst& c, double E, double nu, bool vonMises, const double sig0[6],
+                                      double k0, const double de[6], const double sBar[6], double kBar,
+                                      double sig0Bar[6], double& k0Bar, double deBar[6], double pBar[6]) {
+  const Iso& Ei = c.Ei;
+  const double G = c.G;
+  double trBar[6];
+  for (int i = 0; i < 6; ++i) trBar[i] = sBar[i];
+  double Gbar = 0.0;
+  k0Bar += kBar;  // kappa = kappa0 (+ dK)
+  double nrm = 0.0;
+  for (int i = 0; i < 6; ++i) nrm += de[i] * de[i];
+  if (vonMises && !(nrm < 1e-28)) {
+    double tr[6], ds[6];
+    iso_apply(Ei, de, ds);
+    for (int i = 0; i < 6; ++i) tr[i] = sig0[i] + ds[i];
+    double dev[6];
+    const double mean = (tr[0] + tr[1] + tr[2]) * (1.0 / 3.0);
+    dev[0] = tr[0] - mean;
+    dev[1] = tr[1] - mean;
+    dev[2] = tr[2] - mean;
+    dev[3] = tr[3];
+    dev[4] = tr[4];
+    dev[5] = tr[5];
+    const double q = sqrt(dev[0] * dev[0] + dev[1] * dev[1] + dev[2] * dev[2] +
+                          2.0 * (dev[3] * dev[3] + dev[4] * dev[4] + dev[5] * dev[5]));
+    const double sq23 = sqrt(2.0 / 3.0), sq6 = sqrt(6.0);
+    const double fy_k0 = c.fy0 + c.H * k0 + vm_sat(c, k0);
+    if (q - sq23 * fy_k0 > 0.0) {
+      // the forward's scalar Newton, step for step, for the same converged dK
+      double dK = 0.0;
+      for (int counter = 0;; ++counter) {
+        const double k = k0 + dK;
+        const double R = q - sq6 * G * dK - sq23 * (c.fy0 + c.H * k + vm_sat(c, k));
+        if (!(fabs(R) > 1e-12) || counter == 15) break;
+        const double dR = -sq6 * G - sq23 * (c.H + vm_dsat(c, k));
+        dK -= R / dR;
+      }
+      const double k = k0 + dK;
+      const double g2 = 2.0 * G * (sqrt(1.5) * dK);  // sig = tr - g2 n, n = dev / q
+      double n[6], g2Bar = 0.0, nd = 0.0, devBar[6];
+      for (int i = 0; i < 6; ++i) {
+        n[i] = dev[i] / q;
+        g2Bar -= sBar[i] * n[i];
+      }
+      for (int i = 0; i < 6; ++i) {
+        const double nBar = -g2 * sBar[i];
+        devBar[i] = nBar / q;
+        nd += nBar * dev[i];
+      }
+      double qBar = -nd / (q * q);
+      const double dKBar = kBar + g2Bar * 2.0 * G * sqrt(1.5);
+      Gbar += g2Bar * 2.0 * sqrt(1.5) * dK;
+      // dK(q, kappa0, G, fy0, H, dfy, delta) from R = 0: x_bar += dK_bar * (dR/dx) / D
+      const double dfyk = c.H + vm_dsat(c, k);
+      const double w = dKBar / (sq6 * G + sq23 * dfyk);
+      qBar += w;
+      k0Bar += -sq23 * dfyk * w;
+      Gbar += -sq6 * dK * w;
+      pBar[2] += -sq23 * w;
+      pBar[3] += -sq23 * k * w;
+      if (c.dfy != 0.0) {
+        const double ek = exp(-c.delta * k);
+        pBar[4] += -sq23 * (1.0 - ek) * w;
+        pBar[5] += -sq23 * c.dfy * k * ek * w;
+      }
+      // q = |dev| with doubled shear terms, dev = deviatoric part of tr
+      for (int i = 0; i < 6; ++i) devBar[i] += qBar * (i < 3 ? 1.0 : 2.0) * dev[i] / q;
+      const double mb = (devBar[0] + devBar[1] + devBar[2]) * (1.0 / 3.0);
+      for (int i = 0; i < 6; ++i) trBar[i] += devBar[i] - (i < 3 ? mb : 0.0);
+    }
+  }
+  // trial stress tr = sig0 + Ei de (the elastic branch and the zero-increment shortcut included)
+  double dd[6];
+  iso_apply(Ei, trBar, dd);
+  for (int i = 0; i < 6; ++i) {
+    sig0Bar[i] += trBar[i];
+    deBar[i] += dd[i];
+  }
+  // properties through C11, C12, C44 and G
+  const double c11Bar = trBar[0] * de[0] + trBar[1] * de[1] + trBar[2] * de[2];
+  const double c12Bar = trBar[0] * (de[1] + de[2]) + trBar[1] * (de[0] + de[2]) + trBar[2] * (de[0] + de[1]);
+  const double c44Bar = trBar[3] * de[3] + trBar[4] * de[4] + trBar[5] * de[5];
+  const double den = (1.0 + nu) * (1.0 - 2.0 * nu);
+  const double f = E / den, df = E * (1.0 + 4.0 * nu) / (den * den);
+  pBar[0] += (c11Bar * Ei.c11 + c12Bar * Ei.c12 + c44Bar * Ei.c44 + Gbar * G) / E;
+  pBar[1] += c11Bar * (df * (1.0 - nu) - f) + c12Bar * (df * nu + f) + c44Bar * (df * (1.0 - 2.0 * nu) / 2.0 - f) -
+             Gbar * G / (1.0 + nu);
+}
+
+template <int SHAPE, int RULE>
+struct SSAdjointTile {
+  static constexpr int DIM = ShapeInfo<SHAPE>::DIM, NN = ShapeInfo<SHAPE>::NN, NQ = RuleInfo<RULE>::NQ;
+  static constexpr int NDOF = NN * DIM, NT = 128;
+  static constexpr size_t per_el = sizeof(double) * (2 * NDOF + NQ * NDOF + NQ * 6);
+  static constexpr int EPB0 = NT / NQ > 0 ? NT / NQ : 1;
+  static constexpr int EPB = (size_t)EPB0 * per_el <= 96 * 1024 ? EPB0 : (int)((96 * 1024) / per_el);
+  static_assert(EPB >= 1, "one element must fit in shared memory");
+  static constexpr size_t u_off = 0, p_off = u_off + sizeof(double) * EPB * NDOF,
+                          r_off = p_off + sizeof(double) * EPB * NDOF, g_off = r_off + sizeof(double) * EPB * NQ * NDOF,
+                          bytes = g_off + sizeof(double) * EPB * NQ * 6;
+};
+
+template <int SHAPE, int RULE>
+__global__ void __launch_bounds__(SSAdjointTile<SHAPE, RULE>::NT) adjoint_ss_kernel(SSAdjointArgs a) {
+  using T = SSAdjointTile<SHAPE, RULE>;
+  constexpr int DIM = T::DIM, NN = T::NN, NQ = T::NQ, NDOF = T::NDOF, EPB = T::EPB, NT = T::NT;
+  extern __shared__ __align__(16) unsigned char smem[];
+  double* su = reinterpret_cast<double*>(smem + T::u_off);
+  double* sp = reinterpret_cast<double*>(smem + T::p_off);
+  double* sr = reinterpret_cast<double*>(smem + T::r_off);
+  double* sg = reinterpret_cast<double*>(smem + T::g_off);
+  const int64_t e0 = (int64_t)blockIdx.x * EPB;
+  const int64_t nEl = a.nEl, stride = nEl * NQ;
+  const bool vm = a.material == EFE_MAT_VON_MISES;
+
+  // ---- phase 0: dU_e and PBar_e
+  for (int t = threadIdx.x; t < EPB * NN; t += NT) {
+    const int le = t / NN, n = t % NN;
+    const int64_t e = e0 + le;
+    if (e >= nEl) continue;
+    const int32_t dof = a.nodeDof[a.conn[e * NN + n]];
+    for (int c = 0; c < DIM; ++c) {
+      su[le * NDOF + n * DIM + c] = a.dU[dof + c];
+      sp[le * NDOF + n * DIM + c] = a.Pbar ? a.Pbar[dof + c] : 0.0;
+    }
+  }
+  __syncthreads();
+
+  // ---- phase A: one thread per point
+  for (int t = threadIdx.x; t < EPB * NQ; t += NT) {
+    const int le = t / NQ, q = t % NQ;
+    const int64_t e = e0 + le;
+    if (e >= nEl) continue;
+    const int64_t pt = e * NQ + q;
+    // G is read where it is used (twice) rather than held across the return map: fewer registers
+    const double* Gp = a.geomG + pt;
+    const double s = a.geomS[pt];
+    const double* u = su + le * NDOF;
+    const double* pb = sp + le * NDOF;
+    // B u and B PBar (small-strain Voigt 11,22,33,12,13,23, engineering shear)
+    double de[6] = {0, 0, 0, 0, 0, 0}, bp[6] = {0, 0, 0, 0, 0, 0};
+    for (int n = 0; n < NN; ++n) {
+      const double gx = Gp[(int64_t)n * stride], gy = Gp[(int64_t)(NN + n) * stride];
+      if constexpr (DIM == 3) {
+        const double gz = Gp[(int64_t)(2 * NN + n) * stride];
+        const double ux = u[n * 3], uy = u[n * 3 + 1], uz = u[n * 3 + 2];
+        const double px = pb[n * 3], py = pb[n * 3 + 1], pz = pb[n * 3 + 2];
+        de[0] = fma(gx, ux, de[0]);
+        de[1] = fma(gy, uy, de[1]);
+        de[2] = fma(gz, uz, de[2]);
+        de[3] = fma(gx, uy, fma(gy, ux, de[3]));
+        de[4] = fma(gx, uz, fma(gz, ux, de[4]));
+        de[5] = fma(gy, uz, fma(gz, uy, de[5]));
+        bp[0] += gx * px;
+        bp[1] += gy * py;
+        bp[2] += gz * pz;
+        bp[3] += gy * px + gx * py;
+        bp[4] += gz * px + gx * pz;
+        bp[5] += gz * py + gy * pz;
+      } else {
+        const double ux = u[n * 2], uy = u[n * 2 + 1];
+        const double px = pb[n * 2], py = pb[n * 2 + 1];
+        de[0] += gx * ux;
+        de[1] += gy * uy;
+        de[3] += gy * ux + gx * uy;
+        bp[0] += gx * px;
+        bp[1] += gy * py;
+        bp[3] += gy * px + gx * py;
+      }
+    }
+    // seeds: the new state's adjoint, plus P_e = -sum_q s B^T sig  =>  sigBar -= s B PBar
+    double sBar[6], eBar[6], kBar = 0.0;
+    for (int f = 0; f < 6; ++f) {
+      sBar[f] = (a.barIn ? a.barIn[(int64_t)f * stride + pt] : 0.0) - s * bp[f];
+      eBar[f] = a.barIn ? a.barIn[(int64_t)(6 + f) * stride + pt] : 0.0;
+    }
+    if (vm && a.barIn) kBar = a.barIn[(int64_t)12 * stride + pt];
+    double sig0[6], k0 = 0.0;
+    for (int f = 0; f < 6; ++f) sig0[f] = a.stateBefore[(int64_t)f * stride + pt];
+    if (vm) k0 = a.stateBefore[(int64_t)12 * stride + pt];
+    const double* props = a.props + e * a.nProps;
+    const VMConst mc = vm_const(props, vm);
+    double sig0Bar[6] = {0, 0, 0, 0, 0, 0}, k0Bar = 0.0, pBar[6] = {0, 0, 0, 0, 0, 0};
+    double deBar[6];
+    for (int f = 0; f < 6; ++f) deBar[f] = eBar[f];  // eps = eps0 + de
+    hypo3d_reverse(mc, props[0], props[1], vm, sig0, k0, de, sBar, kBar, sig0Bar, k0Bar, deBar, pBar);
+    if (a.barOut) {
+      for (int f = 0; f < 6; ++f) {
+        a.barOut[(int64_t)f * stride + pt] += sig0Bar[f];
+        a.barOut[(int64_t)(6 + f) * stride + pt] += eBar[f];
+      }
+      if (vm) a.barOut[(int64_t)12 * stride + pt] += k0Bar;
+    }
+    double* gq = sg + (le * NQ + q) * 6;
+    for (int k = 0; k < 6; ++k) gq[k] = pBar[k];
+    // dU_e contribution B^T deBar
+    double* rq = sr + (le * NQ + q) * NDOF;
+    for (int n = 0; n < NN; ++n) {
+      const double gx = Gp[(int64_t)n * stride], gy = Gp[(int64_t)(NN + n) * stride];
+      if constexpr (DIM == 3) {
+        const double gz = Gp[(int64_t)(2 * NN + n) * stride];
+        rq[n * 3 + 0] = deBar[0] * gx + deBar[3] * gy + deBar[4] * gz;
+        rq[n * 3 + 1] = deBar[3] * gx + deBar[1] * gy + deBar[5] * gz;
+        rq[n * 3 + 2] = deBar[4] * gx + deBar[5] * gy + deBar[2] * gz;
+      } else {
+        rq[n * 2 + 0] = deBar[0] * gx + deBar[3] * gy;
+        rq[n * 2 + 1] = deBar[3] * gx + deBar[1] * gy;
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- phase C: per element DOF and per element property
+  for (int t = threadIdx.x; t < EPB * NDOF; t += NT) {
+    const int le = t / NDOF, k = t % NDOF;
+    const int64_t e = e0 + le;
+    if (e >= nEl) continue;
+    double v = 0.0;
+    for (int q = 0; q < NQ; ++q) v += sr[(le * NQ + q) * NDOF + k];
+    const int32_t dof = a.nodeDof[a.conn[e * NN + k / DIM]] + k % DIM;
+    atomicAdd(a.dUbar + dof, v);
+  }
+  if (a.gProps) {
+    const int np = a.nProps < 6 ? a.nProps : 6;
+    for (int t = threadIdx.x; t < EPB * np; t += NT) {
+      const int le = t / np, k = t % np;
+      const int64_t e = e0 + le;
+      if (e >= nEl) continue;
+      double v = 0.0;
+      for (int q = 0; q < NQ; ++q) v += sg[(le * NQ + q) * 6 + k];
+      a.gProps[e * a.nProps + k] += v;
+    }
+  }
+}
+
+template <int SHAPE, int RULE>
+cudaError_t launch_adjoint_ss(const SSAdjointArgs& a, cudaStream_t st) {
+  using T = SSAdjointTile<SHAPE, RULE>;
+  if (a.nEl == 0) return cudaSuccess;
+  auto kern = adjoint_ss_kernel<SHAPE, RULE>;
+  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::bytes);
+  if (err != cudaSuccess) return err;
+  const int64_t blocks = (a.nEl + T::EPB - 1) / T::EPB;
+  kern<<<(unsigned)blocks, T::NT, T::bytes, st>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace efe

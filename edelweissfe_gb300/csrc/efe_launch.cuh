@@ -83,6 +83,27 @@ struct AdjointArgs {
 template <int SHAPE, int RULE>
 cudaError_t launch_adjoint_tl(const AdjointArgs& a, cudaStream_t st);
 
+// reverse mode of one small-strain element pass (efe_adjoint_ss.cuh)
+struct SSAdjointArgs {
+  int64_t nEl;
+  int32_t nProps, material;
+  const int32_t* conn;
+  const int32_t* nodeDof;
+  const double* props;
+  const double* geomG;
+  const double* geomS;
+  const double* stateBefore;  // [S][nPts]
+  const double* dU;           // [nDof]
+  const double* Pbar;         // [nDof] or null
+  const double* barIn;        // [S][nPts] or null
+  double* barOut;             // [S][nPts] or null (accumulated)
+  double* dUbar;              // [nDof] (accumulated)
+  double* gProps;             // [nEl][nProps] or null (accumulated)
+};
+
+template <int SHAPE, int RULE>
+cudaError_t launch_adjoint_ss(const SSAdjointArgs& a, cudaStream_t st);
+
 // form selector: small strain 3D/2D, total Lagrangian hyperelastic, total Lagrangian hypoelastic 3D/2D
 template <int SHAPE, int RULE, typename KT, bool FF = false>
 cudaError_t launch_form(int form, const GroupArgs& g, cudaStream_t st) {
@@ -129,6 +150,10 @@ cudaError_t persistent_pair(int shapeA, int ruleA, int formA, int shapeB, int ru
 // the counter runs through (written before the range check)
 cudaError_t persistent_pair_noalloc(int shapeA, int ruleA, int formA, int shapeB, int ruleB, int formB, int kprec,
                                     const GroupArgs& a, const GroupArgs& b, int64_t* needed, cudaStream_t st);
+cudaError_t adjoint_ss_quad4(int rule, const SSAdjointArgs& a, cudaStream_t st);
+cudaError_t adjoint_ss_quad8(int rule, const SSAdjointArgs& a, cudaStream_t st);
+cudaError_t adjoint_ss_hexa8(int rule, const SSAdjointArgs& a, cudaStream_t st);
+cudaError_t adjoint_ss_hexa20(int rule, const SSAdjointArgs& a, cudaStream_t st);
 cudaError_t adjoint_tl_quad4(int rule, const AdjointArgs& a, cudaStream_t st);
 cudaError_t adjoint_tl_quad8(int rule, const AdjointArgs& a, cudaStream_t st);
 cudaError_t adjoint_tl_hexa8(int rule, const AdjointArgs& a, cudaStream_t st);

@@ -1,5 +1,6 @@
 // efe_quad4.cu -- kernel instantiations for the quad4 element shape (one translation unit per shape).
 #include "efe_adjoint.cuh"
+#include "efe_adjoint_ss.cuh"
 
 namespace efe {
 
@@ -38,6 +39,15 @@ cudaError_t adjoint_tl_quad4(int rule, const AdjointArgs& a, cudaStream_t st) {
     case EFE_RULE_2D_1: return launch_adjoint_tl<EFE_QUAD4, EFE_RULE_2D_1>(a, st);
     case EFE_RULE_2D_2X2: return launch_adjoint_tl<EFE_QUAD4, EFE_RULE_2D_2X2>(a, st);
     case EFE_RULE_2D_3X3: return launch_adjoint_tl<EFE_QUAD4, EFE_RULE_2D_3X3>(a, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t adjoint_ss_quad4(int rule, const SSAdjointArgs& a, cudaStream_t st) {
+  switch (rule) {
+    case EFE_RULE_2D_1: return launch_adjoint_ss<EFE_QUAD4, EFE_RULE_2D_1>(a, st);
+    case EFE_RULE_2D_2X2: return launch_adjoint_ss<EFE_QUAD4, EFE_RULE_2D_2X2>(a, st);
+    case EFE_RULE_2D_3X3: return launch_adjoint_ss<EFE_QUAD4, EFE_RULE_2D_3X3>(a, st);
   }
   return cudaErrorInvalidValue;
 }

@@ -1,5 +1,6 @@
 // efe_quad8.cu -- kernel instantiations for the quad8 element shape (one translation unit per shape).
 #include "efe_adjoint.cuh"
+#include "efe_adjoint_ss.cuh"
 
 namespace efe {
 
@@ -34,6 +35,14 @@ cudaError_t adjoint_tl_quad8(int rule, const AdjointArgs& a, cudaStream_t st) {
   switch (rule) {
     case EFE_RULE_2D_2X2: return launch_adjoint_tl<EFE_QUAD8, EFE_RULE_2D_2X2>(a, st);
     case EFE_RULE_2D_3X3: return launch_adjoint_tl<EFE_QUAD8, EFE_RULE_2D_3X3>(a, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t adjoint_ss_quad8(int rule, const SSAdjointArgs& a, cudaStream_t st) {
+  switch (rule) {
+    case EFE_RULE_2D_2X2: return launch_adjoint_ss<EFE_QUAD8, EFE_RULE_2D_2X2>(a, st);
+    case EFE_RULE_2D_3X3: return launch_adjoint_ss<EFE_QUAD8, EFE_RULE_2D_3X3>(a, st);
   }
   return cudaErrorInvalidValue;
 }

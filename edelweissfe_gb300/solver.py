@@ -168,6 +168,9 @@ class NISTGPU:
         self._diag_pos = torch.from_numpy(np.nonzero(ix == rows)[0]).to(dev)
         self.history = []  # one record per attempted increment
         self.linearIterations = []
+        # called as onAccept(timeStep, U_old, U_new, dU) before each accepted increment's state is
+        # committed (the state of the assembler is still the one before the increment)
+        self.onAccept = None
 
     # ------------------------------------------------------------------ step
     def solveStep(self, stepper, dirichlets=(), nodeforces=(), bodyforces=(), cutbackFactor=0.25, U=None):
@@ -191,6 +194,9 @@ class NISTGPU:
                     prev = ts
                     if iters >= self.criticalIter:
                         stepper.preventIncrementIncrease()
+                    self.lastP = P
+                    if self.onAccept is not None:
+                        self.onAccept(ts, U, U_new, dU)
                     U = U_new
                     asm.acceptLastState()  # FEModel.advanceToTime (models/femodel.py:245-258)
                     self.history.append(dict(timeStep=ts, iterations=iters, error="", residuals=res))
@@ -272,6 +278,16 @@ class NISTGPU:
         P, F, K = asm.constructDofVector(), asm.constructDofVector(), asm.constructSystemMatrix()
         asm.status.zero_()
         asm.launch(U, torch.zeros_like(U), P, K, F)
+        asm.check_status()
+        return K
+
+    def tangentAt_increment(self, U, dU):
+        """The tangent K (CSR data) of the increment dU from the assembler's current stateRef
+        (the state is not committed)."""
+        asm = self.asm
+        P, F, K = asm.constructDofVector(), asm.constructDofVector(), asm.constructSystemMatrix()
+        asm.status.zero_()
+        asm.launch(U, dU, P, K, F)
         asm.check_status()
         return K
 

@@ -185,6 +185,23 @@ int32_t efe_body_force(const EfeMesh* mesh, const EfeGroup* group, const int32_t
 int32_t efe_adjoint_tl(const EfeMesh* mesh, const EfeGroup* group, const double* U, const double* lambda, double* gX,
                        double* gParams, void* stream);
 
+/* Reverse mode of one small-strain element pass (no reference counterpart: the reference has no
+   derivatives; this differentiates displacementelement/element.py:318-346 with
+   linearelastic.py:185-210 and vonmises.py:186-254, the return map through its converged scalar
+   equation).  For an increment with state stateBefore ([S][nElements*nInt], the layout of
+   stateRef) and DOF increment dU, let the pass produce the new state s (stress, strain, kappa) and
+   the residual P.  Given seeds stateBarIn (adjoint of s, same layout; NULL = 0) and Pbar (adjoint
+   of P, DOF vector; NULL = 0), it accumulates
+     dUbar       += (ds/d dU)^T stateBarIn + (dP/d dU)^T Pbar                 (DOF vector),
+     stateBarOut += (ds/d stateBefore)^T stateBarIn + (dP/d stateBefore)^T Pbar (may be NULL),
+     gProps      += the same for the material properties, [nElements][nProps] (may be NULL;
+                    E, nu for linear elasticity; E, nu, fy0, HLin, dfy, delta for von Mises).
+   With stateBarIn = NULL and Pbar = v, dUbar gets -K v (K the consistent tangent).  Solids and
+   plane strain; needs efe_setup_geometry (geomG, geomS). */
+int32_t efe_adjoint_small_strain(const EfeMesh* mesh, const EfeGroup* group, const double* stateBefore,
+                                 const double* dU, const double* Pbar, const double* stateBarIn, double* stateBarOut,
+                                 double* dUbar, double* gProps, void* stream);
+
 /* The element pass of two groups, possibly of different meshes and dimensions (e.g. a batch of
    2D meshes and a batch of 3D meshes), in ONE persistent launch: the resident CTAs take tiles of
    both groups from the work counter until both are done (same results as efe_compute_elements on

@@ -1,0 +1,156 @@
+"""Reverse mode of the small-strain element pass (efe_adjoint_small_strain) and the path adjoint
+over plastic load increments (PathAdjoint), in FP64, against central differences.
+
+1. One increment: L = sum(sbar * s_new) + pbar . P of one element pass from a plastic state s0
+   with increment dU (von Mises with saturation hardening, and linear elasticity); directional
+   derivatives of L in dU, in the state s0 and in the six material properties, h = 1e-7 relative;
+   agreement to 1e-6 relative.
+2. The plastic path: C3D20 (3x3x3 Gauss) von Mises cube, 2x2x2 elements with per-element yield
+   stress U[200, 300] and hardening U[800, 1200]; bottom u_y = 0, left u_x = 0, back u_z = 0, top
+   u_y -> 0.5 % in 4 increments; J = the total top reaction.  dJ/d(fy0, H) by the path adjoint vs
+   central differences of J through full Newton solves (h = 1e-6 relative), and the mixed
+   (FP32-tangent, device PCG with refinement) adjoint vs the FP64 one.
+"""
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _model(elType, material, seed):
+    from edelweissfe_gb300 import ElementGroup, GPUAssembler, meshes
+
+    rng = np.random.default_rng(seed)
+    if elType.startswith("C3D"):
+        nn = 20 if "20" in elType else 8
+        coords, conn, nodeDof, nDof = meshes.box(2, 2, 1, nNodes=nn)
+        coords = meshes.jitter(coords, 0.1, [0.5, 0.5, 1.0], seed, [0, 0, 0], [1, 1, 1])
+    else:
+        coords, conn, nodeDof, nDof = meshes.rect(3, 2, nNodes=8 if "8" in elType else 4)
+        coords = meshes.jitter(coords, 0.1, [1 / 3, 0.5], seed, [0, 0], [1, 1])
+    E = len(conn)
+    if material == "vonmises":
+        props = np.stack([rng.uniform(190e3, 230e3, E), rng.uniform(0.25, 0.35, E), rng.uniform(200, 300, E),
+                          rng.uniform(800, 1200, E), rng.uniform(20, 80, E), rng.uniform(5, 20, E)], 1)  # fmt: skip
+    else:
+        props = np.stack([rng.uniform(190e3, 230e3, E), rng.uniform(0.25, 0.35, E)], 1)
+    asm = GPUAssembler(coords, nodeDof, nDof, [ElementGroup(elType, material, props, conn, 1.0)])
+    return asm, coords, nodeDof, nDof, props
+
+
+def _uniaxial(coords, nodeDof, nDof, strain):
+    dim = coords.shape[1]
+    U = np.zeros(nDof)
+    U[nodeDof + 1] = strain * coords[:, 1]
+    U[nodeDof + 0] = -0.3 * strain * coords[:, 0]
+    if dim == 3:
+        U[nodeDof + 2] = -0.3 * strain * coords[:, 2]
+    return U
+
+
+@pytest.mark.parametrize("elType,material", [("C3D8", "vonmises"), ("C3D20", "vonmises"), ("C3D20R", "vonmises"),
+                                             ("CPE8", "vonmises"), ("CPE4", "vonmises"), ("C3D8", "linearelastic")])
+def test_increment_reverse_matches_finite_differences(elType, material):
+    asm, coords, nodeDof, nDof, props = _model(elType, material, 5)
+    dev = asm.device
+    rng = np.random.default_rng(6)
+    g = asm.groups[0]._dev
+    dU1 = torch.tensor(_uniaxial(coords, nodeDof, nDof, 0.003) + rng.normal(0, 1e-4, nDof), device=dev)
+    P, F, K = asm.constructDofVector(), asm.constructDofVector(), asm.constructSystemMatrix()
+    asm.computeElements(None, dU1, dU1, P, K, F)
+    asm.acceptLastState()
+    s0 = g["stateRef"].clone()
+    if material == "vonmises":
+        assert float((s0[12] > 0).double().mean()) > 0.5  # a plastic state
+    dU = torch.tensor(_uniaxial(coords, nodeDof, nDof, 0.001) + rng.normal(0, 2e-4, nDof), device=dev)
+    sbar = torch.tensor(rng.normal(0, 1, tuple(s0.shape)), device=dev)
+    pbar = torch.tensor(rng.normal(0, 1, nDof), device=dev)
+    props_t = g["props"].clone()
+
+    def L(dUx, s0x, px):
+        g["stateRef"].copy_(s0x)
+        asm.setProperties(0, px)
+        P, F, K = asm.constructDofVector(), asm.constructDofVector(), asm.constructSystemMatrix()
+        asm.computeElements(None, dUx, dUx, P, K, F)
+        return float((sbar * g["stateTemp"]).sum() + (pbar * P).sum())
+
+    L0 = L(dU, s0, props_t)
+    dUbar = asm.constructDofVector()
+    s0bar = torch.zeros_like(s0)
+    gp = torch.zeros_like(props_t)
+    asm.adjointSmallStrain(0, s0, dU, dUbar, Pbar=pbar, stateBarIn=sbar, stateBarOut=s0bar, gProps=gp)
+    h = 1e-7
+    for what in ("dU", "state", "props"):
+        for k in range(2):
+            if what == "dU":
+                d = torch.tensor(rng.normal(0, 1, nDof), device=dev) * 1e-3
+                fd = (L(dU + h * d, s0, props_t) - L(dU - h * d, s0, props_t)) / (2 * h)
+                ad = float((dUbar * d).sum())
+            elif what == "state":
+                d = torch.tensor(rng.normal(0, 1, tuple(s0.shape)), device=dev) * s0.abs().amax(1, keepdim=True)
+                fd = (L(dU, s0 + h * d, props_t) - L(dU, s0 - h * d, props_t)) / (2 * h)
+                ad = float((s0bar * d).sum())
+            else:
+                d = torch.tensor(rng.normal(0, 1, tuple(props_t.shape)), device=dev) * props_t
+                fd = (L(dU, s0, props_t + h * d) - L(dU, s0, props_t - h * d)) / (2 * h)
+                ad = float((gp * d).sum())
+            assert abs(ad - fd) <= 1e-6 * max(abs(fd), 1e-3 * abs(L0)), (what, k, ad, fd)
+
+
+def _path_problem(fy0, H, precision="fp64", linsolver="superlu"):
+    from edelweissfe_gb300 import ElementGroup, GPUAssembler, meshes
+    from edelweissfe_gb300.adjoint import PathAdjoint
+    from edelweissfe_gb300.solver import AdaptiveTimeStepper, Dirichlet, NISTGPU
+
+    coords, conn, nodeDof, nDof = meshes.box(2, 2, 2, nNodes=20)
+    E = len(conn)
+    props = np.stack([np.full(E, 210e3), np.full(E, 0.3), fy0, H, np.zeros(E), np.zeros(E)], 1)
+    asm = GPUAssembler(coords, nodeDof, nDof, [ElementGroup("C3D20", "vonmises", props, conn)], precision=precision)
+    x, y, z = coords[:, 0], coords[:, 1], coords[:, 2]
+    top = nodeDof[y > 1 - 1e-9] + 1
+    dirichlets = [Dirichlet(nodeDof[y < 1e-9] + 1, 0.0), Dirichlet(nodeDof[x < 1e-9], 0.0),
+                  Dirichlet(nodeDof[z < 1e-9] + 2, 0.0), Dirichlet(top, 0.005)]  # fmt: skip
+    solver = NISTGPU(asm, linsolver=linsolver, extrapolation="off", maxIter=25, fluxResidualTolerance=1e-12,
+                     fieldCorrectionTolerance=1e-14, fluxResidualFloor=0.0, pcgTolerance=1e-14)  # fmt: skip
+    adj = PathAdjoint(solver)
+    solver.solveStep(AdaptiveTimeStepper(maxIncrement=0.25, startIncrement=0.25), dirichlets)
+    J = -float(solver.lastP[torch.as_tensor(top, device=asm.device)].sum())
+    ddofs = np.unique(np.concatenate([d.dofs for d in dirichlets]))
+    return J, adj, ddofs, top, asm
+
+
+def _path_gradient(adj, ddofs, top, asm):
+    cP = asm.constructDofVector()
+    cP[torch.as_tensor(top, device=asm.device)] = -1.0
+    return adj.gradient(ddofs, cP=cP)[0].cpu().numpy()
+
+
+def test_path_adjoint_matches_finite_differences():
+    rng = np.random.default_rng(8)
+    fy0 = rng.uniform(200, 300, 8)
+    H = rng.uniform(800, 1200, 8)
+    J0, adj, ddofs, top, asm = _path_problem(fy0, H)
+    assert len(adj.checkpoints) >= 5
+    assert float((asm.groups[0]._dev["stateRef"][12] > 0).double().mean()) > 0.5
+    g = _path_gradient(adj, ddofs, top, asm)
+    h = 1e-6
+    for k in range(3):
+        dfy, dH = rng.normal(0, 1, 8) * fy0, rng.normal(0, 1, 8) * H
+        fd = (_path_problem(fy0 + h * dfy, H + h * dH)[0] - _path_problem(fy0 - h * dfy, H - h * dH)[0]) / (2 * h)
+        ad = float(np.sum(g[:, 2] * dfy) + np.sum(g[:, 3] * dH))
+        assert abs(ad - fd) <= 1e-6 * abs(fd), (k, ad, fd)
+
+
+def test_path_adjoint_mixed_matches_fp64():
+    rng = np.random.default_rng(9)
+    fy0 = rng.uniform(200, 300, 8)
+    H = rng.uniform(800, 1200, 8)
+    J64, adj64, ddofs, top, asm64 = _path_problem(fy0, H)
+    g64 = _path_gradient(adj64, ddofs, top, asm64)
+    J32, adj32, _, _, asm32 = _path_problem(fy0, H, precision="mixed", linsolver="pcg")
+    g32 = _path_gradient(adj32, ddofs, top, asm32)
+    assert abs(J32 - J64) <= 1e-9 * abs(J64)
+    for k in (2, 3):
+        assert np.abs(g32[:, k] - g64[:, k]).max() <= 1e-8 * np.abs(g64[:, k]).max(), k
