@@ -34,6 +34,9 @@ EXPORTS = [
     "efe_compute_elements_persistent",
     "efe_compute_elements_persistent_noalloc",
     "efe_accept_state",
+    "efe_csr_spmv",
+    "efe_pcg_start",
+    "efe_pcg_iterate",
     "efe_body_force",
     "efe_adjoint_tl",
     "efe_adjoint_small_strain",
@@ -77,6 +80,27 @@ class EfeGroup(ctypes.Structure):
         ("auxRef", ctypes.c_void_p),
         ("auxTemp", ctypes.c_void_p),
         ("tileVariant", ctypes.c_int32),
+    ]
+
+
+EFE_PCG_WORK_DOUBLES = 6152
+
+
+class EfePcg(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_int64),
+        ("indptr", ctypes.c_void_p),
+        ("indices", ctypes.c_void_p),
+        ("Kdata", ctypes.c_void_p),
+        ("kPrecision", ctypes.c_int32),
+        ("freeMask", ctypes.c_void_p),
+        ("dinv", ctypes.c_void_p),
+        ("x", ctypes.c_void_p),
+        ("r", ctypes.c_void_p),
+        ("z", ctypes.c_void_p),
+        ("p", ctypes.c_void_p),
+        ("Ap", ctypes.c_void_p),
+        ("work", ctypes.c_void_p),
     ]
 
 
@@ -152,6 +176,12 @@ def load(build_if_missing=False):
     lib.efe_compute_elements_persistent.argtypes = [ctypes.POINTER(EfeWorkItem), i32, i32, P, P, P]
     lib.efe_compute_elements_persistent_noalloc.restype = i32
     lib.efe_compute_elements_persistent_noalloc.argtypes = [ctypes.POINTER(EfeWorkItem), i32, i32, P, P]
+    lib.efe_csr_spmv.restype = i32
+    lib.efe_csr_spmv.argtypes = [ctypes.POINTER(EfePcg), P, P, P]
+    lib.efe_pcg_start.restype = i32
+    lib.efe_pcg_start.argtypes = [ctypes.POINTER(EfePcg), P, P]
+    lib.efe_pcg_iterate.restype = i32
+    lib.efe_pcg_iterate.argtypes = [ctypes.POINTER(EfePcg), i64, i32, P]
     lib.efe_accept_state.restype = i32
     lib.efe_accept_state.argtypes = [ctypes.POINTER(EfeGroup), i32, P]
     lib.efe_pattern_count.restype = i64

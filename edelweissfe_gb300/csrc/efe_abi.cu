@@ -460,6 +460,48 @@ int32_t efe_compute_elements_persistent_noalloc(const EfeWorkItem* items, int32_
   return EFE_OK;
 }
 
+namespace {
+int32_t check_pcg(const EfePcg* s) {
+  if (!s) return fail(EFE_ERR_ARGUMENT, "null solver");
+  if (s->n < 0) return fail(EFE_ERR_ARGUMENT, "negative system size");
+  if (s->kPrecision != EFE_K_FP64 && s->kPrecision != EFE_K_FP32 && s->kPrecision != EFE_K_FP32_FF)
+    return fail(EFE_ERR_ARGUMENT, "unknown K precision");
+  if (s->n > 0 && (!s->indptr || !s->indices || !s->Kdata || !s->dinv || !s->x || !s->r || !s->z || !s->p ||
+                   !s->Ap || !s->work))
+    return fail(EFE_ERR_ARGUMENT, "null solver buffer");
+  return EFE_OK;
+}
+}  // namespace
+
+int32_t efe_csr_spmv(const EfePcg* s, const double* x, double* y, void* stream) {
+  int32_t rc = check_pcg(s);
+  if (rc) return rc;
+  if (s->n > 0 && (!x || !y)) return fail(EFE_ERR_ARGUMENT, "null vector");
+  cudaError_t e = efe::csr_spmv(*s, x, y, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "efe_csr_spmv");
+  return EFE_OK;
+}
+
+int32_t efe_pcg_start(const EfePcg* s, const double* b, void* stream) {
+  int32_t rc = check_pcg(s);
+  if (rc) return rc;
+  if (s->n > 0 && !b) return fail(EFE_ERR_ARGUMENT, "null right-hand side");
+  if (s->n == 0) return EFE_OK;
+  cudaError_t e = efe::pcg_start(*s, b, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "efe_pcg_start");
+  return EFE_OK;
+}
+
+int32_t efe_pcg_iterate(const EfePcg* s, int64_t firstIteration, int32_t nIterations, void* stream) {
+  int32_t rc = check_pcg(s);
+  if (rc) return rc;
+  if (firstIteration < 0 || nIterations < 0) return fail(EFE_ERR_ARGUMENT, "negative iteration count");
+  if (s->n == 0) return EFE_OK;
+  cudaError_t e = efe::pcg_iterate(*s, firstIteration, nIterations, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "efe_pcg_iterate");
+  return EFE_OK;
+}
+
 int32_t efe_accept_state(const EfeGroup* groups, int32_t nGroups, void* stream) {
   if (!groups || nGroups < 0) return fail(EFE_ERR_ARGUMENT, "null argument");
   cudaStream_t st = (cudaStream_t)stream;

@@ -150,6 +150,10 @@ cudaError_t persistent_pair(int shapeA, int ruleA, int formA, int shapeB, int ru
 // the counter runs through (written before the range check)
 cudaError_t persistent_pair_noalloc(int shapeA, int ruleA, int formA, int shapeB, int ruleB, int formB, int kprec,
                                     const GroupArgs& a, const GroupArgs& b, int64_t* needed, cudaStream_t st);
+// device linear solve (efe_solve.cu)
+cudaError_t csr_spmv(const EfePcg& s, const double* x, double* y, cudaStream_t st);
+cudaError_t pcg_start(const EfePcg& s, const double* b, cudaStream_t st);
+cudaError_t pcg_iterate(const EfePcg& s, int64_t k0, int nIter, cudaStream_t st);
 cudaError_t adjoint_ss_quad4(int rule, const SSAdjointArgs& a, cudaStream_t st);
 cudaError_t adjoint_ss_quad8(int rule, const SSAdjointArgs& a, cudaStream_t st);
 cudaError_t adjoint_ss_hexa8(int rule, const SSAdjointArgs& a, cudaStream_t st);

@@ -314,46 +314,51 @@ class NISTGPU:
         return torch.from_numpy(np.asarray(x, np.float64)).to(self.asm.device)
 
     def _solve_pcg(self, K, R, dir_idx):
-        """Jacobi-preconditioned CG on the device.  The reference's system has identity rows for the
-        Dirichlet DOFs; moving the known values to the right-hand side gives the same solution from a
-        symmetric positive-definite system on the free DOFs."""
+        """Jacobi-preconditioned CG on the device (efe_pcg_start / efe_pcg_iterate).  The reference's
+        system has identity rows for the Dirichlet DOFs; moving the known values to the right-hand
+        side gives the same solution from the symmetric positive-definite system on the free DOFs:
+        x = x_d + y with x_d = R on the prescribed DOFs and K_ff y_f = R_f - K_fd x_d.  K is used as
+        assembled (FP32 or FP64 values).  Converged when |r| <= pcgTolerance |b| (checked every
+        10 iterations, as b's norm includes the prescribed values)."""
+        import ctypes
+
+        from . import _lib as L
+
         asm = self.asm
-        Kd = K.double() if K.dtype != torch.float64 else K
-        A = torch.sparse_csr_tensor(asm.indptr, asm.indices, Kd, size=(asm.nDof, asm.nDof))
-        m = torch.ones(asm.nDof, dtype=torch.float64, device=asm.device)
+        dev = asm.device
+        n = asm.nDof
+        lib = L.load()
+        m = torch.ones(n, dtype=torch.uint8, device=dev)
         if dir_idx is not None:
-            m[dir_idx] = 0.0
-        xd = (1.0 - m) * R
-        b = m * (R - (A @ xd.unsqueeze(1)).squeeze(1)) + xd
-
-        def op(v):
-            return m * (A @ (m * v).unsqueeze(1)).squeeze(1) + (1.0 - m) * v
-
-        d = Kd[self._diag_pos]
+            m[dir_idx] = 0
+        mf = m.to(torch.float64)
+        d = K[self._diag_pos].to(torch.float64)
         dinv = torch.where(m > 0, 1.0 / d, torch.ones_like(d))
-        x = xd.clone()
-        r = b - op(x)
-        z = dinv * r
-        p = z.clone()
-        rz = torch.dot(r, z)
-        bnorm = float(torch.linalg.vector_norm(b))
+        vec = torch.empty((5, n), dtype=torch.float64, device=dev)
+        work = torch.zeros(L.EFE_PCG_WORK_DOUBLES, dtype=torch.float64, device=dev)
+        kp = L.EFE_K_FP64 if K.dtype == torch.float64 else L.EFE_K_FP32
+        s = L.EfePcg(n, asm.indptr.data_ptr(), asm.indices.data_ptr(), K.data_ptr(), kp, m.data_ptr(), dinv.data_ptr(),
+                     *[vec[i].data_ptr() for i in range(5)], work.data_ptr())  # fmt: skip
+        stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        xd = (1.0 - mf) * R
+        Kxd = torch.empty_like(R)
+        L.check(lib.efe_csr_spmv(ctypes.byref(s), ctypes.c_void_p(xd.data_ptr()), ctypes.c_void_p(Kxd.data_ptr()),
+                                 stream), "efe_csr_spmv")  # fmt: skip
+        b = mf * (R - Kxd)
+        bnorm = float(torch.linalg.vector_norm(b + xd))
+        L.check(lib.efe_pcg_start(ctypes.byref(s), ctypes.c_void_p(b.data_ptr()), stream), "efe_pcg_start")
+        tol2 = (self.pcgTolerance * bnorm) ** 2
         k = 0
-        if bnorm == 0.0 or float(torch.linalg.vector_norm(r)) <= self.pcgTolerance * bnorm:
-            self.linearIterations.append(0)
-            return x
-        for k in range(1, self.pcgMaxIter + 1):
-            Ap = op(p)
-            pAp = torch.dot(p, Ap)
-            if float(pAp) == 0.0:
+        if bnorm > 0.0 and float(work[2]) > tol2:
+            while k < self.pcgMaxIter:
+                step = min(10, self.pcgMaxIter - k)
+                L.check(lib.efe_pcg_iterate(ctypes.byref(s), k, step, stream), "efe_pcg_iterate")
+                k += step
+                rr = float(work[2])
+                if not rr <= tol2:
+                    if rr != rr or float(work[3]) == 0.0:  # NaN or a breakdown (p.Ap = 0)
+                        break
+                    continue
                 break
-            alpha = rz / pAp
-            x += alpha * p
-            r -= alpha * Ap
-            if k % 10 == 0 and float(torch.linalg.vector_norm(r)) <= self.pcgTolerance * bnorm:
-                break
-            z = dinv * r
-            rz_new = torch.dot(r, z)
-            p = z + (rz_new / rz) * p
-            rz = rz_new
         self.linearIterations.append(k)
-        return x
+        return vec[0] + xd

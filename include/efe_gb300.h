@@ -233,6 +233,38 @@ int32_t efe_compute_elements_persistent(const EfeWorkItem* items, int32_t nItems
 int32_t efe_compute_elements_persistent_noalloc(const EfeWorkItem* items, int32_t nItems, int32_t kPrecision,
                                                 int32_t* status, void* stream);
 
+/* Linear solve on the device: Jacobi-preconditioned conjugate gradients on the free DOFs of the
+   assembled tangent, in place of the reference's direct solve of the Newton correction
+   (linearSolve, solvers/nonlinearimplicitstatic.py:727-751: PARDISO, or SciPy's SuperLU on the
+   row-modified system of applyDirichletK, :559-593).  The operator is A_ij = K_ij on free rows
+   (free_i = 1) and the identity on prescribed rows; K is read as assembled (double or float per
+   kPrecision, int32 CSR), products accumulate in FP64.  efe_pcg_start sets x = 0, r = b,
+   z = dinv r, p = z for a right-hand side b that is zero on the prescribed DOFs;
+   efe_pcg_iterate runs nIterations CG steps (firstIteration = the number already run, whose
+   parity selects the scalar buffers); work[2] then holds r.r for the convergence test (one
+   small device-to-host read per batch of iterations).  All vectors are caller-owned [n] device
+   arrays; work is EFE_PCG_WORK_DOUBLES doubles of caller-owned device scratch. */
+#define EFE_PCG_WORK_DOUBLES 6152
+typedef struct EfePcg {
+  int64_t n;
+  const int32_t* indptr;
+  const int32_t* indices;
+  const void* Kdata;       /* CSR data, double (EFE_K_FP64) or float (EFE_K_FP32, EFE_K_FP32_FF) */
+  int32_t kPrecision;
+  const uint8_t* freeMask; /* [n] 1 = free DOF, 0 = prescribed; NULL = all free                  */
+  const double* dinv;      /* [n] 1 / K_ii on free DOFs, 1 on prescribed ones                   */
+  double* x;
+  double* r;
+  double* z;
+  double* p;
+  double* Ap;
+  double* work;
+} EfePcg;
+/* y_i = free_i ? (K x)_i : x_i */
+int32_t efe_csr_spmv(const EfePcg* solver, const double* x, double* y, void* stream);
+int32_t efe_pcg_start(const EfePcg* solver, const double* b, void* stream);
+int32_t efe_pcg_iterate(const EfePcg* solver, int64_t firstIteration, int32_t nIterations, void* stream);
+
 /* acceptLastState: stateTemp -> stateRef and auxTemp -> auxRef for every group. */
 int32_t efe_accept_state(const EfeGroup* groups, int32_t nGroups, void* stream);
 

@@ -129,7 +129,9 @@ def test_objective_gradient_matches_finite_differences():
 
 def test_autograd_function_matches_finite_differences():
     """TLEquilibrium behind torch.autograd: J(U(E, X)) backpropagates to E and X; checked against
-    central differences of the same objective along one random direction each."""
+    central differences of the same objective along one random direction each (h = 1e-5: a step
+    of 1e-6 moves J by ~1e-9 of itself here, the order of the Newton solution's own accuracy)."""
+    h = 1e-5
     from edelweissfe_gb300 import ElementGroup, GPUAssembler, meshes
     from edelweissfe_gb300.adjoint import TLEquilibrium, TLProblem, young_to_lame
     from edelweissfe_gb300.solver import AdaptiveTimeStepper, Dirichlet
@@ -158,10 +160,10 @@ def test_autograd_function_matches_finite_differences():
     J(E, X).backward()
     with torch.no_grad():
         dE = torch.as_tensor(rng.normal(0, 1, len(conn)) * E0, device=asm.device)
-        fd = (float(J(E + H * dE, X)) - float(J(E - H * dE, X))) / (2 * H)
+        fd = (float(J(E + h * dE, X)) - float(J(E - h * dE, X))) / (2 * h)
         ad = float((E.grad * dE).sum())
         assert abs(ad - fd) <= RTOL * abs(fd), ("E", ad, fd)
         dX = torch.as_tensor(rng.normal(0, 1, coords.shape), device=asm.device)
-        fd = (float(J(E, X + H * dX)) - float(J(E, X - H * dX))) / (2 * H)
+        fd = (float(J(E, X + h * dX)) - float(J(E, X - h * dX))) / (2 * h)
         ad = float((X.grad * dX).sum())
         assert abs(ad - fd) <= RTOL * abs(fd), ("X", ad, fd)
