@@ -592,6 +592,136 @@ def run_adjoint(args):
     }))
 
 
+# ------------------------------------------------------------------ plastic-path adjoint (Hexa20 J2)
+def plastic_setup(n=96, seed=8):
+    """boxGen C3D20 (3x3x3 Gauss) n x n x n/2 on [0,2]x[0,2]x[0,1]; von Mises with E = 210000,
+    nu = 0.3 and per-element yield stress U[200, 300], hardening U[800, 1200] (seed 8); bottom
+    u_y = 0, left u_x = 0, back u_z = 0, top u_y -> 0.01 (0.5 % strain) in 10 increments."""
+    from edelweissfe_gb300 import meshes
+
+    coords, conn, nodeDof, nDof = meshes.box(n, n, max(1, n // 2), lX=2.0, lY=2.0, lZ=1.0, nNodes=20)
+    rng = np.random.default_rng(seed)
+    E = len(conn)
+    props = np.stack([np.full(E, 210e3), np.full(E, 0.3), rng.uniform(200, 300, E), rng.uniform(800, 1200, E),
+                      np.zeros(E), np.zeros(E)], 1)  # fmt: skip
+    x, y, z = coords[:, 0], coords[:, 1], coords[:, 2]
+    top = nodeDof[y > 2 - 1e-9] + 1
+    bcs = [(nodeDof[y < 1e-9] + 1, 0.0), (nodeDof[x < 1e-9], 0.0), (nodeDof[z < 1e-9] + 2, 0.0), (top, 0.01)]
+    return coords, conn, nodeDof, nDof, props, bcs, top
+
+
+def run_plastic(args):
+    """Gradient of the total top reaction after 10 plastic increments w.r.t. the per-element yield
+    stress and hardening (config: C3D20 J2 96x96x48).  Forward: Newton (mixed: FP32 tangent, FP64
+    residual and return map) with the device PCG, checkpointing the history per increment.
+    Backward: PathAdjoint (tangent recomputed per increment from its checkpoint, two reverse
+    passes, one adjoint PCG solve refined against the exact FP64 operator).  `value` = gradient
+    evaluations per second of the element work of the backward sweep (recomputation + reverse
+    passes over all increments), excluding the adjoint solves, which are reported separately.
+    Also reported: one element pass at the final increment in mixed and FP64 (elem/s)."""
+    import torch
+
+    from edelweissfe_gb300 import ElementGroup, GPUAssembler
+    from edelweissfe_gb300.adjoint import PathAdjoint
+    from edelweissfe_gb300.solver import AdaptiveTimeStepper, Dirichlet, NISTGPU
+
+    n = args.n if args.n != N_CUBE else 96
+    t0 = time.perf_counter()
+    coords, conn, nodeDof, nDof, props, bcs, top = plastic_setup(n)
+    dirichlets = [Dirichlet(d, v) for d, v in bcs]
+    ddofs = np.unique(np.concatenate([d for d, _ in bcs]))
+
+    def forward(pr, precision="mixed"):
+        asm = GPUAssembler(coords, nodeDof, nDof, [ElementGroup("C3D20", "vonmises", pr, conn)], precision=precision)
+        solver = NISTGPU(asm, linsolver="pcg", extrapolation="linear", maxIter=15, fluxResidualTolerance=1e-10,
+                         fieldCorrectionTolerance=1e-10, fluxResidualFloor=0.0, pcgTolerance=args.pcg_tol)  # fmt: skip
+        adj = PathAdjoint(solver)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        solver.solveStep(AdaptiveTimeStepper(maxIncrement=0.1, startIncrement=0.1), dirichlets)
+        torch.cuda.synchronize()
+        J = -float(solver.lastP[torch.as_tensor(top, device=asm.device)].sum())
+        return asm, solver, adj, J, time.perf_counter() - t
+
+    asm, solver, adj, J, fwd_s = forward(props)
+    setup_s = time.perf_counter() - t0 - fwd_s
+    newton = [h["iterations"] for h in solver.history]
+    pcg_fwd = sum(solver.linearIterations)
+    cP = asm.constructDofVector()
+    cP[torch.as_tensor(top, device=asm.device)] = -1.0
+    solver.pcgTolerance = args.pcg_tol_adjoint
+    timing = {}
+    t = time.perf_counter()
+    g = adj.gradient(ddofs, cP=cP, timing=timing)[0]
+    torch.cuda.synchronize()
+    bwd_s = time.perf_counter() - t
+    pcg_adj = [sum(x) for x in adj.linearIterations]
+    gH = g[:, 3].cpu().numpy()
+    gy = g[:, 2].cpu().numpy()
+    plastic = float((asm.groups[0]._dev["stateRef"][12] > 0).double().mean())
+
+    # one element pass at the final increment, mixed and FP64, from the last checkpoint
+    ck = adj.checkpoints[-1]
+    passes = {}
+    for precision in ("mixed", "fp64"):
+        a2 = asm if precision == "mixed" else GPUAssembler(coords, nodeDof, nDof, [ElementGroup(
+            "C3D20", "vonmises", props, conn)], precision="fp64")  # fmt: skip
+        a2.groups[0]._dev["stateRef"].copy_(ck["states"][0])
+        P, F, K = a2.constructDofVector(), a2.constructDofVector(), a2.constructSystemMatrix()
+        evs = []
+        for k in range(args.warmup + args.steps):
+            P.zero_()
+            F.zero_()
+            K.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            a2.launch(ck["U"], ck["dU"], P, K, F)
+            e1.record()
+            if k >= args.warmup:
+                evs.append((e0, e1))
+        torch.cuda.synchronize()
+        a2.check_status()
+        ms = sum(a.elapsed_time(b) for a, b in evs) / len(evs)
+        passes[precision] = {"ms": ms, "elem_per_s": len(conn) / (ms * 1e-3)}
+        if precision == "fp64":
+            del a2, P, F, K
+            torch.cuda.empty_cache()
+
+    fd = None
+    if args.plastic_fd:
+        rng = np.random.default_rng(11)
+        errs = []
+        for _ in range(args.plastic_fd):
+            d = np.zeros_like(props)
+            d[:, 2] = rng.normal(0, 1, len(conn)) * props[:, 2]
+            d[:, 3] = rng.normal(0, 1, len(conn)) * props[:, 3]
+            h = 1e-6
+            Jp = forward(props + h * d)[3]
+            Jm = forward(props - h * d)[3]
+            f = (Jp - Jm) / (2 * h)
+            ad = float(np.sum(gy * d[:, 2]) + np.sum(gH * d[:, 3]))
+            errs.append(abs(ad - f) / abs(f))
+        fd = {"directions": args.plastic_fd, "h": 1e-6, "max_rel_err": max(errs), "errors": errs}
+    nInc = len(adj.checkpoints)
+    print(json.dumps({
+        "metric": "adjoint grads/s (dJ/d(fy0, H) per element through the plastic path), excluding the adjoint solves",
+        "value": 1e3 / timing["kernel_ms"], "unit": "grad/s", "higher_is_better": True,
+        "dtype": "f64 residual/state/return map + f32 tangent (mixed); f64 reverse passes", "data": "synthetic",
+        "config": {"workload": f"C3D20 von Mises J2 {n}x{n}x{max(1, n // 2)} on [0,2]x[0,2]x[0,1], per-element "
+                               "fy0 ~ U[200,300], H ~ U[800,1200], 10 uniaxial increments to 0.5% strain; "
+                               "J = total top reaction", "elements": len(conn), "dofs": nDof, "nnz": int(asm.nnz)},
+        "backward_kernel_ms": timing["kernel_ms"], "backward_solve_ms": timing["solve_ms"], "backward_wall_s": bwd_s,
+        "increments": nInc, "adjoint_pcg_iterations": pcg_adj,
+        "forward_wall_s": fwd_s, "forward_newton_iterations": newton, "forward_pcg_iterations": pcg_fwd,
+        "pcg_tolerance": {"forward": args.pcg_tol, "adjoint": args.pcg_tol_adjoint},
+        "J": J, "plastic_point_fraction": plastic,
+        "grad_norm": {"fy0": float(np.linalg.norm(gy)), "H": float(np.linalg.norm(gH))},
+        "element_pass": passes, "mixed_over_fp64": passes["fp64"]["ms"] / passes["mixed"]["ms"],
+        "setup_s": setup_s, "fd_check": fd,
+        "gpu_launches": 3 * nInc,
+    }))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -600,9 +730,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_CUBE, help="elements per cube edge")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="cube", choices=["cube", "batched", "newton", "adjoint"],
+    ap.add_argument("--workload", default="cube", choices=["cube", "batched", "newton", "adjoint", "plastic"],
                     help="cube: the 64^3 von Mises headline; batched: the uneven-mesh batch; newton: Newton "
-                         "iterations FP64 vs mixed on the 64^3 cube; adjoint: 32^3 Neo-Hooke gradients")
+                         "iterations FP64 vs mixed on the 64^3 cube; adjoint: 32^3 Neo-Hooke gradients; "
+                         "plastic: Hexa20 J2 96x96x48 path adjoint")
+    ap.add_argument("--plastic-fd", type=int, default=0, help="FD directions for the plastic workload")
+    ap.add_argument("--pcg-tol", type=float, default=1e-8, help="forward Newton PCG tolerance (plastic)")
+    ap.add_argument("--pcg-tol-adjoint", type=float, default=1e-10, help="adjoint PCG tolerance (plastic)")
     ap.add_argument("--fd-directions", type=int, default=3)
     ap.add_argument("--batch-meshes", type=int, default=512)
     ap.add_argument("--batch-scale", type=float, default=1.0)
@@ -615,9 +749,10 @@ def main():
         if rank == 0:
             run_reference(args)
         return
-    if args.workload in ("batched", "newton", "adjoint"):
+    if args.workload in ("batched", "newton", "adjoint", "plastic"):
         if rank == 0:
-            {"batched": run_batched, "newton": run_newton, "adjoint": run_adjoint}[args.workload](args)
+            {"batched": run_batched, "newton": run_newton, "adjoint": run_adjoint,
+             "plastic": run_plastic}[args.workload](args)
         return
     if world > 1:
         import torch

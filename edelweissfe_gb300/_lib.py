@@ -101,6 +101,7 @@ class EfePcg(ctypes.Structure):
         ("p", ctypes.c_void_p),
         ("Ap", ctypes.c_void_p),
         ("work", ctypes.c_void_p),
+        ("pFF", ctypes.c_void_p),
     ]
 
 

@@ -126,10 +126,12 @@ class PathAdjoint:
     Checkpoints hold one state array per group and increment (13 doubles per point for von Mises),
     i.e. history memory grows with the number of increments; nothing else is stored."""
 
-    def __init__(self, solver, refine_steps=2):
+    def __init__(self, solver, refine_steps=2, refine_tolerance=1e-4):
         self.solver = solver
         self.asm = solver.asm
         self.refine_steps = refine_steps
+        # each refinement only has to shrink the error left by the FP32 tangent (~1e-7 relative)
+        self.refine_tolerance = refine_tolerance
         self.checkpoints = []
         solver.onAccept = self._record
 
@@ -145,8 +147,20 @@ class PathAdjoint:
             asm.adjointSmallStrain(gi, ck["states"][gi], ck["dU"], out, Pbar=v)
         return -out
 
-    def gradient(self, dirichletDofs, cP=None, cU=None):
-        """dJ/dprops per group ([E, nProps] tensors) for J = cP . P_N + cU . u_N."""
+    def gradient(self, dirichletDofs, cP=None, cU=None, timing=None):
+        """dJ/dprops per group ([E, nProps] tensors) for J = cP . P_N + cU . u_N.  With a dict as
+        `timing`, the device time of the element work (tangent recomputation and the two reverse
+        passes per increment) and of the adjoint solves is added to timing["kernel_ms"] and
+        timing["solve_ms"] (CUDA events on the current stream)."""
+
+        def event():
+            if timing is None:
+                return None
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record()
+            return ev
+
+        marks = []
         asm = self.asm
         solver = self.solver
         dev = asm.device
@@ -166,12 +180,14 @@ class PathAdjoint:
             # recompute increment n from its checkpoint: the tangent K_n
             for gi, g in enumerate(asm.groups):
                 g._dev["stateRef"].copy_(ck["states"][gi])
+            e0 = event()
             K = solver.tangentAt_increment(ck["U"], ck["dU"])
             a = asm.constructDofVector()
             sprev = [torch.zeros_like(s) for s in sbar]
             for gi in range(len(asm.groups)):
                 asm.adjointSmallStrain(gi, ck["states"][gi], ck["dU"], a, Pbar=cP if last else None,
                                        stateBarIn=sbar[gi], stateBarOut=sprev[gi], gProps=gP[gi])  # fmt: skip
+            e1 = event()
             rhs = a + carry
             if last and cU is not None:
                 rhs = rhs + cU
@@ -180,20 +196,33 @@ class PathAdjoint:
             n0 = len(solver.linearIterations)
             lam = solver.linearSolve(K, rhs, dir_idx)
             if K.dtype != torch.float64:
-                for _ in range(self.refine_steps):
-                    r = rhs - self._exact_Kv(ck, lam)
-                    if dir_idx is not None:
-                        r[dir_idx] = 0.0
-                    lam = lam + solver.linearSolve(K, r, dir_idx)
+                tol = solver.pcgTolerance
+                solver.pcgTolerance = max(tol, self.refine_tolerance)
+                try:
+                    for _ in range(self.refine_steps):
+                        r = rhs - self._exact_Kv(ck, lam)
+                        if dir_idx is not None:
+                            r[dir_idx] = 0.0
+                        lam = lam + solver.linearSolve(K, r, dir_idx)
+                finally:
+                    solver.pcgTolerance = tol
             if dir_idx is not None:
                 lam[dir_idx] = 0.0
             self.linearIterations.append(solver.linearIterations[n0:])
+            e2 = event()
             b = asm.constructDofVector()
             for gi in range(len(asm.groups)):
                 asm.adjointSmallStrain(gi, ck["states"][gi], ck["dU"], b, Pbar=lam, stateBarOut=sprev[gi],
                                        gProps=gP[gi])  # fmt: skip
+            e3 = event()
+            marks.append((e0, e1, e2, e3))
             carry = -(a + b)
             sbar = sprev
         for gi, g in enumerate(asm.groups):
             g._dev["stateRef"].copy_(saved[gi])
+        if timing is not None:
+            torch.cuda.synchronize(dev)
+            timing["kernel_ms"] = timing.get("kernel_ms", 0.0) + sum(
+                a.elapsed_time(b) + c.elapsed_time(d) for a, b, c, d in marks)
+            timing["solve_ms"] = timing.get("solve_ms", 0.0) + sum(b.elapsed_time(c) for a, b, c, d in marks)
         return gP

@@ -469,6 +469,7 @@ int32_t check_pcg(const EfePcg* s) {
   if (s->n > 0 && (!s->indptr || !s->indices || !s->Kdata || !s->dinv || !s->x || !s->r || !s->z || !s->p ||
                    !s->Ap || !s->work))
     return fail(EFE_ERR_ARGUMENT, "null solver buffer");
+  if (reinterpret_cast<uintptr_t>(s->pFF) % 8 != 0) return fail(EFE_ERR_ARGUMENT, "pFF must be 8-byte aligned");
   return EFE_OK;
 }
 }  // namespace

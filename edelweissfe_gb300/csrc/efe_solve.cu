@@ -3,10 +3,21 @@
 // solvers/nonlinearimplicitstatic.py:727-751) and the adjoint systems.
 //
 // The matrix is the CSR data the element pass assembled (FP32 or FP64 values, int32 pattern); it is
-// never converted.  Products accumulate in FP64; vectors are FP64.  The operator is K restricted
+// never converted.  Vectors and scalars are FP64.  The operator is K restricted
 // to the free rows (prescribed rows are the identity): CG starts from x = 0 with a right-hand side
 // that is zero on the prescribed DOFs, so every search direction is zero there and the column
 // restriction comes for free.
+//
+// Precision of the product.  This part issues FP64 at ~1/60 of its FP32 rate, so a product that
+// spends even two FP64 operations per stored entry (a float->double conversion and a DFMA) is
+// bound by the FP64 pipe, not by memory.  For FP32 tangents the CG iterations therefore keep the
+// search direction also as float-float pairs (pFF[i] = (hi, lo), ~48-bit significand, written once per DOF
+// by the vector kernels) and form every product and partial sum in float-float arithmetic on the
+// FP32 pipe: k * (xh + xl) = fl(k xh) + [fma(k, xh, -fl(k xh)) + k xl], accumulated with
+// error-free sums; one conversion to double per row.  The result carries ~2^-48 relative error of
+// sum |K_ij x_j| -- below the attainable accuracy of a CG residual at any tolerance used here, and
+// the Newton and adjoint drivers check their solutions with FP64 residuals.  FP64 tangents use
+// DFMA.  Eight lanes per row (four rows per warp) keep the cross-lane reduction short.
 //
 // One iteration is three kernels: (1) Ap = A p with the partial sums of p.Ap per block, (2) alpha,
 // x += alpha p, r -= alpha Ap, z = D^-1 r with the partial sums of r.z and r.r, (3) beta,
@@ -54,30 +65,97 @@ __device__ __forceinline__ double sum_partials(const double* part, int n, double
   return sh[WARPS];
 }
 
-template <typename KT>
-__device__ __forceinline__ double row_product(int64_t r, const int32_t* __restrict__ indptr,
-                                              const int32_t* __restrict__ indices, const KT* __restrict__ K,
-                                              const double* __restrict__ x, int lane) {
-  const int32_t b = indptr[r], e = indptr[r + 1];
-  double s = 0.0;
-  for (int32_t j = b + lane; j < e; j += 32) s = fma((double)K[j], x[indices[j]], s);
-  return warp_sum(s);
+constexpr int G = 8;  // lanes per row
+
+__device__ __forceinline__ double group_sum(double v) {
+  v += __shfl_xor_sync(0xffffffffu, v, 4);
+  v += __shfl_xor_sync(0xffffffffu, v, 2);
+  v += __shfl_xor_sync(0xffffffffu, v, 1);
+  return v;
 }
 
-// y_i = free_i ? (K x)_i : x_i; with part != null also the block partials of x.y.
+// (h, l) += (a, b): error-free sum of the high parts, low parts added
+__device__ __forceinline__ void ff_acc(float& h, float& l, float a, float b) {
+  const float s = __fadd_rn(h, a);
+  const float bb = __fsub_rn(s, h);
+  const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(a, bb));
+  l = __fadd_rn(l, __fadd_rn(err, b));
+  h = s;
+}
+// (h, l) += k * (xh + xl)
+__device__ __forceinline__ void ff_madd(float& h, float& l, float k, float xh, float xl) {
+  const float p = __fmul_rn(k, xh);
+  float e = __fmaf_rn(k, xh, -p);
+  e = __fmaf_rn(k, xl, e);
+  ff_acc(h, l, p, e);
+}
+
+// (K x)_r with FP64 arithmetic (double or float values); every lane of the row's group gets it
 template <typename KT>
+__device__ __forceinline__ double row_product(int32_t b, int32_t e, const int32_t* __restrict__ indices,
+                                              const KT* __restrict__ K, const double* __restrict__ x, int sl) {
+  // four independent loads per lane per step: the rows of solid tangents hold 81-243 entries
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  for (int32_t j = b + sl; j < e; j += 4 * G) {
+    const bool p1 = j + G < e, p2 = j + 2 * G < e, p3 = j + 3 * G < e;
+    const int32_t c0 = indices[j];
+    const int32_t c1 = p1 ? indices[j + G] : c0, c2 = p2 ? indices[j + 2 * G] : c0, c3 = p3 ? indices[j + 3 * G] : c0;
+    const double k0 = (double)K[j], k1 = p1 ? (double)K[j + G] : 0.0, k2 = p2 ? (double)K[j + 2 * G] : 0.0,
+                 k3 = p3 ? (double)K[j + 3 * G] : 0.0;
+    s0 = fma(k0, x[c0], s0);
+    s1 = fma(k1, x[c1], s1);
+    s2 = fma(k2, x[c2], s2);
+    s3 = fma(k3, x[c3], s3);
+  }
+  return group_sum((s0 + s1) + (s2 + s3));
+}
+
+// (K x)_r with float values and x = xh + xl in float-float arithmetic (FP32 pipe only)
+__device__ __forceinline__ double row_product_ff(int32_t b, int32_t e, const int32_t* __restrict__ indices,
+                                                 const float* __restrict__ K, const float2* __restrict__ xf, int sl) {
+  float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f;
+  for (int32_t j = b + sl; j < e; j += 2 * G) {
+    const bool p1 = j + G < e;
+    const int32_t c0 = indices[j];
+    const int32_t c1 = p1 ? indices[j + G] : c0;
+    const float k0 = K[j], k1 = p1 ? K[j + G] : 0.f;
+    const float2 x0 = xf[c0], x1 = xf[c1];
+    ff_madd(h0, l0, k0, x0.x, x0.y);
+    ff_madd(h1, l1, k1, x1.x, x1.y);
+  }
+  ff_acc(h0, l0, h1, l1);
+  for (int o = 4; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, h0, o), ol = __shfl_xor_sync(0xffffffffu, l0, o);
+    ff_acc(h0, l0, oh, ol);
+  }
+  return (double)h0 + (double)l0;
+}
+
+// y_r = free_r ? (K x)_r : x_r for rows r; with part != null also the block partials of x.y.
+// FF: x is also given as the float-float pairs xf and K is float (the CG iterations of FP32 tangents).
+template <typename KT, bool FF>
 __global__ void __launch_bounds__(NT) spmv_kernel(int64_t n, const int32_t* __restrict__ indptr,
                                                   const int32_t* __restrict__ indices, const KT* __restrict__ K,
                                                   const uint8_t* __restrict__ freeMask, const double* __restrict__ x,
-                                                  double* __restrict__ y, double* part) {
+                                                  const float2* __restrict__ xf, double* __restrict__ y,
+                                                  double* part) {
   __shared__ double sh[WARPS + 1];
-  const int lane = threadIdx.x % 32;
+  const int lane = threadIdx.x % 32, g = lane / G, sl = lane % G;
+  constexpr int RPW = 32 / G;  // rows per warp and step
   const int64_t warp = ((int64_t)blockIdx.x * NT + threadIdx.x) / 32;
   const int64_t nw = (int64_t)gridDim.x * WARPS;
   double acc = 0.0;
-  for (int64_t r = warp; r < n; r += nw) {
-    const double v = row_product(r, indptr, indices, K, x, lane);
-    if (lane == 0) {
+  // the loop condition depends on the warp only: all 32 lanes reach every shuffle
+  for (int64_t rb = warp * RPW; rb < n; rb += nw * RPW) {
+    const int64_t r = rb + g;
+    const bool live = r < n;
+    const int32_t b = live ? indptr[r] : 0, e = live ? indptr[r + 1] : 0;
+    double v;
+    if constexpr (FF)
+      v = row_product_ff(b, e, indices, reinterpret_cast<const float*>(K), xf, sl);
+    else
+      v = row_product(b, e, indices, K, x, sl);
+    if (live && sl == 0) {
       const double yr = (!freeMask || freeMask[r]) ? v : x[r];
       y[r] = yr;
       acc = fma(x[r], yr, acc);
@@ -93,7 +171,8 @@ __global__ void __launch_bounds__(NT) spmv_kernel(int64_t n, const int32_t* __re
 __global__ void __launch_bounds__(NT) pcg_start_kernel(int64_t n, const double* __restrict__ b,
                                                        const double* __restrict__ dinv, double* __restrict__ x,
                                                        double* __restrict__ r, double* __restrict__ z,
-                                                       double* __restrict__ p, double* work) {
+                                                       double* __restrict__ p, float2* __restrict__ pf,
+                                                       double* work) {
   __shared__ double sh[WARPS + 1];
   double rz = 0.0, rr = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
@@ -102,6 +181,10 @@ __global__ void __launch_bounds__(NT) pcg_start_kernel(int64_t n, const double* 
     r[i] = ri;
     z[i] = zi;
     p[i] = zi;
+    if (pf) {
+      const float h = __double2float_rn(zi);
+      pf[i] = make_float2(h, __double2float_rn(zi - (double)h));
+    }
     rz = fma(ri, zi, rz);
     rr = fma(ri, ri, rr);
   }
@@ -152,13 +235,20 @@ __global__ void __launch_bounds__(NT) pcg_update_kernel(int64_t n, int cur, int 
 
 // beta = rz_new / rz[cur]; p = z + beta p; block 0 stores rz_new in rz[cur ^ 1] and r.r in work[2]
 __global__ void __launch_bounds__(NT) pcg_direction_kernel(int64_t n, int cur, int nbVec, const double* __restrict__ z,
-                                                           double* __restrict__ p, double* work) {
+                                                           double* __restrict__ p, float2* __restrict__ pf,
+                                                           double* work) {
   __shared__ double sh[WARPS + 1];
   const double rzNew = sum_partials(work + PART1, nbVec, sh);
   const double rzOld = work[cur];
   const double beta = rzOld != 0.0 ? rzNew / rzOld : 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT)
-    p[i] = fma(beta, p[i], z[i]);
+  for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
+    const double pi = fma(beta, p[i], z[i]);
+    p[i] = pi;
+    if (pf) {  // float-float copy for the FP32 product: pi = h + l to ~48 bits
+      const float h = __double2float_rn(pi);
+      pf[i] = make_float2(h, __double2float_rn(pi - (double)h));
+    }
+  }
   if (blockIdx.x == 0) {
     const double rr = sum_partials(work + PART2, nbVec, sh);
     if (threadIdx.x == 0) {
@@ -177,8 +267,8 @@ int vec_blocks(int64_t n, int sms) {
 }
 
 int spmv_blocks(int64_t n, int sms) {
-  int64_t b = (n + WARPS - 1) / WARPS;
-  const int64_t cap = (int64_t)sms * 8;
+  int64_t b = (n + WARPS * (32 / G) - 1) / (WARPS * (32 / G));
+  const int64_t cap = (int64_t)sms * 6;  // resident blocks at <= 40 registers per thread
   if (b > cap) b = cap;
   if (b > MAX_BLOCKS) b = MAX_BLOCKS;
   return (int)(b < 1 ? 1 : b);
@@ -194,15 +284,21 @@ int sm_count() {
   return sms;
 }
 
-template <typename KT>
-cudaError_t spmv_t(const EfePcg& s, const double* x, double* y, double* part, int nb, cudaStream_t st) {
-  spmv_kernel<KT><<<nb, NT, 0, st>>>(s.n, s.indptr, s.indices, static_cast<const KT*>(s.Kdata), s.freeMask, x, y,
-                                      part);
+bool use_ff(const EfePcg& s) { return s.kPrecision != EFE_K_FP64 && s.pFF; }
+float2* pff(const EfePcg& s) { return use_ff(s) ? reinterpret_cast<float2*>(s.pFF) : nullptr; }
+
+template <typename KT, bool FF>
+cudaError_t spmv_t(const EfePcg& s, const double* x, const float2* xf, double* y, double* part, int nb,
+                   cudaStream_t st) {
+  spmv_kernel<KT, FF><<<nb, NT, 0, st>>>(s.n, s.indptr, s.indices, static_cast<const KT*>(s.Kdata), s.freeMask, x, xf,
+                                          y, part);
   return cudaGetLastError();
 }
 
+// FP64 arithmetic product (any x)
 cudaError_t spmv(const EfePcg& s, const double* x, double* y, double* part, int nb, cudaStream_t st) {
-  return s.kPrecision == EFE_K_FP64 ? spmv_t<double>(s, x, y, part, nb, st) : spmv_t<float>(s, x, y, part, nb, st);
+  return s.kPrecision == EFE_K_FP64 ? spmv_t<double, false>(s, x, nullptr, y, part, nb, st)
+                                    : spmv_t<float, false>(s, x, nullptr, y, part, nb, st);
 }
 
 }  // namespace
@@ -214,7 +310,7 @@ cudaError_t csr_spmv(const EfePcg& s, const double* x, double* y, cudaStream_t s
 
 cudaError_t pcg_start(const EfePcg& s, const double* b, cudaStream_t st) {
   const int nb = vec_blocks(s.n, sm_count());
-  pcg_start_kernel<<<nb, NT, 0, st>>>(s.n, b, s.dinv, s.x, s.r, s.z, s.p, s.work);
+  pcg_start_kernel<<<nb, NT, 0, st>>>(s.n, b, s.dinv, s.x, s.r, s.z, s.p, pff(s), s.work);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   pcg_start_finish<<<1, NT, 0, st>>>(s.work, nb);
@@ -224,13 +320,15 @@ cudaError_t pcg_start(const EfePcg& s, const double* b, cudaStream_t st) {
 cudaError_t pcg_iterate(const EfePcg& s, int64_t k0, int nIter, cudaStream_t st) {
   const int sms = sm_count();
   const int nbS = spmv_blocks(s.n, sms), nbV = vec_blocks(s.n, sms);
+  float2* pf = pff(s);
   for (int k = 0; k < nIter; ++k) {
     const int cur = (int)((k0 + k) & 1);
-    cudaError_t e = spmv(s, s.p, s.Ap, s.work + PART0, nbS, st);
+    cudaError_t e = pf ? spmv_t<float, true>(s, s.p, pf, s.Ap, s.work + PART0, nbS, st)
+                       : spmv(s, s.p, s.Ap, s.work + PART0, nbS, st);
     if (e != cudaSuccess) return e;
     pcg_update_kernel<<<nbV, NT, 0, st>>>(s.n, cur, nbS, s.p, s.Ap, s.dinv, s.x, s.r, s.z, s.work);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    pcg_direction_kernel<<<nbV, NT, 0, st>>>(s.n, cur, nbV, s.z, s.p, s.work);
+    pcg_direction_kernel<<<nbV, NT, 0, st>>>(s.n, cur, nbV, s.z, s.p, pf, s.work);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   return cudaSuccess;

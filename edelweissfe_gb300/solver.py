@@ -337,8 +337,10 @@ class NISTGPU:
         vec = torch.empty((5, n), dtype=torch.float64, device=dev)
         work = torch.zeros(L.EFE_PCG_WORK_DOUBLES, dtype=torch.float64, device=dev)
         kp = L.EFE_K_FP64 if K.dtype == torch.float64 else L.EFE_K_FP32
+        split = torch.empty((n, 2), dtype=torch.float32, device=dev) if kp == L.EFE_K_FP32 else None
         s = L.EfePcg(n, asm.indptr.data_ptr(), asm.indices.data_ptr(), K.data_ptr(), kp, m.data_ptr(), dinv.data_ptr(),
-                     *[vec[i].data_ptr() for i in range(5)], work.data_ptr())  # fmt: skip
+                     *[vec[i].data_ptr() for i in range(5)], work.data_ptr(),
+                     split.data_ptr() if split is not None else None)  # fmt: skip
         stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
         xd = (1.0 - mf) * R
         Kxd = torch.empty_like(R)

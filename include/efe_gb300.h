@@ -259,6 +259,9 @@ typedef struct EfePcg {
   double* p;
   double* Ap;
   double* work;
+  float* pFF;              /* optional [n][2], 8-byte aligned: with FP32 K the CG products run in
+                              float-float arithmetic on p = pFF[i][0] + pFF[i][1] (FP32 pipe);
+                              NULL: FP64 arithmetic                                            */
 } EfePcg;
 /* y_i = free_i ? (K x)_i : x_i */
 int32_t efe_csr_spmv(const EfePcg* solver, const double* x, double* y, void* stream);

@@ -52,7 +52,7 @@ def test_pcg_matches_direct_solve(elType, precision):
     work = torch.zeros(L.EFE_PCG_WORK_DOUBLES, dtype=torch.float64, device=asm.device)
     kp = L.EFE_K_FP64 if K.dtype == torch.float64 else L.EFE_K_FP32
     s = L.EfePcg(nDof, asm.indptr.data_ptr(), asm.indices.data_ptr(), K.data_ptr(), kp, None, y.data_ptr(),
-                 y.data_ptr(), y.data_ptr(), y.data_ptr(), y.data_ptr(), y.data_ptr(), work.data_ptr())  # fmt: skip
+                 y.data_ptr(), y.data_ptr(), y.data_ptr(), y.data_ptr(), y.data_ptr(), work.data_ptr(), None)  # fmt: skip
     L.check(L.load().efe_csr_spmv(ctypes.byref(s), ctypes.c_void_p(v.data_ptr()), ctypes.c_void_p(y.data_ptr()),
                                   None), "efe_csr_spmv")  # fmt: skip
     torch.cuda.synchronize()
