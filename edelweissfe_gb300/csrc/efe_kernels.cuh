@@ -158,12 +158,17 @@ struct Layout {
   static constexpr int DIM = ShapeInfo<SHAPE>::DIM, NN = ShapeInfo<SHAPE>::NN, NQ = RuleInfo<RULE>::NQ;
   static constexpr int NVEC = FormInfo<FORM, DIM>::NVEC, NSCAL = FormInfo<FORM, DIM>::NSCAL;
   static constexpr int NDOF = NN * DIM;
+  // total-Lagrangian Neo-Hooke: per-point record between its sub-phases (F, F^-1, tau, B, c1-c3, s)
+  // in FP64 and a copy of F, B, c1 s, c2 s, c3 s in the tangent's precision
+  static constexpr int NX = FORM == TLH ? 40 : 0, NXK = FORM == TLH ? 24 : 0;
   // offsets in bytes; doubles first for alignment
   static constexpr size_t u_off = 0;                                              // double [EPB][NN][DIM]
-  static constexpr size_t r_off = u_off + sizeof(double) * EPB * NDOF;            // double [EPB][NQ][NDOF]
+  static constexpr size_t x_off = u_off + sizeof(double) * EPB * NDOF;            // double [EPB][NQ][NX]
+  static constexpr size_t r_off = x_off + sizeof(double) * EPB * NQ * NX;         // double [EPB][NQ][NDOF]
   static constexpr size_t sc_off = r_off + sizeof(double) * EPB * NQ * NDOF;      // KT [EPB][NQ][NSCAL]
   static constexpr size_t v_off = sc_off + sizeof(KT) * EPB * NQ * NSCAL;         // KT [EPB][NQ][NN][NVEC][DIM]
-  static constexpr size_t mc_off = (v_off + sizeof(KT) * EPB * NQ * NN * NVEC * DIM + 15) / 16 * 16;  // VMConst [EPB]
+  static constexpr size_t xk_off = v_off + sizeof(KT) * EPB * NQ * NN * NVEC * DIM;  // KT [EPB][NQ][NXK]
+  static constexpr size_t mc_off = (xk_off + sizeof(KT) * EPB * NQ * NXK + 15) / 16 * 16;  // VMConst [EPB]
   static constexpr size_t rl_off = mc_off + sizeof(VMConst) * EPB;                                     // int [EPB][NN]
   static constexpr size_t bytes = rl_off + sizeof(int) * EPB * NN;
 };
@@ -221,6 +226,156 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
 
   // ---- phase A: material points
   const int64_t stride = nEl * NQ;
+  if constexpr (FORM == TLH) {
+    // Total Lagrangian Neo-Hooke (displacementtlelement/element.py:346-414) in three sub-phases, so
+    // the per-node work of a point (the heavy part for 20-node elements) runs one thread per
+    // (point, node) instead of one thread per point.
+    double* sx = reinterpret_cast<double*>(smem + L::x_off);
+    KT* sxk = reinterpret_cast<KT*>(smem + L::xk_off);
+    // A0: F = I + sum_a U_a (x) dN_a/dX, one thread per (point, component)
+    for (int t = threadIdx.x; t < EPB * NQ * DIM * DIM; t += NT) {
+      const int c = t / (EPB * NQ), r = t % (EPB * NQ);
+      const int le = r / NQ, q = r % NQ;
+      const int64_t e = e0 + le;
+      if (e >= nEl) continue;
+      const int i = c / DIM, j = c % DIM;
+      const int64_t pt = e * NQ + q;
+      const double* u = su + le * NN * DIM;
+      double h = 0.0;
+      for (int a = 0; a < NN; ++a) h += u[a * DIM + i] * g.geomG[(int64_t)(j * NN + a) * stride + pt];
+      double f = (i == j) ? 1.0 : 0.0;
+      f += h;
+      sx[(le * NQ + q) * L::NX + i * 3 + j] = f;
+    }
+    __syncthreads();
+    // A1: one thread per point: E, F^-1, Kirchhoff stress and its tangent scalars, state
+    for (int t = threadIdx.x; t < EPB * NQ; t += NT) {
+      const int le = t / NQ, q = t % NQ;
+      const int64_t e = e0 + le;
+      if (e >= nEl) continue;
+      const int64_t pt = e * NQ + q;
+      double* rec = sx + (le * NQ + q) * L::NX;
+      KT* reck = sxk + (le * NQ + q) * L::NXK;
+      const double* props = g.props + e * g.nProps;
+      double F[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+      for (int i = 0; i < DIM; ++i)
+        for (int j = 0; j < DIM; ++j) F[i][j] = rec[i * 3 + j];
+      // Green-Lagrange E = 1/2 (H + H^T + H^T H), H = F - I  (:386)
+      double Eg[3][3];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          double hh = 0.0;
+          for (int k = 0; k < DIM; ++k) hh += (F[k][i] - (k == i)) * (F[k][j] - (k == j));
+          Eg[i][j] = (i < DIM && j < DIM) ? 0.5 * ((F[i][j] - (i == j)) + (F[j][i] - (i == j)) + hh) : 0.0;
+        }
+      const double Ev[6] = {Eg[0][0], Eg[1][1], Eg[2][2], Eg[0][1], Eg[1][2], Eg[0][2]};
+      for (int f = 0; f < 6; ++f) g.auxTemp[(int64_t)f * stride + pt] = Ev[f];
+      double detF, iF[3][3];
+      if constexpr (DIM == 2) {
+        detF = F[0][0] * F[1][1] - F[0][1] * F[1][0];
+        iF[0][0] = F[1][1] / detF;
+        iF[0][1] = -F[0][1] / detF;
+        iF[1][0] = -F[1][0] / detF;
+        iF[1][1] = F[0][0] / detF;
+        iF[0][2] = iF[1][2] = iF[2][0] = iF[2][1] = 0.0;
+        iF[2][2] = 1.0;
+      } else {
+        detF = det3(F);
+        inv3(F, detF, iF);
+      }
+      NeoHookeOut o;
+      neo_hooke(g.material, props[0], props[1], F, o);
+      const double sig[6] = {o.tau[0][0], o.tau[1][1], o.tau[2][2], o.tau[0][1], o.tau[1][2], o.tau[0][2]};
+      // strain slot = Voigt(E) at the active indices, zero elsewhere (:393, :404)
+      double eps[6] = {Eg[0][0], Eg[1][1], 0.0, 2.0 * Eg[0][1], 0.0, 0.0};
+      if constexpr (DIM == 3) {
+        eps[2] = Eg[2][2];
+        eps[4] = 2.0 * Eg[1][2];
+        eps[5] = 2.0 * Eg[0][2];
+      }
+      const double s = g.geomS[pt];
+      KT* sc = ssc + (le * NQ + q) * NSCAL;
+      sc[0] = (KT)(o.c1 * s);
+      sc[1] = (KT)(o.c4 * s);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          rec[i * 3 + j] = F[i][j];
+          rec[9 + i * 3 + j] = iF[i][j];
+          rec[18 + i * 3 + j] = o.tau[i][j];
+          rec[27 + i * 3 + j] = o.Bm[i][j];
+          reck[i * 3 + j] = (KT)F[i][j];
+          reck[9 + i * 3 + j] = (KT)o.Bm[i][j];
+        }
+      rec[36] = o.c1;
+      rec[37] = o.c2;
+      rec[38] = o.c3;
+      rec[39] = s;
+      reck[18] = (KT)(o.c1 * s);
+      reck[19] = (KT)(o.c2 * s);
+      reck[20] = (KT)(o.c3 * s);
+      // state write (stateTemp = updated copy of stateRef)
+      for (int f = 0; f < 6; ++f) {
+        g.stateTemp[(int64_t)f * stride + pt] = sig[f];
+        g.stateTemp[(int64_t)(6 + f) * stride + pt] = eps[f];
+      }
+      g.stateTemp[(int64_t)12 * stride + pt] = o.energy;
+      bool finite = true;
+      for (int f = 0; f < 6; ++f) finite = finite && isfinite(sig[f]);
+      if (!finite) atomicOr(g.status, EFE_STATUS_NONFINITE);
+    }
+    __syncthreads();
+    // A2: one thread per (point, node): h_a = F^-T dN_a/dX and the residual s tau h_a in FP64
+    // (P_e -= s dN/dX^T F^-1 tau, :402, :414); the tangent's vectors in its own precision
+    for (int t = threadIdx.x; t < EPB * NQ * NN; t += NT) {
+      const int a = t / (EPB * NQ), r = t % (EPB * NQ);
+      const int le = r / NQ, q = r % NQ;
+      const int64_t e = e0 + le;
+      if (e >= nEl) continue;
+      const int64_t pt = e * NQ + q;
+      const double* rec = sx + (le * NQ + q) * L::NX;
+      const KT* reck = sxk + (le * NQ + q) * L::NXK;
+      double G[3] = {0, 0, 0};
+      for (int j = 0; j < DIM; ++j) G[j] = g.geomG[(int64_t)(j * NN + a) * stride + pt];
+      double h[3] = {0, 0, 0};
+      for (int i = 0; i < DIM; ++i)
+        for (int I = 0; I < DIM; ++I) h[i] += G[I] * rec[9 + I * 3 + i];
+      const double s = rec[39];
+      double* rq = sr + (le * NQ + q) * NDOF;
+      double ths[3];
+      for (int j = 0; j < DIM; ++j) {
+        double th = 0.0;
+        for (int i = 0; i < DIM; ++i) th += rec[18 + j * 3 + i] * h[i];
+        ths[j] = th * s;
+        rq[a * DIM + j] = ths[j];
+      }
+      KT Gk[3], hk[3], gg[3], bh[3];
+      for (int j = 0; j < DIM; ++j) {
+        if constexpr (std::is_same<KT, float>::value)
+          Gk[j] = g.geomG32 ? (KT)g.geomG32[(int64_t)(j * NN + a) * stride + pt] : (KT)G[j];
+        else
+          Gk[j] = (KT)G[j];
+        hk[j] = (KT)h[j];
+      }
+      for (int i = 0; i < DIM; ++i) {
+        KT v1 = KT(0), v2 = KT(0);
+        for (int I = 0; I < DIM; ++I) {
+          v1 += reck[i * 3 + I] * Gk[I];      // g_a = F dN_a/dX
+          v2 += reck[9 + i * 3 + I] * hk[I];  // B h_a
+        }
+        gg[i] = v1;
+        bh[i] = v2;
+      }
+      const KT c1s = reck[18], c2s = reck[19], c3s = reck[20];
+      KT* v = sv + ((size_t)(le * NQ + q) * NN + a) * NVEC * DIM;
+      for (int j = 0; j < DIM; ++j) {
+        v[0 * DIM + j] = Gk[j];
+        v[1 * DIM + j] = hk[j];
+        v[2 * DIM + j] = gg[j];
+        v[3 * DIM + j] = c1s * gg[j] - (KT)ths[j];
+        v[4 * DIM + j] = c2s * hk[j] + c3s * bh[j];
+      }
+    }
+  } else {
   for (int t = threadIdx.x; t < EPB * NQ; t += NT) {
     const int le = t / NQ, q = t % NQ;
     const int64_t e = e0 + le;
@@ -414,58 +569,7 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
         detF = det3(F);
         inv3(F, detF, iF);
       }
-      if constexpr (FORM == TLH) {
-        NeoHookeOut o;
-        neo_hooke(g.material, props[0], props[1], F, o);
-        sig[0] = o.tau[0][0];
-        sig[1] = o.tau[1][1];
-        sig[2] = o.tau[2][2];
-        sig[3] = o.tau[0][1];
-        sig[4] = o.tau[1][2];
-        sig[5] = o.tau[0][2];
-        kappa = o.energy;
-        // strain slot = Voigt(E) at the active indices, zero elsewhere (:393, :404)
-        for (int f = 0; f < 6; ++f) eps[f] = 0.0;
-        eps[0] = Eg[0][0];
-        eps[1] = Eg[1][1];
-        if constexpr (DIM == 3) {
-          eps[2] = Eg[2][2];
-          eps[3] = 2.0 * Eg[0][1];
-          eps[4] = 2.0 * Eg[1][2];
-          eps[5] = 2.0 * Eg[0][2];
-        } else {
-          eps[3] = 2.0 * Eg[0][1];
-        }
-        sc[0] = (KT)(o.c1 * s);
-        sc[1] = (KT)(o.c4 * s);
-        for (int a = 0; a < NN; ++a) {
-          double h[3] = {0, 0, 0}, gg[3] = {0, 0, 0};
-          for (int i = 0; i < DIM; ++i)
-            for (int I = 0; I < DIM; ++I) {
-              h[i] += Gm[I][a] * iF[I][i];  // h_a = F^-T dN_a/dX  (NAi, :391)
-              gg[i] += F[i][I] * Gm[I][a];  // g_a = F dN_a/dX
-            }
-          double th[3], bh[3];
-          for (int j = 0; j < DIM; ++j) {
-            th[j] = 0.0;
-            bh[j] = 0.0;
-            for (int i = 0; i < DIM; ++i) {
-              th[j] += o.tau[j][i] * h[i];
-              bh[j] += o.Bm[j][i] * h[i];
-            }
-          }
-          // P_e -= s * (dN/dX^T F^-1 tau) = s * tau h_a  (:402, :414)
-          for (int j = 0; j < DIM; ++j) rq[a * DIM + j] = th[j] * s;
-          KT* v = vq + a * NVEC * DIM;
-          for (int j = 0; j < DIM; ++j) {
-            v[0 * DIM + j] = (KT)Gm[j][a];
-            v[1 * DIM + j] = (KT)h[j];
-            v[2 * DIM + j] = (KT)gg[j];
-            v[3 * DIM + j] = (KT)((o.c1 * gg[j] - th[j]) * s);
-            v[4 * DIM + j] = (KT)((o.c2 * h[j] + o.c3 * bh[j]) * s);
-          }
-        }
-      } else {
+      {
         // hypoelastic material on the Green-Lagrange strain increment (:416-426)
         double de[6] = {0, 0, 0, 0, 0, 0};
         const double* Eo = g.auxRef;
@@ -564,6 +668,7 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
     for (int f = 0; f < 6; ++f) finite = finite && isfinite(sig[f]);
     if (!ok) report(g.status, EFE_STATUS_CUTBACK, g.elementOffset + e, 1);
     if (!finite) atomicOr(g.status, EFE_STATUS_NONFINITE);
+  }
   }
   __syncthreads();
 
