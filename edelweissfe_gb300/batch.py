@@ -18,11 +18,36 @@ from . import _lib as L
 from .assembly import ElementGroup, GPUAssembler
 
 
+def chunk_meshes(meshes, elType, limit=2**31 - 1):
+    """Split a list of meshes of one element type into consecutive chunks whose CSR patterns fit the
+    int32 indexing of one batch: every element contributes at most (nodes x dim)^2 entries, so a
+    chunk holds at most limit / (nodes x dim)^2 elements."""
+    from .library import element_type
+
+    et = element_type(elType)
+    per = (et.nNodes * et.dim) ** 2
+    cap = max(1, limit // per)
+    chunks, cur, n = [], [], 0
+    for m in meshes:
+        e = len(m["conn"])
+        if e > cap:
+            raise ValueError(f"a single mesh of {e} elements exceeds the int32 CSR of one batch")
+        if cur and n + e > cap:
+            chunks.append(cur)
+            cur, n = [], 0
+        cur.append(m)
+        n += e
+    if cur:
+        chunks.append(cur)
+    return chunks
+
+
 class MeshBatch:
     """meshes: list of dicts with coords [n, d], conn [E, nN], nodeDof [n], nDof, props [nP] or [E, nP],
-    thickness (2D); all of one element type and material."""
+    thickness (2D); all of one element type and material.  keep_host_pattern=False drops the host
+    copies of the CSR indices and slot maps once they are on the device (large batches)."""
 
-    def __init__(self, meshes, elType, material, precision="mixed", device=None):
+    def __init__(self, meshes, elType, material, precision="mixed", device=None, keep_host_pattern=True):
         node_off = np.cumsum([0] + [len(m["coords"]) for m in meshes])
         dof_off = np.cumsum([0] + [int(m["nDof"]) for m in meshes])
         el_off = np.cumsum([0] + [len(m["conn"]) for m in meshes])
@@ -42,6 +67,10 @@ class MeshBatch:
         self.element_offsets = el_off
         ip = self.asm.indptr_host
         self.nnz_offsets = np.array([ip[d] for d in dof_off])
+        if not keep_host_pattern:
+            self.asm.indices_host = None
+            self.asm._slots_host = None
+            self.asm._conns_host = None
         self.nElements = int(el_off[-1])
         self.U = self.asm.constructDofVector()
         self.dU = self.asm.constructDofVector()
