@@ -171,6 +171,7 @@ efe::GroupArgs make_args(const EfeMesh* mesh, const EfeGroup& gr, const double* 
 }
 
 int32_t check_item_buffers(const EfeGroup& gr, const double* U, const double* dU) {
+  if (gr.nElements == 0) return EFE_OK;  // an empty group touches no buffer
   const bool tl = gr.kinematics == EFE_TOTAL_LAGRANGIAN;
   if (!gr.conn || !gr.pairSlot || !gr.props || !gr.geomG || !gr.geomS || !gr.stateRef || !gr.stateTemp)
     return fail(EFE_ERR_ARGUMENT, "null group buffer");
@@ -252,6 +253,7 @@ int32_t efe_setup_geometry(const EfeMesh* mesh, const EfeGroup* g, int32_t* stat
   if (!mesh || !g || !status) return fail(EFE_ERR_ARGUMENT, "null argument");
   int32_t rc = check_group(mesh, *g);
   if (rc) return rc;
+  if (g->nElements == 0) return EFE_OK;
   if (!g->geomG || !g->geomS || !g->conn || !mesh->coords) return fail(EFE_ERR_ARGUMENT, "null geometry buffer");
   if (mesh->dim == 2 && !g->thickness) return fail(EFE_ERR_ARGUMENT, "2D elements need a thickness array");
   static const efe::Hexa20Fix fix = hexa20_fix();
@@ -284,7 +286,8 @@ int32_t efe_compute_elements(const EfeMesh* mesh, const EfeGroup* groups, int32_
                              double* P, double* F, int32_t* status, void* stream) {
   (void)time2;
   (void)dT;
-  if (!mesh || !groups || nGroups < 0 || !Kdata || !P || !F || !status)
+  // a model without elements has an empty pattern: K may then be a null pointer
+  if (!mesh || !groups || nGroups < 0 || (!Kdata && mesh->nnz > 0) || !P || !F || !status)
     return fail(EFE_ERR_ARGUMENT, "null argument");
   if (kPrecision != EFE_K_FP64 && kPrecision != EFE_K_FP32 && kPrecision != EFE_K_FP32_FF)
     return fail(EFE_ERR_ARGUMENT, "unknown K precision");
@@ -322,6 +325,7 @@ int32_t efe_body_force(const EfeMesh* mesh, const EfeGroup* g, const int32_t* el
   int32_t rc = check_group(mesh, *g);
   if (rc) return rc;
   if (!elements) nSelected = g->nElements;
+  if (nSelected == 0) return EFE_OK;
   if (!g->geomS || !g->conn || !mesh->nodeDof) return fail(EFE_ERR_ARGUMENT, "group without geometry");
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e = cudaErrorInvalidValue;
@@ -342,6 +346,7 @@ int32_t efe_adjoint_tl(const EfeMesh* mesh, const EfeGroup* g, const double* U, 
   if (rc) return rc;
   if (g->kinematics != EFE_TOTAL_LAGRANGIAN || !hyperelastic(g->material))
     return fail(EFE_ERR_UNSUPPORTED, "the adjoint covers total-Lagrangian Neo-Hooke groups");
+  if (g->nElements == 0) return EFE_OK;
   if (!mesh->coords || !mesh->nodeDof || !g->conn || !g->props) return fail(EFE_ERR_ARGUMENT, "null group buffer");
   if (mesh->dim == 2 && !g->thickness) return fail(EFE_ERR_ARGUMENT, "2D elements need a thickness array");
   static const efe::Hexa20Fix fix = hexa20_fix();
@@ -371,6 +376,7 @@ int32_t efe_adjoint_small_strain(const EfeMesh* mesh, const EfeGroup* g, const d
     return fail(EFE_ERR_UNSUPPORTED, "efe_adjoint_small_strain covers linear elastic and von Mises groups");
   if (mesh->dim == 2 && g->plane != EFE_PLANE_STRAIN)
     return fail(EFE_ERR_UNSUPPORTED, "efe_adjoint_small_strain covers solids and plane strain");
+  if (g->nElements == 0) return EFE_OK;
   if (!mesh->nodeDof || !g->conn || !g->props || !g->geomG || !g->geomS)
     return fail(EFE_ERR_ARGUMENT, "null group buffer (has efe_setup_geometry run?)");
   efe::SSAdjointArgs a;
