@@ -712,7 +712,8 @@ def run_plastic(args):
     print(json.dumps({
         "metric": "adjoint grads/s (dJ/d(fy0, H) per element through the plastic path), excluding the adjoint solves",
         "value": 1e3 / timing["kernel_ms"], "unit": "grad/s", "higher_is_better": True,
-        "dtype": "f64 residual/state/return map + f32 tangent (mixed); f64 reverse passes", "data": "synthetic",
+        "dtype": "f64 residual/state/return map + f32 tangent (mixed); reverse passes: f64 return map, "
+                 "float-float B-products", "data": "synthetic",
         "config": {"workload": f"C3D20 von Mises J2 {n}x{n}x{max(1, n // 2)} on [0,2]x[0,2]x[0,1], per-element "
                                "fy0 ~ U[200,300], H ~ U[800,1200], 10 uniaxial increments to 0.5% strain; "
                                "J = total top reaction", "elements": len(conn), "dofs": nDof, "nnz": int(asm.nnz)},

@@ -141,7 +141,9 @@ class GPUAssembler:
         d["geomG"] = torch.zeros((et.dim * et.nNodes, nPts), dtype=torch.float64, device=dev)
         if self.kPrecision in (L.EFE_K_FP32, L.EFE_K_FP32_FF):
             d["geomG32"] = torch.zeros((et.dim * et.nNodes, nPts), dtype=torch.float32, device=dev)
-        if self.kPrecision == L.EFE_K_FP32_FF:
+        if self.kPrecision in (L.EFE_K_FP32, L.EFE_K_FP32_FF):
+            # float-float form of dN/dX (with geomG32): read by the mixed-ff pass and by the reverse
+            # small-strain pass, which forms its B-products on the FP32 pipe when it is present
             d["geomGlo"] = torch.zeros((et.dim * et.nNodes, nPts), dtype=torch.float32, device=dev)
         d["geomS"] = torch.zeros(nPts, dtype=torch.float64, device=dev)
         d["stateRef"] = torch.zeros((S, nPts), dtype=torch.float64, device=dev)

@@ -387,6 +387,8 @@ int32_t efe_adjoint_small_strain(const EfeMesh* mesh, const EfeGroup* g, const d
   a.nodeDof = mesh->nodeDof;
   a.props = g->props;
   a.geomG = g->geomG;
+  a.geomG32 = g->geomG32;
+  a.geomGlo = g->geomGlo;
   a.geomS = g->geomS;
   a.stateBefore = stateBefore;
   a.dU = dU;

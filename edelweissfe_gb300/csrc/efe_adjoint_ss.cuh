@@ -122,7 +122,10 @@ struct SSAdjointTile {
                           bytes = g_off + sizeof(double) * EPB * NQ * 6;
 };
 
-template <int SHAPE, int RULE>
+// FF: the three B-products (B dU, B PBar, B^T deBar) in float-float arithmetic on the FP32 pipe from the
+// float-float geometry (geomG32 + geomGlo), with nodal values taken relative to the element's first
+// node (sum_a dN_a/dX = 0); the reverse return map stays FP64.  ~2^-48 relative accuracy.
+template <int SHAPE, int RULE, bool FF>
 __global__ void __launch_bounds__(SSAdjointTile<SHAPE, RULE>::NT) adjoint_ss_kernel(SSAdjointArgs a) {
   using T = SSAdjointTile<SHAPE, RULE>;
   constexpr int DIM = T::DIM, NN = T::NN, NQ = T::NQ, NDOF = T::NDOF, EPB = T::EPB, NT = T::NT;
@@ -141,9 +144,19 @@ __global__ void __launch_bounds__(SSAdjointTile<SHAPE, RULE>::NT) adjoint_ss_ker
     const int64_t e = e0 + le;
     if (e >= nEl) continue;
     const int32_t dof = a.nodeDof[a.conn[e * NN + n]];
-    for (int c = 0; c < DIM; ++c) {
-      su[le * NDOF + n * DIM + c] = a.dU[dof + c];
-      sp[le * NDOF + n * DIM + c] = a.Pbar ? a.Pbar[dof + c] : 0.0;
+    if constexpr (FF) {
+      const int32_t dof0 = a.nodeDof[a.conn[e * NN]];
+      ff* uf = reinterpret_cast<ff*>(su);
+      ff* pf = reinterpret_cast<ff*>(sp);
+      for (int c = 0; c < DIM; ++c) {
+        uf[le * NDOF + n * DIM + c] = ff_split(a.dU[dof + c] - a.dU[dof0 + c]);
+        pf[le * NDOF + n * DIM + c] = ff_split(a.Pbar ? a.Pbar[dof + c] - a.Pbar[dof0 + c] : 0.0);
+      }
+    } else {
+      for (int c = 0; c < DIM; ++c) {
+        su[le * NDOF + n * DIM + c] = a.dU[dof + c];
+        sp[le * NDOF + n * DIM + c] = a.Pbar ? a.Pbar[dof + c] : 0.0;
+      }
     }
   }
   __syncthreads();
@@ -157,37 +170,85 @@ __global__ void __launch_bounds__(SSAdjointTile<SHAPE, RULE>::NT) adjoint_ss_ker
     // G is read where it is used (twice) rather than held across the return map: fewer registers
     const double* Gp = a.geomG + pt;
     const double s = a.geomS[pt];
-    const double* u = su + le * NDOF;
-    const double* pb = sp + le * NDOF;
     // B u and B PBar (small-strain Voigt 11,22,33,12,13,23, engineering shear)
     double de[6] = {0, 0, 0, 0, 0, 0}, bp[6] = {0, 0, 0, 0, 0, 0};
-    for (int n = 0; n < NN; ++n) {
-      const double gx = Gp[(int64_t)n * stride], gy = Gp[(int64_t)(NN + n) * stride];
-      if constexpr (DIM == 3) {
-        const double gz = Gp[(int64_t)(2 * NN + n) * stride];
-        const double ux = u[n * 3], uy = u[n * 3 + 1], uz = u[n * 3 + 2];
-        const double px = pb[n * 3], py = pb[n * 3 + 1], pz = pb[n * 3 + 2];
-        de[0] = fma(gx, ux, de[0]);
-        de[1] = fma(gy, uy, de[1]);
-        de[2] = fma(gz, uz, de[2]);
-        de[3] = fma(gx, uy, fma(gy, ux, de[3]));
-        de[4] = fma(gx, uz, fma(gz, ux, de[4]));
-        de[5] = fma(gy, uz, fma(gz, uy, de[5]));
-        bp[0] += gx * px;
-        bp[1] += gy * py;
-        bp[2] += gz * pz;
-        bp[3] += gy * px + gx * py;
-        bp[4] += gz * px + gx * pz;
-        bp[5] += gz * py + gy * pz;
-      } else {
-        const double ux = u[n * 2], uy = u[n * 2 + 1];
-        const double px = pb[n * 2], py = pb[n * 2 + 1];
-        de[0] += gx * ux;
-        de[1] += gy * uy;
-        de[3] += gy * ux + gx * uy;
-        bp[0] += gx * px;
-        bp[1] += gy * py;
-        bp[3] += gy * px + gx * py;
+    if constexpr (FF) {
+      const ff* uf = reinterpret_cast<const ff*>(su) + le * NDOF;
+      const ff* pf = reinterpret_cast<const ff*>(sp) + le * NDOF;
+      ff ad[6] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}}, ab[6] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}};
+      for (int n = 0; n < NN; ++n) {
+        const ff gx = ff{a.geomG32[(int64_t)n * stride + pt], a.geomGlo[(int64_t)n * stride + pt]};
+        const ff gy = ff{a.geomG32[(int64_t)(NN + n) * stride + pt], a.geomGlo[(int64_t)(NN + n) * stride + pt]};
+        if constexpr (DIM == 3) {
+          const ff gz = ff{a.geomG32[(int64_t)(2 * NN + n) * stride + pt], a.geomGlo[(int64_t)(2 * NN + n) * stride + pt]};
+          const ff ux = uf[n * 3], uy = uf[n * 3 + 1], uz = uf[n * 3 + 2];
+          const ff px = pf[n * 3], py = pf[n * 3 + 1], pz = pf[n * 3 + 2];
+          ff_fma(ad[0], gx, ux);
+          ff_fma(ad[1], gy, uy);
+          ff_fma(ad[2], gz, uz);
+          ff_fma(ad[3], gy, ux);
+          ff_fma(ad[3], gx, uy);
+          ff_fma(ad[4], gz, ux);
+          ff_fma(ad[4], gx, uz);
+          ff_fma(ad[5], gz, uy);
+          ff_fma(ad[5], gy, uz);
+          ff_fma(ab[0], gx, px);
+          ff_fma(ab[1], gy, py);
+          ff_fma(ab[2], gz, pz);
+          ff_fma(ab[3], gy, px);
+          ff_fma(ab[3], gx, py);
+          ff_fma(ab[4], gz, px);
+          ff_fma(ab[4], gx, pz);
+          ff_fma(ab[5], gz, py);
+          ff_fma(ab[5], gy, pz);
+        } else {
+          const ff ux = uf[n * 2], uy = uf[n * 2 + 1];
+          const ff px = pf[n * 2], py = pf[n * 2 + 1];
+          ff_fma(ad[0], gx, ux);
+          ff_fma(ad[1], gy, uy);
+          ff_fma(ad[3], gy, ux);
+          ff_fma(ad[3], gx, uy);
+          ff_fma(ab[0], gx, px);
+          ff_fma(ab[1], gy, py);
+          ff_fma(ab[3], gy, px);
+          ff_fma(ab[3], gx, py);
+        }
+      }
+      for (int f = 0; f < 6; ++f) {
+        de[f] = ff_to_double(ad[f]);
+        bp[f] = ff_to_double(ab[f]);
+      }
+    } else {
+      const double* u = su + le * NDOF;
+      const double* pb = sp + le * NDOF;
+      for (int n = 0; n < NN; ++n) {
+        const double gx = Gp[(int64_t)n * stride], gy = Gp[(int64_t)(NN + n) * stride];
+        if constexpr (DIM == 3) {
+          const double gz = Gp[(int64_t)(2 * NN + n) * stride];
+          const double ux = u[n * 3], uy = u[n * 3 + 1], uz = u[n * 3 + 2];
+          const double px = pb[n * 3], py = pb[n * 3 + 1], pz = pb[n * 3 + 2];
+          de[0] = fma(gx, ux, de[0]);
+          de[1] = fma(gy, uy, de[1]);
+          de[2] = fma(gz, uz, de[2]);
+          de[3] = fma(gx, uy, fma(gy, ux, de[3]));
+          de[4] = fma(gx, uz, fma(gz, ux, de[4]));
+          de[5] = fma(gy, uz, fma(gz, uy, de[5]));
+          bp[0] += gx * px;
+          bp[1] += gy * py;
+          bp[2] += gz * pz;
+          bp[3] += gy * px + gx * py;
+          bp[4] += gz * px + gx * pz;
+          bp[5] += gz * py + gy * pz;
+        } else {
+          const double ux = u[n * 2], uy = u[n * 2 + 1];
+          const double px = pb[n * 2], py = pb[n * 2 + 1];
+          de[0] += gx * ux;
+          de[1] += gy * uy;
+          de[3] += gy * ux + gx * uy;
+          bp[0] += gx * px;
+          bp[1] += gy * py;
+          bp[3] += gy * px + gx * py;
+        }
       }
     }
     // seeds: the new state's adjoint, plus P_e = -sum_q s B^T sig  =>  sigBar -= s B PBar
@@ -217,16 +278,50 @@ __global__ void __launch_bounds__(SSAdjointTile<SHAPE, RULE>::NT) adjoint_ss_ker
     for (int k = 0; k < 6; ++k) gq[k] = pBar[k];
     // dU_e contribution B^T deBar
     double* rq = sr + (le * NQ + q) * NDOF;
-    for (int n = 0; n < NN; ++n) {
-      const double gx = Gp[(int64_t)n * stride], gy = Gp[(int64_t)(NN + n) * stride];
-      if constexpr (DIM == 3) {
-        const double gz = Gp[(int64_t)(2 * NN + n) * stride];
-        rq[n * 3 + 0] = deBar[0] * gx + deBar[3] * gy + deBar[4] * gz;
-        rq[n * 3 + 1] = deBar[3] * gx + deBar[1] * gy + deBar[5] * gz;
-        rq[n * 3 + 2] = deBar[4] * gx + deBar[5] * gy + deBar[2] * gz;
-      } else {
-        rq[n * 2 + 0] = deBar[0] * gx + deBar[3] * gy;
-        rq[n * 2 + 1] = deBar[3] * gx + deBar[1] * gy;
+    if constexpr (FF) {
+      ff db[6];
+      for (int f = 0; f < 6; ++f) db[f] = ff_split(deBar[f]);
+      ff* rf = reinterpret_cast<ff*>(rq);
+      for (int n = 0; n < NN; ++n) {
+        const ff gx = ff{a.geomG32[(int64_t)n * stride + pt], a.geomGlo[(int64_t)n * stride + pt]};
+        const ff gy = ff{a.geomG32[(int64_t)(NN + n) * stride + pt], a.geomGlo[(int64_t)(NN + n) * stride + pt]};
+        if constexpr (DIM == 3) {
+          const ff gz = ff{a.geomG32[(int64_t)(2 * NN + n) * stride + pt], a.geomGlo[(int64_t)(2 * NN + n) * stride + pt]};
+          ff r0{0, 0}, r1{0, 0}, r2{0, 0};
+          ff_fma(r0, db[0], gx);
+          ff_fma(r0, db[3], gy);
+          ff_fma(r0, db[4], gz);
+          ff_fma(r1, db[3], gx);
+          ff_fma(r1, db[1], gy);
+          ff_fma(r1, db[5], gz);
+          ff_fma(r2, db[4], gx);
+          ff_fma(r2, db[5], gy);
+          ff_fma(r2, db[2], gz);
+          rf[n * 3 + 0] = r0;
+          rf[n * 3 + 1] = r1;
+          rf[n * 3 + 2] = r2;
+        } else {
+          ff r0{0, 0}, r1{0, 0};
+          ff_fma(r0, db[0], gx);
+          ff_fma(r0, db[3], gy);
+          ff_fma(r1, db[3], gx);
+          ff_fma(r1, db[1], gy);
+          rf[n * 2 + 0] = r0;
+          rf[n * 2 + 1] = r1;
+        }
+      }
+    } else {
+      for (int n = 0; n < NN; ++n) {
+        const double gx = Gp[(int64_t)n * stride], gy = Gp[(int64_t)(NN + n) * stride];
+        if constexpr (DIM == 3) {
+          const double gz = Gp[(int64_t)(2 * NN + n) * stride];
+          rq[n * 3 + 0] = deBar[0] * gx + deBar[3] * gy + deBar[4] * gz;
+          rq[n * 3 + 1] = deBar[3] * gx + deBar[1] * gy + deBar[5] * gz;
+          rq[n * 3 + 2] = deBar[4] * gx + deBar[5] * gy + deBar[2] * gz;
+        } else {
+          rq[n * 2 + 0] = deBar[0] * gx + deBar[3] * gy;
+          rq[n * 2 + 1] = deBar[3] * gx + deBar[1] * gy;
+        }
       }
     }
   }
@@ -238,7 +333,14 @@ __global__ void __launch_bounds__(SSAdjointTile<SHAPE, RULE>::NT) adjoint_ss_ker
     const int64_t e = e0 + le;
     if (e >= nEl) continue;
     double v = 0.0;
-    for (int q = 0; q < NQ; ++q) v += sr[(le * NQ + q) * NDOF + k];
+    if constexpr (FF) {
+      const ff* rf = reinterpret_cast<const ff*>(sr);
+      ff acc{0, 0};
+      for (int q = 0; q < NQ; ++q) ff_add(acc, rf[(le * NQ + q) * NDOF + k]);
+      v = ff_to_double(acc);
+    } else {
+      for (int q = 0; q < NQ; ++q) v += sr[(le * NQ + q) * NDOF + k];
+    }
     const int32_t dof = a.nodeDof[a.conn[e * NN + k / DIM]] + k % DIM;
     atomicAdd(a.dUbar + dof, v);
   }
@@ -259,7 +361,7 @@ template <int SHAPE, int RULE>
 cudaError_t launch_adjoint_ss(const SSAdjointArgs& a, cudaStream_t st) {
   using T = SSAdjointTile<SHAPE, RULE>;
   if (a.nEl == 0) return cudaSuccess;
-  auto kern = adjoint_ss_kernel<SHAPE, RULE>;
+  auto kern = (a.geomG32 && a.geomGlo) ? adjoint_ss_kernel<SHAPE, RULE, true> : adjoint_ss_kernel<SHAPE, RULE, false>;
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::bytes);
   if (err != cudaSuccess) return err;
   const int64_t blocks = (a.nEl + T::EPB - 1) / T::EPB;

@@ -91,6 +91,8 @@ struct SSAdjointArgs {
   const int32_t* nodeDof;
   const double* props;
   const double* geomG;
+  const float* geomG32;       // optional: with geomGlo the float-float geometry (B-products on the FP32 pipe)
+  const float* geomGlo;
   const double* geomS;
   const double* stateBefore;  // [S][nPts]
   const double* dU;           // [nDof]

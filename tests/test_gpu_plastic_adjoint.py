@@ -4,7 +4,8 @@ over plastic load increments (PathAdjoint), in FP64, against central differences
 1. One increment: L = sum(sbar * s_new) + pbar . P of one element pass from a plastic state s0
    with increment dU (von Mises with saturation hardening, and linear elasticity); directional
    derivatives of L in dU, in the state s0 and in the six material properties, h = 1e-7 relative;
-   agreement to 1e-6 relative.
+   agreement to 1e-6 relative.  Both forms of the reverse pass: FP64 B-products (FP64 assembler)
+   and float-float B-products (mixed assembler, which carries the float-float geometry).
 2. The plastic path: C3D20 (3x3x3 Gauss) von Mises cube, 2x2x2 elements with per-element yield
    stress U[200, 300] and hardening U[800, 1200]; bottom u_y = 0, left u_x = 0, back u_z = 0, top
    u_y -> 0.5 % in 4 increments; J = the total top reaction.  dJ/d(fy0, H) by the path adjoint vs
@@ -19,7 +20,7 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 
-def _model(elType, material, seed):
+def _model(elType, material, seed, precision="fp64"):
     from edelweissfe_gb300 import ElementGroup, GPUAssembler, meshes
 
     rng = np.random.default_rng(seed)
@@ -36,7 +37,7 @@ def _model(elType, material, seed):
                           rng.uniform(800, 1200, E), rng.uniform(20, 80, E), rng.uniform(5, 20, E)], 1)  # fmt: skip
     else:
         props = np.stack([rng.uniform(190e3, 230e3, E), rng.uniform(0.25, 0.35, E)], 1)
-    asm = GPUAssembler(coords, nodeDof, nDof, [ElementGroup(elType, material, props, conn, 1.0)])
+    asm = GPUAssembler(coords, nodeDof, nDof, [ElementGroup(elType, material, props, conn, 1.0)], precision=precision)
     return asm, coords, nodeDof, nDof, props
 
 
@@ -50,10 +51,11 @@ def _uniaxial(coords, nodeDof, nDof, strain):
     return U
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])  # mixed: B-products in float-float arithmetic
 @pytest.mark.parametrize("elType,material", [("C3D8", "vonmises"), ("C3D20", "vonmises"), ("C3D20R", "vonmises"),
                                              ("CPE8", "vonmises"), ("CPE4", "vonmises"), ("C3D8", "linearelastic")])
-def test_increment_reverse_matches_finite_differences(elType, material):
-    asm, coords, nodeDof, nDof, props = _model(elType, material, 5)
+def test_increment_reverse_matches_finite_differences(elType, material, precision):
+    asm, coords, nodeDof, nDof, props = _model(elType, material, 5, precision)
     dev = asm.device
     rng = np.random.default_rng(6)
     g = asm.groups[0]._dev
