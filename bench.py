@@ -132,6 +132,49 @@ def ncu_traffic(name):
     return None
 
 
+# ------------------------------------------------------------------ shared measurement helpers
+def bytes_per_pass(nEl, nQ, nState, nNodes, nDof, nnz, kbytes, nn, dim, state_read=True, n_props=0):
+    """Algorithmic bytes of one element pass (unique inputs read once, outputs written once):
+    QP history (read and written; written only for hyperelastic states), connectivity, nodal
+    coordinates, the displacement vector, per-element properties, K values, R and F."""
+    hist = nEl * nQ * nState * 8 * (2 if state_read else 1)
+    return hist + nEl * nn * 4 + nNodes * dim * 8 + nDof * 8 + nEl * n_props * 8 + nnz * kbytes + 2 * nDof * 8
+
+
+def roofline_hbm(abytes, kernel_ms, traffic=None):
+    peak, kind = peaks()
+    achieved = abytes / (kernel_ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic, "peak_kind": kind, "algorithmic_bytes_per_launch": abytes, "kernel_ms": kernel_ms}
+
+
+def oracle_rate(elType, kind, props, n_side, disp, seed=0, reps=2):
+    """Elements per second of the oracle port (the reference's element/material/assembly algorithm)
+    on one core for a small n_side^3 (3D) or n_side^2 (2D) block of elType with nodal displacements
+    `disp` x N(0, 1) (TL elements: total U; small strain: the increment); `disp` is chosen per call
+    as about 1 % of the element size (1.2 % strain, plastic, for the von Mises sample)."""
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    from edelweissfe_gb300 import meshes
+    from edelweissfe_gb300.library import element_type
+    from oracle.assembly import Model
+
+    et = element_type(elType)
+    if et.dim == 3:
+        coords, conn, nodeDof, nDof = meshes.box(n_side, n_side, n_side, nNodes=et.nNodes)
+    else:
+        coords, conn, nodeDof, nDof = meshes.rect(n_side, n_side, nNodes=et.nNodes)
+    U = np.random.default_rng(seed).normal(0, disp, nDof)
+    g = dict(elType=elType, kind=kind, props=np.tile(props, (len(conn), 1)), conn=conn.astype(np.int64),
+             thickness=np.ones(len(conn)), order=np.arange(len(conn)))  # fmt: skip
+    m = Model(coords, nodeDof, nDof, [g])
+    st = m.initial_state()
+    t = time.perf_counter()
+    for _ in range(reps):
+        m.compute_elements(U, U, st)
+    secs = time.perf_counter() - t
+    return len(conn) * reps / secs, len(conn) * reps, secs
+
+
 # ------------------------------------------------------------------ GPU arm
 def run_gpu(args, rank, world):
     import torch
@@ -400,6 +443,17 @@ def run_batched(args):
     ms = a.elapsed_time(b) / args.steps
     nEl = sum(b.nElements for b in batches)
     n2 = sum(b.nElements for b in batches if b.asm.dim == 2)
+    abytes = sum(bytes_per_pass(b.nElements, b.asm.groups[0]._dev["type"].nInt, 13, b.asm.nNodes, b.asm.nDof,
+                                b.asm.nnz, 4, b.asm.groups[0]._dev["type"].nNodes, b.asm.dim, state_read=False,
+                                n_props=2) for b in batches)  # fmt: skip
+    cpu = None
+    if not args.no_cpu_baseline:
+        r20, d20, s20 = oracle_rate("C3D20TL", "neohookewa", [1000.0, 10000.0], 3, 0.003, reps=10)
+        r8, d8, s8 = oracle_rate("CPE8RTL", "neohookewa", [1000.0, 10000.0], 16, 0.0006, reps=40)
+        rate = nEl / ((nEl - n2) / r20 + n2 / r8)
+        cpu = {"value": rate, "unit": "elem/s", "cores": 1, "kind": "port",
+               "sample": f"oracle port: {d20} C3D20TL evaluations ({s20:.1f} s) and {d8} CPE8RTL evaluations "
+                         f"({s8:.1f} s), combined in the batch's element mix"}  # fmt: skip
     print(json.dumps({
         "metric": "assembled elem/s (K+R), batched uneven meshes, one CUDA graph (persistent or per-batch launches, "
                   "autotuned)",
@@ -410,6 +464,7 @@ def run_batched(args):
                    "elements_quad8": n2, "elements_hexa20": nEl - n2, "meshes_2d": len(m2),
                    "meshes_3d": len(m3), "batches": len(batches), "nnz": int(sum(b.asm.nnz for b in batches)),
                    "setup_s": setup_s},
+        "roofline": roofline_hbm(abytes, ms), "cpu_baseline": cpu,
         "launch": "persistent" if bp.persistent else "per-batch",
         "tuning": {"persistent_ms": tuning.get(True), "per_batch_ms": tuning.get(False),
                    "tile_variants": [(k, v, best) for k, v, best in tuner.log if k != "persistent"]},
@@ -581,6 +636,14 @@ def run_adjoint(args):
             ad = float((gE * dE).sum() + (gX * dX).sum())
             errs.append(abs(ad - fd) / abs(fd))
     nEl = len(conn)
+    # adjoint kernel algorithmic bytes: read U, lambda (DOF vectors), X, (mu, K); write dX, d(mu, K)
+    adj_bytes = 2 * nDof * 8 + 2 * len(coords) * 3 * 8 + nEl * 2 * 8 * 2 + nEl * 8 * 4
+    cpu = None
+    if not args.no_cpu_baseline:
+        r, d, secs = oracle_rate("C3D8TL", "neohookewa", [400.0, 800.0], 8, 0.001, reps=10)
+        cpu = {"value": r, "unit": "elem/s", "cores": 1, "kind": "port",
+               "sample": f"oracle port forward element pass (the reference has no derivatives): {d} C3D8TL "
+                         f"Neo-Hooke evaluations in {secs:.1f} s"}  # fmt: skip
     print(json.dumps({
         "metric": "adjoint grads/s (dJ/dE per element + dJ/dX), excluding the adjoint linear solve",
         "value": 1e3 / ms, "unit": "grad/s", "ms_per_step": ms, "steps": args.steps, "warmup": args.warmup,
@@ -594,6 +657,7 @@ def run_adjoint(args):
         "forward_newton_s": forward_s, "forward_newton_iterations": newton, "autograd_backward_s": backward_s,
         "fd_check": {"directions": args.fd_directions, "h": 1e-6, "max_rel_err": max(errs) if errs else None,
                      "median_rel_err": float(np.median(errs)) if errs else None},
+        "roofline": roofline_hbm(adj_bytes, adjoint_ms), "cpu_baseline": cpu,
         "gpu_launches": 2 * args.steps,
     }))
 
@@ -709,6 +773,17 @@ def run_plastic(args):
             errs.append(abs(ad - f) / abs(f))
         fd = {"directions": args.plastic_fd, "h": 1e-6, "max_rel_err": max(errs), "errors": errs}
     nInc = len(adj.checkpoints)
+    # backward element work per increment: one element pass (the tangent) and two reverse passes,
+    # each reading the checkpointed history, the reverse passes also the state adjoint (read + write)
+    nQ = 27
+    fwd = bytes_per_pass(len(conn), nQ, 13, len(coords), nDof, asm.nnz, 4, 20, 3, n_props=6)
+    rev = len(conn) * nQ * 13 * 8 * 4 + len(conn) * 20 * 4 + 3 * nDof * 8 + len(conn) * 6 * 8 * 2
+    cpu = None
+    if not args.no_cpu_baseline:
+        r, d, secs = oracle_rate("C3D20", "vonmises", VM, 3, 0.004, reps=15)
+        cpu = {"value": r, "unit": "elem/s", "cores": 1, "kind": "port",
+               "sample": f"oracle port forward element pass (the reference has no derivatives): {d} C3D20 von Mises "
+                         f"evaluations in {secs:.1f} s"}  # fmt: skip
     print(json.dumps({
         "metric": "adjoint grads/s (dJ/d(fy0, H) per element through the plastic path), excluding the adjoint solves",
         "value": 1e3 / timing["kernel_ms"], "unit": "grad/s", "higher_is_better": True,
@@ -725,6 +800,7 @@ def run_plastic(args):
         "grad_norm": {"fy0": float(np.linalg.norm(gy)), "H": float(np.linalg.norm(gH))},
         "element_pass": passes, "mixed_over_fp64": passes["fp64"]["ms"] / passes["mixed"]["ms"],
         "setup_s": setup_s, "fd_check": fd,
+        "roofline": roofline_hbm(nInc * (fwd + 2 * rev), timing["kernel_ms"]), "cpu_baseline": cpu,
         "gpu_launches": 3 * nInc,
     }))
 
