@@ -258,39 +258,75 @@ def run_gpu(args, rank, world):
 
 
 def run_e2e(asm, U_host, dU_host, args, dev):
-    """The same pass through the public API with host buffers: pinned H2D of U and dU, the pass,
-    D2H of P, F and K, all inside the timed region (wall clock, synchronised)."""
+    """The same pass through the public API with host buffers, every step moving its own data: pinned
+    H2D of U and dU, zeroing, the element pass (GPUAssembler.launch), D2H of P, F, K and the status
+    word, all inside the timed region (wall clock, synchronised at both ends).  Steps are pipelined
+    over three streams with double-buffered device and host buffers: the read-back of step k
+    overlaps the pass of step k+1; step k+2 reuses step k's buffers only after their copies are
+    done.  Every step's status is checked after the loop (CutbackRequest as computeElements)."""
     import torch
 
     Uh = torch.tensor(U_host).pin_memory()
     dUh = torch.tensor(dU_host).pin_memory()
-    U, dU = asm.constructDofVector(), asm.constructDofVector()
-    P, F, K = asm.constructDofVector(), asm.constructDofVector(), asm.constructSystemMatrix()
-    Ph = torch.empty_like(P, device="cpu").pin_memory()
-    Fh = torch.empty_like(F, device="cpu").pin_memory()
-    Kh = torch.empty_like(K, device="cpu").pin_memory()
+    nb = 2
+    U = [asm.constructDofVector() for _ in range(nb)]
+    dU = [asm.constructDofVector() for _ in range(nb)]
+    P = [asm.constructDofVector() for _ in range(nb)]
+    F = [asm.constructDofVector() for _ in range(nb)]
+    K = [asm.constructSystemMatrix() for _ in range(nb)]
+    st = [torch.zeros(4, dtype=torch.int32, device=dev) for _ in range(nb)]
+    Ph = [torch.empty_like(P[0], device="cpu").pin_memory() for _ in range(nb)]
+    Fh = [torch.empty_like(F[0], device="cpu").pin_memory() for _ in range(nb)]
+    Kh = [torch.empty_like(K[0], device="cpu").pin_memory() for _ in range(nb)]
+    nsteps = args.warmup + args.steps
+    Sh = torch.zeros((nsteps, 4), dtype=torch.int32).pin_memory()
+    s_in, s_run, s_out = torch.cuda.Stream(dev), torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    ev = lambda: torch.cuda.Event()  # noqa: E731
+    in_done = [ev() for _ in range(nb)]
+    run_done = [ev() for _ in range(nb)]
+    out_done = [ev() for _ in range(nb)]
+    used = [False] * nb
 
-    def step():
-        U.copy_(Uh, non_blocking=True)
-        dU.copy_(dUh, non_blocking=True)
-        P.zero_()
-        F.zero_()
-        K.zero_()
-        asm.computeElements(None, U, dU, P, K, F, check=True)
-        Ph.copy_(P, non_blocking=True)
-        Fh.copy_(F, non_blocking=True)
-        Kh.copy_(K, non_blocking=True)
-        torch.cuda.synchronize(dev)
+    def step(k):
+        b = k % nb
+        with torch.cuda.stream(s_in):
+            if used[b]:
+                s_in.wait_event(run_done[b])  # the pass of step k-2 has read U[b], dU[b]
+            U[b].copy_(Uh, non_blocking=True)
+            dU[b].copy_(dUh, non_blocking=True)
+            in_done[b].record(s_in)
+        with torch.cuda.stream(s_run):
+            s_run.wait_event(in_done[b])
+            if used[b]:
+                s_run.wait_event(out_done[b])  # step k-2's outputs have left the device
+            P[b].zero_()
+            F[b].zero_()
+            K[b].zero_()
+            st[b].zero_()
+            asm.launch(U[b], dU[b], P[b], K[b], F[b], status=st[b])
+            run_done[b].record(s_run)
+        with torch.cuda.stream(s_out):
+            s_out.wait_event(run_done[b])
+            Ph[b].copy_(P[b], non_blocking=True)
+            Fh[b].copy_(F[b], non_blocking=True)
+            Kh[b].copy_(K[b], non_blocking=True)
+            Sh[k].copy_(st[b], non_blocking=True)
+            out_done[b].record(s_out)
+        used[b] = True
 
-    for _ in range(args.warmup):
-        step()
+    for k in range(args.warmup):
+        step(k)
     torch.cuda.synchronize(dev)
     t = time.perf_counter()
-    for _ in range(args.steps):
-        step()
+    for k in range(args.warmup, nsteps):
+        step(k)
     torch.cuda.synchronize(dev)
     ms = (time.perf_counter() - t) * 1e3 / args.steps
-    return dict(ms=ms, h2d=2 * U.numel() * 8, d2h=2 * P.numel() * 8 + K.numel() * K.element_size())
+    if (Sh[:, 0] & 1).any():
+        from edelweissfe_gb300.exceptions import CutbackRequest
+
+        raise CutbackRequest("material point failed in the end-to-end pass", 0.5)
+    return dict(ms=ms, h2d=2 * U[0].numel() * 8, d2h=2 * P[0].numel() * 8 + K[0].numel() * K[0].element_size() + 16)
 
 
 # ------------------------------------------------------------------ CPU baseline (oracle port)

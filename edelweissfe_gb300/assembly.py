@@ -222,8 +222,10 @@ class GPUAssembler:
             return x.contiguous()
         return torch.as_tensor(np.asarray(x, np.float64), device=self.device)
 
-    def launch(self, U_np, dU, P, K, F, time=None, dT=0.0):
-        """Enqueue one element pass on the current stream (no synchronisation, no status check)."""
+    def launch(self, U_np, dU, P, K, F, time=None, dT=0.0, status=None):
+        """Enqueue one element pass on the current stream (no synchronisation, no status check).
+        status: an int32 device tensor of 4 words to report into instead of the assembler's own
+        (for passes in flight at the same time); the caller zeroes it."""
         if K.dtype != self.kdtype or K.numel() != self.nnz:
             raise ValueError(f"K must be a {self.kdtype} vector of length nnz={self.nnz}")
         for v in (U_np, dU, P, F):
@@ -234,8 +236,8 @@ class GPUAssembler:
             self.lib.efe_compute_elements(
                 ctypes.byref(self.mesh), self._groups_c, len(self.groups), ctypes.c_void_p(U_np.data_ptr()),
                 ctypes.c_void_p(dU.data_ptr()), t2, float(dT), self.kPrecision, ctypes.c_void_p(K.data_ptr()),
-                ctypes.c_void_p(P.data_ptr()), ctypes.c_void_p(F.data_ptr()), ctypes.c_void_p(self.status.data_ptr()),
-                self._stream(),
+                ctypes.c_void_p(P.data_ptr()), ctypes.c_void_p(F.data_ptr()),
+                ctypes.c_void_p((self.status if status is None else status).data_ptr()), self._stream(),
             ),
             "efe_compute_elements",
         )
