@@ -175,6 +175,21 @@ def oracle_rate(elType, kind, props, n_side, disp, seed=0, reps=2):
     return len(conn) * reps / secs, len(conn) * reps, secs
 
 
+def max_over_ranks(values, device):
+    """Element-wise maximum of per-rank timings over all ranks (every rank gets the result): the
+    job's step time is its slowest replica's."""
+    import torch
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
+def job_throughput(units_per_rank, world, ms):
+    """Whole-job units per second: every replica processes units_per_rank in the max-over-ranks ms."""
+    return world * units_per_rank / (ms * 1e-3)
+
+
 # ------------------------------------------------------------------ GPU arm
 def run_gpu(args, rank, world):
     import torch
@@ -229,9 +244,7 @@ def run_gpu(args, rank, world):
         ms = t0.elapsed_time(t1) / args.steps
         kms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
         if world > 1:
-            tt = torch.tensor([ms, kms], device=dev)
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            ms, kms = float(tt[0]), float(tt[1])
+            ms, kms = max_over_ranks([ms, kms], dev)
         asm.check_status()
         state[precision] = dict(P=P.clone(), K=K.double().clone(), st=asm.group_state(0))
         results[precision] = dict(ms=ms, kernel_ms=kms, nnz=asm.nnz, asm=asm)
@@ -886,7 +899,7 @@ def main():
                           "elem_per_s": nEl / (r["ms"] * 1e-3)}))
         return
     mixed, fp64, e2e = results["mixed"], results["fp64"], results["e2e"]
-    value = world * nEl / (mixed["ms"] * 1e-3)
+    value = job_throughput(nEl, world, mixed["ms"])
     peak, peak_kind = peaks()
     abytes = algorithmic_bytes(nEl, 8, 13, nNodes, nDof, mixed["nnz"], 4)
     achieved = abytes / (mixed["kernel_ms"] * 1e-3) / 1e9
