@@ -102,6 +102,7 @@ class EfePcg(ctypes.Structure):
         ("Ap", ctypes.c_void_p),
         ("work", ctypes.c_void_p),
         ("pFF", ctypes.c_void_p),
+        ("blockSize", ctypes.c_int32),
     ]
 
 

@@ -478,6 +478,8 @@ int32_t check_pcg(const EfePcg* s) {
                    !s->Ap || !s->work))
     return fail(EFE_ERR_ARGUMENT, "null solver buffer");
   if (reinterpret_cast<uintptr_t>(s->pFF) % 8 != 0) return fail(EFE_ERR_ARGUMENT, "pFF must be 8-byte aligned");
+  if (s->blockSize < 1 || s->blockSize > 3 || s->n % s->blockSize != 0)
+    return fail(EFE_ERR_ARGUMENT, "blockSize must be 1, 2 or 3 and divide n");
   return EFE_OK;
 }
 }  // namespace

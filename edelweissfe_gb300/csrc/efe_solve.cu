@@ -19,8 +19,11 @@
 // the Newton and adjoint drivers check their solutions with FP64 residuals.  FP64 tangents use
 // DFMA.  Eight lanes per row (four rows per warp) keep the cross-lane reduction short.
 //
+// Preconditioner: the inverse of the diagonal (blockSize 1) or of the nodal diagonal blocks
+// (blockSize = 2 or 3 consecutive DOFs, the node's displacement components), built by the caller.
+//
 // One iteration is three kernels: (1) Ap = A p with the partial sums of p.Ap per block, (2) alpha,
-// x += alpha p, r -= alpha Ap, z = D^-1 r with the partial sums of r.z and r.r, (3) beta,
+// x += alpha p, r -= alpha Ap, z = M^-1 r with the partial sums of r.z and r.r, (3) beta,
 // p = z + beta p.  The scalars stay on the device: every block sums the previous kernel's partials
 // in the same fixed order, so the iteration is deterministic, and rz is double-buffered by the
 // parity of the iteration number so no kernel overwrites a scalar another block is reading.
@@ -167,7 +170,28 @@ __global__ void __launch_bounds__(NT) spmv_kernel(int64_t n, const int32_t* __re
   }
 }
 
-// r = b, z = dinv r, p = z (x = 0); partials of r.z and r.r
+// z = M^-1 r on one block of BS consecutive DOFs (BS = 1: point Jacobi; 2, 3: the inverse of the
+// node's diagonal block, [BS][BS] row-major per block)
+template <int BS>
+__device__ __forceinline__ void precondition(const double* __restrict__ dinv, int64_t blk, const double r[BS],
+                                             double z[BS]) {
+  const double* D = dinv + blk * BS * BS;
+#pragma unroll
+  for (int i = 0; i < BS; ++i) {
+    double v = 0.0;
+#pragma unroll
+    for (int j = 0; j < BS; ++j) v = fma(D[i * BS + j], r[j], v);
+    z[i] = v;
+  }
+}
+
+__device__ __forceinline__ void split_ff(double v, float2* pf, int64_t i) {
+  const float h = __double2float_rn(v);
+  pf[i] = make_float2(h, __double2float_rn(v - (double)h));
+}
+
+// r = b, z = M^-1 r, p = z (x = 0); partials of r.z and r.r; one thread per block of BS DOFs
+template <int BS>
 __global__ void __launch_bounds__(NT) pcg_start_kernel(int64_t n, const double* __restrict__ b,
                                                        const double* __restrict__ dinv, double* __restrict__ x,
                                                        double* __restrict__ r, double* __restrict__ z,
@@ -175,18 +199,23 @@ __global__ void __launch_bounds__(NT) pcg_start_kernel(int64_t n, const double* 
                                                        double* work) {
   __shared__ double sh[WARPS + 1];
   double rz = 0.0, rr = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
-    const double ri = b[i], zi = dinv[i] * ri;
-    x[i] = 0.0;
-    r[i] = ri;
-    z[i] = zi;
-    p[i] = zi;
-    if (pf) {
-      const float h = __double2float_rn(zi);
-      pf[i] = make_float2(h, __double2float_rn(zi - (double)h));
+  const int64_t nb = n / BS;
+  for (int64_t k = (int64_t)blockIdx.x * NT + threadIdx.x; k < nb; k += (int64_t)gridDim.x * NT) {
+    double rv[BS], zv[BS];
+#pragma unroll
+    for (int c = 0; c < BS; ++c) rv[c] = b[k * BS + c];
+    precondition<BS>(dinv, k, rv, zv);
+#pragma unroll
+    for (int c = 0; c < BS; ++c) {
+      const int64_t i = k * BS + c;
+      x[i] = 0.0;
+      r[i] = rv[c];
+      z[i] = zv[c];
+      p[i] = zv[c];
+      if (pf) split_ff(zv[c], pf, i);
+      rz = fma(rv[c], zv[c], rz);
+      rr = fma(rv[c], rv[c], rr);
     }
-    rz = fma(ri, zi, rz);
-    rr = fma(ri, ri, rr);
   }
   const double s1 = block_sum(rz, sh);
   if (threadIdx.x == 0) work[PART1 + blockIdx.x] = s1;
@@ -206,7 +235,8 @@ __global__ void __launch_bounds__(NT) pcg_start_finish(double* work, int nb) {
   }
 }
 
-// alpha = rz[cur] / p.Ap; x += alpha p; r -= alpha Ap; z = dinv r; partials of r.z (PART1), r.r (PART2)
+// alpha = rz[cur] / p.Ap; x += alpha p; r -= alpha Ap; z = M^-1 r; partials of r.z (PART1), r.r (PART2)
+template <int BS>
 __global__ void __launch_bounds__(NT) pcg_update_kernel(int64_t n, int cur, int nbSpmv, const double* __restrict__ p,
                                                         const double* __restrict__ Ap, const double* __restrict__ dinv,
                                                         double* __restrict__ x, double* __restrict__ r,
@@ -215,14 +245,23 @@ __global__ void __launch_bounds__(NT) pcg_update_kernel(int64_t n, int cur, int 
   const double pAp = sum_partials(work + PART0, nbSpmv, sh);
   const double alpha = pAp != 0.0 ? work[cur] / pAp : 0.0;
   double rz = 0.0, rr = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
-    x[i] = fma(alpha, p[i], x[i]);
-    const double ri = fma(-alpha, Ap[i], r[i]);
-    const double zi = dinv[i] * ri;
-    r[i] = ri;
-    z[i] = zi;
-    rz = fma(ri, zi, rz);
-    rr = fma(ri, ri, rr);
+  const int64_t nb = n / BS;
+  for (int64_t k = (int64_t)blockIdx.x * NT + threadIdx.x; k < nb; k += (int64_t)gridDim.x * NT) {
+    double rv[BS], zv[BS];
+#pragma unroll
+    for (int c = 0; c < BS; ++c) {
+      const int64_t i = k * BS + c;
+      x[i] = fma(alpha, p[i], x[i]);
+      rv[c] = fma(-alpha, Ap[i], r[i]);
+      r[i] = rv[c];
+    }
+    precondition<BS>(dinv, k, rv, zv);
+#pragma unroll
+    for (int c = 0; c < BS; ++c) {
+      z[k * BS + c] = zv[c];
+      rz = fma(rv[c], zv[c], rz);
+      rr = fma(rv[c], rv[c], rr);
+    }
   }
   const double s1 = block_sum(rz, sh);
   if (threadIdx.x == 0) work[PART1 + blockIdx.x] = s1;
@@ -310,7 +349,11 @@ cudaError_t csr_spmv(const EfePcg& s, const double* x, double* y, cudaStream_t s
 
 cudaError_t pcg_start(const EfePcg& s, const double* b, cudaStream_t st) {
   const int nb = vec_blocks(s.n, sm_count());
-  pcg_start_kernel<<<nb, NT, 0, st>>>(s.n, b, s.dinv, s.x, s.r, s.z, s.p, pff(s), s.work);
+  switch (s.blockSize) {
+    case 1: pcg_start_kernel<1><<<nb, NT, 0, st>>>(s.n, b, s.dinv, s.x, s.r, s.z, s.p, pff(s), s.work); break;
+    case 2: pcg_start_kernel<2><<<nb, NT, 0, st>>>(s.n, b, s.dinv, s.x, s.r, s.z, s.p, pff(s), s.work); break;
+    default: pcg_start_kernel<3><<<nb, NT, 0, st>>>(s.n, b, s.dinv, s.x, s.r, s.z, s.p, pff(s), s.work); break;
+  }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   pcg_start_finish<<<1, NT, 0, st>>>(s.work, nb);
@@ -326,7 +369,11 @@ cudaError_t pcg_iterate(const EfePcg& s, int64_t k0, int nIter, cudaStream_t st)
     cudaError_t e = pf ? spmv_t<float, true>(s, s.p, pf, s.Ap, s.work + PART0, nbS, st)
                        : spmv(s, s.p, s.Ap, s.work + PART0, nbS, st);
     if (e != cudaSuccess) return e;
-    pcg_update_kernel<<<nbV, NT, 0, st>>>(s.n, cur, nbS, s.p, s.Ap, s.dinv, s.x, s.r, s.z, s.work);
+    switch (s.blockSize) {
+      case 1: pcg_update_kernel<1><<<nbV, NT, 0, st>>>(s.n, cur, nbS, s.p, s.Ap, s.dinv, s.x, s.r, s.z, s.work); break;
+      case 2: pcg_update_kernel<2><<<nbV, NT, 0, st>>>(s.n, cur, nbS, s.p, s.Ap, s.dinv, s.x, s.r, s.z, s.work); break;
+      default: pcg_update_kernel<3><<<nbV, NT, 0, st>>>(s.n, cur, nbS, s.p, s.Ap, s.dinv, s.x, s.r, s.z, s.work); break;
+    }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     pcg_direction_kernel<<<nbV, NT, 0, st>>>(s.n, cur, nbV, s.z, s.p, pf, s.work);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;

@@ -148,7 +148,8 @@ class NISTGPU:
 
     def __init__(self, assembler, linsolver="pcg", extrapolation="linear", maxIter=10, criticalIter=5,
                  maxGrowingIter=10, fluxResidualTolerance=1e-8, fluxResidualToleranceAlternative=5e-3,
-                 fieldCorrectionTolerance=1e-8, pcgTolerance=1e-12, pcgMaxIter=20000, fluxResidualFloor=1e-7):  # fmt: skip
+                 fieldCorrectionTolerance=1e-8, pcgTolerance=1e-12, pcgMaxIter=20000, fluxResidualFloor=1e-7,
+                 pcgPreconditioner="jacobi"):  # fmt: skip
         self.asm = assembler
         self.linsolver = linsolver
         self.extrapolation = extrapolation
@@ -161,6 +162,10 @@ class NISTGPU:
         self.pcgTolerance = pcgTolerance
         self.pcgMaxIter = pcgMaxIter
         self.fluxFloor = fluxResidualFloor
+        # "jacobi": inverse of the diagonal; "block": inverses of the nodal diagonal blocks (the node's
+        # displacement components) -- on near-regular hexahedral meshes of isotropic material the
+        # same-node couplings nearly cancel and both need the same iterations
+        self.pcgPreconditioner = pcgPreconditioner
         self.nAccumulatedFluxes = sum(len(g.conn) * len(g.conn[0]) * assembler.dim for g in assembler.groups if len(g.conn))
         dev = assembler.device
         ip, ix = assembler.indptr_host, assembler.indices_host
@@ -314,7 +319,8 @@ class NISTGPU:
         return torch.from_numpy(np.asarray(x, np.float64)).to(self.asm.device)
 
     def _solve_pcg(self, K, R, dir_idx):
-        """Jacobi-preconditioned CG on the device (efe_pcg_start / efe_pcg_iterate).  The reference's
+        """Preconditioned CG on the device (efe_pcg_start / efe_pcg_iterate), nodal block-Jacobi or
+        Jacobi (pcgPreconditioner).  The reference's
         system has identity rows for the Dirichlet DOFs; moving the known values to the right-hand
         side gives the same solution from the symmetric positive-definite system on the free DOFs:
         x = x_d + y with x_d = R on the prescribed DOFs and K_ff y_f = R_f - K_fd x_d.  K is used as
@@ -332,15 +338,26 @@ class NISTGPU:
         if dir_idx is not None:
             m[dir_idx] = 0
         mf = m.to(torch.float64)
-        d = K[self._diag_pos].to(torch.float64)
-        dinv = torch.where(m > 0, 1.0 / d, torch.ones_like(d))
+        bs = asm.dim if self.pcgPreconditioner == "block" and n % asm.dim == 0 else 1
+        if bs > 1:
+            # a node's DOFs are consecutive and its own columns are contiguous in every one of its
+            # rows, ending with column = row at the diagonal position: block (i, j) of node k is at
+            # diag_pos[k*bs + i] - i + j
+            ij = torch.arange(bs, device=dev)
+            pos = self._diag_pos.view(-1, bs)[:, :, None] - ij[None, :, None] + ij[None, None, :]
+            mb = mf.view(-1, bs)
+            B = K[pos].to(torch.float64) * mb[:, :, None] * mb[:, None, :] + torch.diag_embed(1.0 - mb)
+            dinv = torch.linalg.inv(B).contiguous()
+        else:
+            d = K[self._diag_pos].to(torch.float64)
+            dinv = torch.where(m > 0, 1.0 / d, torch.ones_like(d))
         vec = torch.empty((5, n), dtype=torch.float64, device=dev)
         work = torch.zeros(L.EFE_PCG_WORK_DOUBLES, dtype=torch.float64, device=dev)
         kp = L.EFE_K_FP64 if K.dtype == torch.float64 else L.EFE_K_FP32
         split = torch.empty((n, 2), dtype=torch.float32, device=dev) if kp == L.EFE_K_FP32 else None
         s = L.EfePcg(n, asm.indptr.data_ptr(), asm.indices.data_ptr(), K.data_ptr(), kp, m.data_ptr(), dinv.data_ptr(),
                      *[vec[i].data_ptr() for i in range(5)], work.data_ptr(),
-                     split.data_ptr() if split is not None else None)  # fmt: skip
+                     split.data_ptr() if split is not None else None, bs)  # fmt: skip
         stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
         xd = (1.0 - mf) * R
         Kxd = torch.empty_like(R)

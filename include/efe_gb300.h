@@ -252,7 +252,9 @@ typedef struct EfePcg {
   const void* Kdata;       /* CSR data, double (EFE_K_FP64) or float (EFE_K_FP32, EFE_K_FP32_FF) */
   int32_t kPrecision;
   const uint8_t* freeMask; /* [n] 1 = free DOF, 0 = prescribed; NULL = all free                  */
-  const double* dinv;      /* [n] 1 / K_ii on free DOFs, 1 on prescribed ones                   */
+  const double* dinv;      /* preconditioner: blockSize 1: [n] 1 / K_ii on free DOFs, 1 on
+                              prescribed ones; blockSize 2 or 3: [n / bs][bs][bs] inverses of the
+                              nodal diagonal blocks (prescribed rows/columns replaced by identity) */
   double* x;
   double* r;
   double* z;
@@ -262,6 +264,7 @@ typedef struct EfePcg {
   float* pFF;              /* optional [n][2], 8-byte aligned: with FP32 K the CG products run in
                               float-float arithmetic on p = pFF[i][0] + pFF[i][1] (FP32 pipe);
                               NULL: FP64 arithmetic                                            */
+  int32_t blockSize;       /* 1, 2 or 3 DOFs per preconditioner block (n a multiple of it)     */
 } EfePcg;
 /* y_i = free_i ? (K x)_i : x_i */
 int32_t efe_csr_spmv(const EfePcg* solver, const double* x, double* y, void* stream);

@@ -1,5 +1,5 @@
-"""Device linear solve (efe_csr_spmv, efe_pcg_start, efe_pcg_iterate) against SciPy's direct solve of
-the same system: the assembled tangent of a jittered Hexa8 / Hexa20 von Mises block (FP64 and FP32
+"""Device linear solve (efe_csr_spmv, efe_pcg_start, efe_pcg_iterate; nodal block-Jacobi and point
+Jacobi preconditioners) against SciPy's direct solve of the same system: the assembled tangent of a jittered Hexa8 / Hexa20 von Mises block (FP64 and FP32
 CSR data), a random right-hand side and a set of prescribed DOFs whose values are carried by the
 right-hand side (identity rows, as applyDirichletK).  PCG relative tolerance 1e-14: solutions
 agree to 1e-9 relative; two runs are bitwise identical (fixed-order reductions)."""
@@ -11,8 +11,9 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("preconditioner", ["block", "jacobi"])
 @pytest.mark.parametrize("elType,precision", [("C3D8", "fp64"), ("C3D8", "mixed"), ("C3D20", "mixed")])
-def test_pcg_matches_direct_solve(elType, precision):
+def test_pcg_matches_direct_solve(elType, precision, preconditioner):
     import scipy.sparse as sp
     import scipy.sparse.linalg as sla
 
@@ -23,7 +24,7 @@ def test_pcg_matches_direct_solve(elType, precision):
     coords = meshes.jitter(coords, 0.1, [0.25, 1 / 3, 0.5], 3, [0, 0, 0], [1, 1, 1])
     asm = GPUAssembler(coords, nodeDof, nDof, [ElementGroup(elType, "vonmises", [210e3, 0.3, 250, 1000, 0, 0], conn)],
                        precision=precision)  # fmt: skip
-    solver = NISTGPU(asm, pcgTolerance=1e-14)
+    solver = NISTGPU(asm, pcgTolerance=1e-14, pcgPreconditioner=preconditioner)
     rng = np.random.default_rng(1)
     U = torch.tensor(rng.normal(0, 1e-3, nDof), device=asm.device)
     K = solver.tangentAt(U)
@@ -52,7 +53,7 @@ def test_pcg_matches_direct_solve(elType, precision):
     work = torch.zeros(L.EFE_PCG_WORK_DOUBLES, dtype=torch.float64, device=asm.device)
     kp = L.EFE_K_FP64 if K.dtype == torch.float64 else L.EFE_K_FP32
     s = L.EfePcg(nDof, asm.indptr.data_ptr(), asm.indices.data_ptr(), K.data_ptr(), kp, None, y.data_ptr(),
-                 y.data_ptr(), y.data_ptr(), y.data_ptr(), y.data_ptr(), y.data_ptr(), work.data_ptr(), None)  # fmt: skip
+                 y.data_ptr(), y.data_ptr(), y.data_ptr(), y.data_ptr(), y.data_ptr(), work.data_ptr(), None, 1)  # fmt: skip
     L.check(L.load().efe_csr_spmv(ctypes.byref(s), ctypes.c_void_p(v.data_ptr()), ctypes.c_void_p(y.data_ptr()),
                                   None), "efe_csr_spmv")  # fmt: skip
     torch.cuda.synchronize()
