@@ -214,6 +214,15 @@ def run_gpu(args, rank, world):
         U = torch.tensor(dU1 + dU2, device=dev)
         dU = torch.tensor(dU2, device=dev)
         stream = torch.cuda.current_stream(dev)
+        if not args.no_autotune:
+            # the tile shape per group, chosen by timing the variants on these inputs (untimed; the
+            # pass reads stateRef and writes stateTemp only, so the state is unchanged)
+            from edelweissfe_gb300.autotune import Autotuner
+
+            tuner = Autotuner()
+            tuner.tune_assembler(asm, U, dU, P, K, F)
+            results.setdefault("tile_variants", {})[precision] = {
+                "chosen": int(asm._groups_c[0].tileVariant), "ms": tuner.log[-1][1] if tuner.log else None}
 
         def step(ev=None):
             P.zero_()
@@ -862,6 +871,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_CUBE, help="elements per cube edge")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default tile variant (0)")
     ap.add_argument("--workload", default="cube", choices=["cube", "batched", "newton", "adjoint", "plastic"],
                     help="cube: the 64^3 von Mises headline; batched: the uneven-mesh batch; newton: Newton "
                          "iterations FP64 vs mixed on the 64^3 cube; adjoint: 32^3 Neo-Hooke gradients; "
@@ -933,6 +943,7 @@ def main():
         },
         "fp64": {"value": world * nEl / (fp64["ms"] * 1e-3), "ms_per_step": fp64["ms"], "kernel_ms": fp64["kernel_ms"]},
         "mixed_over_fp64": fp64["ms"] / mixed["ms"],
+        "tile_variants": results.get("tile_variants"),
         "mixed_ff": {"value": world * nEl / (results["mixed-ff"]["ms"] * 1e-3), "ms_per_step": results["mixed-ff"]["ms"],
                      "kernel_ms": results["mixed-ff"]["kernel_ms"]},
         "errors": errs,

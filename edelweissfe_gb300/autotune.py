@@ -8,7 +8,7 @@ import os
 
 import torch
 
-VARIANTS = (0, 1)
+VARIANTS = (0, 1, 2)
 
 
 def _key(asm, gi):

@@ -10,17 +10,22 @@ namespace efe {
 // The autotuner (edelweissfe_gb300/autotune.py) picks one per group by timing both.
 template <int SHAPE, int RULE, int FORM, typename KT, int VARIANT = 0>
 struct Tile {
+  // variant 0: 128 threads, ~128 points, 3 CTAs/SM where they fit; 1: 256 threads, ~256 points;
+  // 2: variant 0's tile with 4 CTAs/SM where shared memory allows (the compiler then holds the
+  // kernel to 128 registers per thread)
   static constexpr int NQ = RuleInfo<RULE>::NQ;
   static constexpr size_t per_element = Layout<SHAPE, RULE, FORM, KT, 1>::bytes;
-  static constexpr size_t budget = VARIANT == 0 ? 72 * 1024 : 110 * 1024;
-  static constexpr int points = VARIANT == 0 ? 128 : 256;
+  static constexpr size_t budget = VARIANT == 1 ? 110 * 1024 : 72 * 1024;
+  static constexpr int points = VARIANT == 1 ? 256 : 128;
   static constexpr int fit = (int)(budget / per_element);
   static constexpr int want = (points + NQ - 1) / NQ;
   static constexpr int e0 = fit < want ? fit : want;
   static constexpr int EPB = e0 < 1 ? 1 : (e0 > 32 ? 32 : e0);
-  static constexpr int NT = VARIANT == 0 ? 128 : 256;
+  static constexpr int NT = VARIANT == 1 ? 256 : 128;
   static constexpr size_t bytes = Layout<SHAPE, RULE, FORM, KT, EPB>::bytes;
-  static constexpr int MINB = VARIANT == 0 ? (bytes <= 72 * 1024 ? 3 : 1) : 1;
+  static constexpr int MINB = VARIANT == 1 ? 1
+                              : (VARIANT == 2 && bytes <= 56 * 1024) ? 4
+                              : (bytes <= 72 * 1024 ? 3 : 1);
 };
 
 template <int SHAPE, int RULE, int FORM, typename KT, bool FF, int VARIANT>
@@ -39,6 +44,9 @@ cudaError_t launch_assemble_variant(const GroupArgs& g, cudaStream_t st) {
 template <int SHAPE, int RULE, int FORM, typename KT, bool FF = false>
 cudaError_t launch_assemble(const GroupArgs& g, cudaStream_t st) {
   if (g.tileVariant == 1) return launch_assemble_variant<SHAPE, RULE, FORM, KT, FF, 1>(g, st);
+  if constexpr (Tile<SHAPE, RULE, FORM, KT, 2>::MINB != Tile<SHAPE, RULE, FORM, KT, 0>::MINB) {
+    if (g.tileVariant == 2) return launch_assemble_variant<SHAPE, RULE, FORM, KT, FF, 2>(g, st);
+  }
   return launch_assemble_variant<SHAPE, RULE, FORM, KT, FF, 0>(g, st);
 }
 

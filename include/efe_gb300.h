@@ -128,7 +128,8 @@ typedef struct EfeGroup {
                                 hyperelastic materials                                        */
   double* auxTemp;           /* TL only: Green-Lagrange strain of this call                  */
   int32_t tileVariant;       /* CTA shape of the element pass: 0 = 128 threads, 3 CTAs/SM;
-                                1 = 256 threads, larger tiles (chosen by the autotuner)       */
+                                1 = 256 threads, larger tiles; 2 = as 0 with 4 CTAs/SM where
+                                shared memory allows (chosen by the autotuner)                */
 } EfeGroup;
 
 /* One (mesh, group) pair of a persistent launch, with its own DOF vectors and CSR data. */
