@@ -45,7 +45,12 @@ class TLAdjoint:
             dir_idx = torch.as_tensor(dirichletDofs, dtype=torch.int64, device=asm.device)
             g[dir_idx] = 0.0
         if K is None:
-            K = self.solver.tangentAt(U.to(asm.device, torch.float64))
+            # the forward solve's last element pass assembled K at exactly this U (hyperelastic: the
+            # tangent depends on U only); otherwise assemble it
+            if getattr(self.solver, "lastU", None) is U and self.solver.lastK is not None:
+                K = self.solver.lastK
+            else:
+                K = self.solver.tangentAt(U.to(asm.device, torch.float64))
         n0 = len(self.solver.linearIterations)
         lam = self.solver._solve_pcg(K, g, dir_idx)
         self.lastLinearIterations = self.solver.linearIterations[n0:]
@@ -55,8 +60,8 @@ class TLAdjoint:
 
     def gradient(self, U, dJdU, dirichletDofs):
         """(dJ/dX [nNodes, dim], [dJ/d(mu, K) per group [E, 2]]) at the equilibrium U."""
-        U = U.to(self.asm.device, torch.float64)
         lam = self.solve_adjoint(U, dJdU, dirichletDofs)
+        U = U.to(self.asm.device, torch.float64)
         return self.asm.adjointTL(U, lam)
 
 

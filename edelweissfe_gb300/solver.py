@@ -173,6 +173,7 @@ class NISTGPU:
         self._diag_pos = torch.from_numpy(np.nonzero(ix == rows)[0]).to(dev)
         self.history = []  # one record per attempted increment
         self.linearIterations = []
+        self.lastK = self.lastU = self.lastP = None
         # called as onAccept(timeStep, U_old, U_new, dU) before each accepted increment's state is
         # committed (the state of the assembler is still the one before the increment)
         self.onAccept = None
@@ -200,6 +201,8 @@ class NISTGPU:
                     if iters >= self.criticalIter:
                         stepper.preventIncrementIncrease()
                     self.lastP = P
+                    # the final tangent, assembled at exactly the accepted U (reused by adjoints)
+                    self.lastK, self.lastU = self._incrementK, U_new
                     if self.onAccept is not None:
                         self.onAccept(ts, U, U_new, dU)
                     U = U_new
@@ -275,6 +278,7 @@ class NISTGPU:
                 raise DivergingSolution("Obtained NaN in linear solve")
             dU = dU + ddU
             it += 1
+        self._incrementK = K  # the tangent of the last element pass, at the converged U_np
         return U_np, dU, P, it, residuals
 
     def tangentAt(self, U):
