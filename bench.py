@@ -484,9 +484,11 @@ def run_batched(args):
             b.U.copy_(torch.tensor(np.concatenate([m["U"] for m in chunk])))
             batches.append(b)
     setup_s = time.perf_counter() - t0
-    bp = BatchedPass(batches, persistent=len(batches) == 2)
+    bp = BatchedPass(batches, persistent=True)
     tuner = Autotuner()
-    tuning = tuner.tune_batched(bp)
+    tuning = tuner.tune_batched(bp)  # tile variants per batch; persistent vs per-batch timed
+    if args.batch_launch == "persistent" and bp.can_persist:
+        bp.persistent = True
     bp.capture()
     for _ in range(args.warmup):
         bp.replay()
@@ -877,6 +879,8 @@ def main():
     ap.add_argument("--fd-directions", type=int, default=3)
     ap.add_argument("--batch-meshes", type=int, default=512)
     ap.add_argument("--batch-scale", type=float, default=1.0)
+    ap.add_argument("--batch-launch", default="persistent", choices=["persistent", "auto"],
+                    help="batched workload: one persistent launch over all batches, or the autotuner's choice")
     ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64", "mixed-ff"],
                     help="profiling aid: run one mode only (the JSON line needs both)")
     args = ap.parse_args()

@@ -79,7 +79,7 @@ class Autotuner:
         """Choose persistent vs per-batch launches for a BatchedPass (and the variants of its groups)."""
         for b in bp.batches:
             self.tune_assembler(b.asm, b.U, b.dU, b.P, b.K, b.F)
-        if len(bp.batches) != 2:
+        if not bp.can_persist:
             bp.persistent = False
             return {}
         times = {}

@@ -3,10 +3,10 @@
 Meshes of one dimension are concatenated into one block-diagonal system (`MeshBatch`): their
 nodes, DOFs and CSR rows are stacked, so one group spans every mesh of a batch and each mesh's
 DOF vectors and CSR data are contiguous slices of the batch's.  `BatchedPass` runs the element
-pass of up to two batches (e.g. the 2D and the 3D meshes) either as one persistent launch
-(`efe_compute_elements_persistent`: the resident CTAs take tiles of both batches from one work
-counter) or as one launch per batch, and can capture the whole pass (zeroing of P, F, K and the
-launches) in a CUDA graph.
+pass of several batches (e.g. the 2D and the 3D meshes, each split into int32-indexable chunks)
+either as one persistent launch (`efe_compute_elements_persistent`: the resident CTAs take tiles of
+all batches from one work counter) or as one launch per batch, and can capture the whole pass
+(zeroing of P, F, K and the launches) in a CUDA graph.
 """
 
 import ctypes
@@ -84,19 +84,38 @@ class MeshBatch:
                 slice(int(self.nnz_offsets[i]), int(self.nnz_offsets[i + 1])))  # fmt: skip
 
 
+# element types of the persistent kernel (efe_compute_elements_persistent)
+PERSISTENT_TYPES = {"C3D20TL": "heavy", "C3D20NTL": "heavy", "CPE8RTL": "light", "CPS8RTL": "light"}
+PERSISTENT_MAX_GROUPS = 8
+
+
+def persistent_capable(batches):
+    """True if one persistent launch can run all batches: total-Lagrangian Neo-Hooke Hexa20 3x3x3 and
+    Quad8 2x2 batches, at most eight of each, one precision."""
+    kinds = [PERSISTENT_TYPES.get(b.asm.groups[0].elType.upper()) for b in batches]
+    if None in kinds or any(not b.asm.groups[0].material.lower().startswith("neohooke") for b in batches):
+        return False
+    if kinds.count("heavy") > PERSISTENT_MAX_GROUPS or kinds.count("light") > PERSISTENT_MAX_GROUPS:
+        return False
+    return len({b.K.dtype for b in batches}) == 1
+
+
 class BatchedPass:
-    """The element pass of one or two MeshBatch objects."""
+    """The element pass of several MeshBatch objects: one persistent launch over all of them (when
+    persistent_capable) or one launch per batch."""
 
     def __init__(self, batches, persistent=True):
         self.batches = list(batches)
         self.lib = L.load()
-        self.persistent = persistent and len(self.batches) == 2
+        self.can_persist = persistent_capable(self.batches)
+        self.persistent = persistent and self.can_persist
         dev = self.batches[0].asm.device
         self.counter = torch.zeros(1, dtype=torch.int64, device=dev)
         self.status = torch.zeros(4, dtype=torch.int32, device=dev)
         self.graph = None
-        if len(self.batches) == 2:
-            self._items = (L.EfeWorkItem * 2)(*[
+        if self.can_persist:
+            n = len(self.batches)
+            self._items = (L.EfeWorkItem * n)(*[
                 L.EfeWorkItem(ctypes.addressof(b.asm.mesh), ctypes.addressof(b.asm._groups_c[0]), b.U.data_ptr(),
                               b.dU.data_ptr(), b.K.data_ptr(), b.P.data_ptr(), b.F.data_ptr())
                 for b in self.batches
@@ -107,7 +126,7 @@ class BatchedPass:
     def _launch(self):
         stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         if self.persistent:
-            L.check(self.lib.efe_compute_elements_persistent(self._items, 2, self._prec,
+            L.check(self.lib.efe_compute_elements_persistent(self._items, len(self.batches), self._prec,
                                                              ctypes.c_void_p(self.counter.data_ptr()),
                                                              ctypes.c_void_p(self.status.data_ptr()), stream),
                     "efe_compute_elements_persistent")  # fmt: skip

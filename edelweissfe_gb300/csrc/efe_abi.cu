@@ -409,27 +409,48 @@ int32_t efe_adjoint_small_strain(const EfeMesh* mesh, const EfeGroup* g, const d
   return EFE_OK;
 }
 
-int32_t efe_compute_elements_persistent(const EfeWorkItem* items, int32_t nItems, int32_t kPrecision,
-                                        uint64_t* workCounter, int32_t* status, void* stream) {
-  if (!items || nItems != 2 || !workCounter || !status) return fail(EFE_ERR_ARGUMENT, "two work items expected");
+namespace {
+// Sort the work items of a persistent pass by element type: heavy = Hexa20 3x3x3 and light = Quad8
+// 2x2, both total-Lagrangian Neo-Hooke.
+int32_t persistent_items(const EfeWorkItem* items, int32_t nItems, int32_t kPrecision, int32_t* status,
+                         efe::GroupArgs* heavy, int& nHeavy, efe::GroupArgs* light, int& nLight) {
+  nHeavy = nLight = 0;
+  if (!items || nItems < 1 || !status) return fail(EFE_ERR_ARGUMENT, "work items and a status word expected");
   if (kPrecision != EFE_K_FP64 && kPrecision != EFE_K_FP32) return fail(EFE_ERR_ARGUMENT, "unknown K precision");
-  efe::GroupArgs args[2];
-  int forms[2];
-  for (int i = 0; i < 2; ++i) {
+  for (int32_t i = 0; i < nItems; ++i) {
     const EfeWorkItem& it = items[i];
-    if (!it.mesh || !it.group || !it.Kdata || !it.P || !it.F) return fail(EFE_ERR_ARGUMENT, "null work item buffer");
+    if (!it.mesh || !it.group || !it.P || !it.F || (!it.Kdata && it.mesh->nnz > 0))
+      return fail(EFE_ERR_ARGUMENT, "null work item buffer");
     int32_t rc = check_group(it.mesh, *it.group);
     if (rc) return rc;
     rc = check_item_buffers(*it.group, it.U, it.dU);
     if (rc) return rc;
-    args[i] = make_args(it.mesh, *it.group, it.U, it.dU, it.Kdata, it.P, it.F, status);
-    forms[i] = form_of(*it.group);
+    const EfeGroup& g = *it.group;
+    const int form = form_of(g);
+    const bool h = g.shape == EFE_HEXA20 && g.rule == EFE_RULE_3D_3X3X3 && form == efe::TLH;
+    const bool l = g.shape == EFE_QUAD8 && g.rule == EFE_RULE_2D_2X2 && form == efe::TLH;
+    if (!h && !l)
+      return fail(EFE_ERR_UNSUPPORTED, "no persistent kernel for this element type (implemented: Hexa20 3x3x3 and "
+                                       "Quad8 2x2, total-Lagrangian Neo-Hooke)");
+    int& n = h ? nHeavy : nLight;
+    if (n == efe::MAX_PERSISTENT_GROUPS)
+      return fail(EFE_ERR_ARGUMENT, "at most " + std::to_string(efe::MAX_PERSISTENT_GROUPS) +
+                                        " groups of each element type in one persistent pass");
+    (h ? heavy : light)[n++] = make_args(it.mesh, g, it.U, it.dU, it.Kdata, it.P, it.F, status);
   }
-  cudaError_t e = efe::persistent_pair(items[0].group->shape, items[0].group->rule, forms[0], items[1].group->shape,
-                                       items[1].group->rule, forms[1], kPrecision, args[0], args[1],
-                                       (unsigned long long*)workCounter, (cudaStream_t)stream);
-  if (e == cudaErrorNotSupported)
-    return fail(EFE_ERR_UNSUPPORTED, "no persistent kernel for this pair of element types");
+  return EFE_OK;
+}
+}  // namespace
+
+int32_t efe_compute_elements_persistent(const EfeWorkItem* items, int32_t nItems, int32_t kPrecision,
+                                        uint64_t* workCounter, int32_t* status, void* stream) {
+  if (!workCounter) return fail(EFE_ERR_ARGUMENT, "null work counter");
+  efe::GroupArgs heavy[efe::MAX_PERSISTENT_GROUPS], light[efe::MAX_PERSISTENT_GROUPS];
+  int nHeavy = 0, nLight = 0;
+  int32_t rc = persistent_items(items, nItems, kPrecision, status, heavy, nHeavy, light, nLight);
+  if (rc) return rc;
+  cudaError_t e = efe::persistent_groups(kPrecision, heavy, nHeavy, light, nLight, (unsigned long long*)workCounter,
+                                         (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "efe_compute_elements_persistent");
   return EFE_OK;
 }
@@ -438,26 +459,13 @@ int32_t efe_compute_elements_persistent(const EfeWorkItem* items, int32_t nItems
 // library's static scratch array (efe_batch.cu), so nothing here allocates device memory.
 int32_t efe_compute_elements_persistent_noalloc(const EfeWorkItem* items, int32_t nItems, int32_t kPrecision,
                                                 int32_t* status, void* stream) {
-  if (!items || nItems != 2 || !status) return fail(EFE_ERR_ARGUMENT, "two work items expected");
-  if (kPrecision != EFE_K_FP64 && kPrecision != EFE_K_FP32) return fail(EFE_ERR_ARGUMENT, "unknown K precision");
-  efe::GroupArgs args[2];
-  int forms[2];
-  for (int i = 0; i < 2; ++i) {
-    const EfeWorkItem& it = items[i];
-    if (!it.mesh || !it.group || !it.Kdata || !it.P || !it.F) return fail(EFE_ERR_ARGUMENT, "null work item buffer");
-    int32_t rc = check_group(it.mesh, *it.group);
-    if (rc) return rc;
-    rc = check_item_buffers(*it.group, it.U, it.dU);
-    if (rc) return rc;
-    args[i] = make_args(it.mesh, *it.group, it.U, it.dU, it.Kdata, it.P, it.F, status);
-    forms[i] = form_of(*it.group);
-  }
+  efe::GroupArgs heavy[efe::MAX_PERSISTENT_GROUPS], light[efe::MAX_PERSISTENT_GROUPS];
+  int nHeavy = 0, nLight = 0;
+  int32_t rc = persistent_items(items, nItems, kPrecision, status, heavy, nHeavy, light, nLight);
+  if (rc) return rc;
   int64_t needed = 0;
-  cudaError_t e = efe::persistent_pair_noalloc(items[0].group->shape, items[0].group->rule, forms[0],
-                                               items[1].group->shape, items[1].group->rule, forms[1], kPrecision,
-                                               args[0], args[1], &needed, (cudaStream_t)stream);
-  if (e == cudaErrorNotSupported)
-    return fail(EFE_ERR_UNSUPPORTED, "no persistent kernel for this pair of element types");
+  cudaError_t e =
+      efe::persistent_groups_noalloc(kPrecision, heavy, nHeavy, light, nLight, &needed, (cudaStream_t)stream);
   if (needed > EFE_NOALLOC_MAX_TILES) {
     return fail(EFE_ERR_ARGUMENT, "efe_compute_elements_persistent_noalloc: the batch needs " + std::to_string(needed) +
                                       " tile indices, the 32-bit work counter in the static scratch allows at most " +

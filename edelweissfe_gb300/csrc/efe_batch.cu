@@ -1,5 +1,5 @@
-// efe_batch.cu -- persistent launch over two element groups (uneven batches of meshes), and its
-// variant for callers that cannot allocate device memory.
+// efe_batch.cu -- persistent launch over several element groups of two types (uneven batches of
+// meshes), and its variant for callers that cannot allocate device memory.
 #include <mutex>
 
 #include "efe_launch.cuh"
@@ -8,15 +8,32 @@ namespace efe {
 
 namespace {
 
-template <int SA, int RA, int FA, int SB, int RB, int FB, typename KT, typename CT>
-cudaError_t run_pair(const GroupArgs& a, const GroupArgs& b, CT* counter, int64_t maxTiles, int64_t* needed,
-                     cudaStream_t st) {
-  using TA = Tile<SA, RA, FA, KT>;
-  using TB = Tile<SB, RB, FB, KT>;
+// Fill a group table: group k owns ceil(nElements / EPB) tiles.
+template <int EPB>
+void fill_table(GroupTable& t, const GroupArgs* g, int n) {
+  t = GroupTable{};
+  t.n = n;
+  t.tileStart[0] = 0;
+  for (int k = 0; k < MAX_PERSISTENT_GROUPS; ++k) {
+    if (k < n) t.g[k] = g[k];
+    t.tileStart[k + 1] = t.tileStart[k] + (k < n ? (g[k].nElements + EPB - 1) / EPB : 0);
+  }
+}
+
+// heavy: Hexa20 3x3x3 total-Lagrangian Neo-Hooke groups, light: Quad8 2x2 total-Lagrangian
+// Neo-Hooke groups; the heavier tiles are handed out first
+template <typename KT, typename CT>
+cudaError_t run_groups(const GroupArgs* heavy, int nHeavy, const GroupArgs* light, int nLight, CT* counter,
+                       int64_t maxTiles, int64_t* needed, cudaStream_t st) {
+  constexpr int SA = EFE_HEXA20, RA = EFE_RULE_3D_3X3X3, SB = EFE_QUAD8, RB = EFE_RULE_2D_2X2;
+  using TA = Tile<SA, RA, TLH, KT>;
+  using TB = Tile<SB, RB, TLH, KT>;
   static_assert(TA::NT == TB::NT, "both tile types must use the same CTA size");
   constexpr int NT = TA::NT;
   constexpr size_t bytes = TA::bytes > TB::bytes ? TA::bytes : TB::bytes;
-  auto kern = assemble_persistent_kernel<SA, RA, FA, TA::EPB, SB, RB, FB, TB::EPB, KT, NT, CT>;
+  if (nHeavy < 0 || nLight < 0 || nHeavy > MAX_PERSISTENT_GROUPS || nLight > MAX_PERSISTENT_GROUPS)
+    return cudaErrorInvalidValue;
+  auto kern = assemble_persistent_kernel<SA, RA, TLH, TA::EPB, SB, RB, TLH, TB::EPB, KT, NT, CT>;
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (err != cudaSuccess) return err;
   int dev = 0, sms = 0, perSM = 0;
@@ -24,8 +41,10 @@ cudaError_t run_pair(const GroupArgs& a, const GroupArgs& b, CT* counter, int64_
   if ((err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return err;
   if ((err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, NT, bytes)) != cudaSuccess) return err;
   if (perSM < 1) return cudaErrorInvalidConfiguration;
-  const int64_t tilesA = (a.nElements + TA::EPB - 1) / TA::EPB;
-  const int64_t tilesB = (b.nElements + TB::EPB - 1) / TB::EPB;
+  GroupTable ta, tb;
+  fill_table<TA::EPB>(ta, heavy, nHeavy);
+  fill_table<TB::EPB>(tb, light, nLight);
+  const int64_t tilesA = ta.tileStart[nHeavy], tilesB = tb.tileStart[nLight];
   int64_t grid = (int64_t)sms * perSM;
   if (grid > tilesA + tilesB) grid = tilesA + tilesB;
   // the counter ends at tilesA + tilesB + grid (every CTA takes one tile index past the end)
@@ -33,41 +52,23 @@ cudaError_t run_pair(const GroupArgs& a, const GroupArgs& b, CT* counter, int64_
   if (tilesA + tilesB + grid > maxTiles) return cudaErrorInvalidValue;
   if ((err = cudaMemsetAsync(counter, 0, sizeof(CT), st)) != cudaSuccess) return err;
   if (grid == 0) return cudaSuccess;
-  kern<<<(unsigned)grid, NT, bytes, st>>>(a, b, tilesA, tilesB, counter);
+  kern<<<(unsigned)grid, NT, bytes, st>>>(ta, tb, counter);
   return cudaGetLastError();
 }
 
-template <typename KT, typename CT>
-cudaError_t dispatch(int shapeA, int ruleA, int formA, int shapeB, int ruleB, int formB, const GroupArgs& a,
-                     const GroupArgs& b, CT* counter, int64_t maxTiles, int64_t* needed, cudaStream_t st) {
-  const bool aH20 = shapeA == EFE_HEXA20 && ruleA == EFE_RULE_3D_3X3X3 && formA == TLH;
-  const bool bQ8 = shapeB == EFE_QUAD8 && ruleB == EFE_RULE_2D_2X2 && formB == TLH;
-  const bool aQ8 = shapeA == EFE_QUAD8 && ruleA == EFE_RULE_2D_2X2 && formA == TLH;
-  const bool bH20 = shapeB == EFE_HEXA20 && ruleB == EFE_RULE_3D_3X3X3 && formB == TLH;
-  // the heavier Hexa20 tiles are handed out first
-  if (aH20 && bQ8)
-    return run_pair<EFE_HEXA20, EFE_RULE_3D_3X3X3, TLH, EFE_QUAD8, EFE_RULE_2D_2X2, TLH, KT>(a, b, counter, maxTiles,
-                                                                                             needed, st);
-  if (aQ8 && bH20)
-    return run_pair<EFE_HEXA20, EFE_RULE_3D_3X3X3, TLH, EFE_QUAD8, EFE_RULE_2D_2X2, TLH, KT>(b, a, counter, maxTiles,
-                                                                                             needed, st);
-  return cudaErrorNotSupported;
-}
-
 template <typename CT>
-cudaError_t persistent_pair_t(int shapeA, int ruleA, int formA, int shapeB, int ruleB, int formB, int kprec,
-                              const GroupArgs& a, const GroupArgs& b, CT* counter, int64_t maxTiles, int64_t* needed,
-                              cudaStream_t st) {
+cudaError_t persistent_groups_t(int kprec, const GroupArgs* heavy, int nHeavy, const GroupArgs* light, int nLight,
+                                CT* counter, int64_t maxTiles, int64_t* needed, cudaStream_t st) {
   if (kprec == EFE_K_FP32)
-    return dispatch<float>(shapeA, ruleA, formA, shapeB, ruleB, formB, a, b, counter, maxTiles, needed, st);
-  return dispatch<double>(shapeA, ruleA, formA, shapeB, ruleB, formB, a, b, counter, maxTiles, needed, st);
+    return run_groups<float>(heavy, nHeavy, light, nLight, counter, maxTiles, needed, st);
+  return run_groups<double>(heavy, nHeavy, light, nLight, counter, maxTiles, needed, st);
 }
 
 }  // namespace
 
-cudaError_t persistent_pair(int shapeA, int ruleA, int formA, int shapeB, int ruleB, int formB, int kprec,
-                            const GroupArgs& a, const GroupArgs& b, unsigned long long* counter, cudaStream_t st) {
-  return persistent_pair_t(shapeA, ruleA, formA, shapeB, ruleB, formB, kprec, a, b, counter, INT64_MAX, nullptr, st);
+cudaError_t persistent_groups(int kprec, const GroupArgs* heavy, int nHeavy, const GroupArgs* light, int nLight,
+                              unsigned long long* counter, cudaStream_t st) {
+  return persistent_groups_t(kprec, heavy, nHeavy, light, nLight, counter, INT64_MAX, nullptr, st);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -109,13 +110,12 @@ cudaError_t noalloc_scratch_address(unsigned int** out) {
 
 }  // namespace
 
-cudaError_t persistent_pair_noalloc(int shapeA, int ruleA, int formA, int shapeB, int ruleB, int formB, int kprec,
-                                    const GroupArgs& a, const GroupArgs& b, int64_t* needed, cudaStream_t st) {
+cudaError_t persistent_groups_noalloc(int kprec, const GroupArgs* heavy, int nHeavy, const GroupArgs* light,
+                                      int nLight, int64_t* needed, cudaStream_t st) {
   unsigned int* counter = nullptr;
   cudaError_t err = noalloc_scratch_address(&counter);
   if (err != cudaSuccess) return err;
-  return persistent_pair_t(shapeA, ruleA, formA, shapeB, ruleB, formB, kprec, a, b, counter,
-                           (int64_t)EFE_NOALLOC_MAX_TILES, needed, st);
+  return persistent_groups_t(kprec, heavy, nHeavy, light, nLight, counter, (int64_t)EFE_NOALLOC_MAX_TILES, needed, st);
 }
 
 }  // namespace efe

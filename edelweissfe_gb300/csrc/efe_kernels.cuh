@@ -825,25 +825,42 @@ __global__ void __launch_bounds__(NT, MINB) assemble_kernel(GroupArgs g) {
   assemble_tile<SHAPE, RULE, FORM, KT, EPB, NT, FF>(g, (int64_t)blockIdx.x * EPB, smem);
 }
 
-// Persistent form: a grid sized to the resident CTAs pulls tiles of two element types from one
-// work counter (scratch, zeroed before the launch), heavier type first, until both are done.
+// Groups of one element type for the persistent pass: group k owns the tiles
+// [tileStart[k], tileStart[k+1]) of its type.  Passed by value (kernel parameters).
+constexpr int MAX_PERSISTENT_GROUPS = EFE_PERSISTENT_MAX_GROUPS;
+struct GroupTable {
+  GroupArgs g[MAX_PERSISTENT_GROUPS];
+  int64_t tileStart[MAX_PERSISTENT_GROUPS + 1];
+  int n;
+};
+
+// Persistent form: a grid sized to the resident CTAs pulls tiles of up to MAX_PERSISTENT_GROUPS groups
+// of each of two element types from one work counter (scratch, zeroed before the launch), the
+// heavier type first, until all are done.
 template <int SA, int RA, int FA, int EA, int SB, int RB, int FB, int EB, typename KT, int NT,
           typename CT = unsigned long long>
 __global__ void __launch_bounds__(NT, 1)
-    assemble_persistent_kernel(GroupArgs ga, GroupArgs gb, int64_t tilesA, int64_t tilesB, CT* counter) {
+    assemble_persistent_kernel(GroupTable ta, GroupTable tb, CT* counter) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ long long tile;
+  const long long tilesA = ta.tileStart[ta.n], tilesB = tb.tileStart[tb.n];
   while (true) {
     if (threadIdx.x == 0) tile = (long long)atomicAdd(counter, (CT)1);
     __syncthreads();
     const long long t = tile;
     __syncthreads();
-    if (t < tilesA)
-      assemble_tile<SA, RA, FA, KT, EA, NT, false>(ga, (int64_t)t * EA, smem);
-    else if (t < tilesA + tilesB)
-      assemble_tile<SB, RB, FB, KT, EB, NT, false>(gb, (int64_t)(t - tilesA) * EB, smem);
-    else
+    if (t < tilesA) {
+      int k = 0;
+      while (t >= ta.tileStart[k + 1]) ++k;
+      assemble_tile<SA, RA, FA, KT, EA, NT, false>(ta.g[k], (int64_t)(t - ta.tileStart[k]) * EA, smem);
+    } else if (t < tilesA + tilesB) {
+      const long long u = t - tilesA;
+      int k = 0;
+      while (u >= tb.tileStart[k + 1]) ++k;
+      assemble_tile<SB, RB, FB, KT, EB, NT, false>(tb.g[k], (int64_t)(u - tb.tileStart[k]) * EB, smem);
+    } else {
       break;
+    }
     __syncthreads();
   }
 }

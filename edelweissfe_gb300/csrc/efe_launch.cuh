@@ -154,12 +154,14 @@ EFE_BODY_DECL(quad8)
 EFE_BODY_DECL(hexa8)
 EFE_BODY_DECL(hexa20)
 #undef EFE_BODY_DECL
-cudaError_t persistent_pair(int shapeA, int ruleA, int formA, int shapeB, int ruleB, int formB, int kprec,
-                            const GroupArgs& a, const GroupArgs& b, unsigned long long* counter, cudaStream_t st);
+// the persistent pass over up to MAX_PERSISTENT_GROUPS groups of each of its two element types
+// (heavy: Hexa20 3x3x3 total-Lagrangian Neo-Hooke; light: Quad8 2x2 total-Lagrangian Neo-Hooke)
+cudaError_t persistent_groups(int kprec, const GroupArgs* heavy, int nHeavy, const GroupArgs* light, int nLight,
+                              unsigned long long* counter, cudaStream_t st);
 // same pass with the work counter in the library's static scratch array; *needed = tile indices
 // the counter runs through (written before the range check)
-cudaError_t persistent_pair_noalloc(int shapeA, int ruleA, int formA, int shapeB, int ruleB, int formB, int kprec,
-                                    const GroupArgs& a, const GroupArgs& b, int64_t* needed, cudaStream_t st);
+cudaError_t persistent_groups_noalloc(int kprec, const GroupArgs* heavy, int nHeavy, const GroupArgs* light,
+                                      int nLight, int64_t* needed, cudaStream_t st);
 // device linear solve (efe_solve.cu)
 cudaError_t csr_spmv(const EfePcg& s, const double* x, double* y, cudaStream_t st);
 cudaError_t pcg_start(const EfePcg& s, const double* b, cudaStream_t st);

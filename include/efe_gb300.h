@@ -203,12 +203,14 @@ int32_t efe_adjoint_small_strain(const EfeMesh* mesh, const EfeGroup* group, con
                                  const double* dU, const double* Pbar, const double* stateBarIn, double* stateBarOut,
                                  double* dUbar, double* gProps, void* stream);
 
-/* The element pass of two groups, possibly of different meshes and dimensions (e.g. a batch of
-   2D meshes and a batch of 3D meshes), in ONE persistent launch: the resident CTAs take tiles of
-   both groups from the work counter until both are done (same results as efe_compute_elements on
-   each item).  workCounter: one device uint64 of scratch, zeroed by this call.  Implemented for
-   the pair (Hexa20 3x3x3, Quad8 2x2) total-Lagrangian Neo-Hooke in either order and precision
-   EFE_K_FP64 / EFE_K_FP32; other pairs return EFE_ERR_UNSUPPORTED. */
+/* The element pass of several groups, possibly of different meshes and dimensions (e.g. batches of
+   2D meshes and batches of 3D meshes), in ONE persistent launch: the resident CTAs take tiles of all
+   groups from the work counter until all are done (same results as efe_compute_elements on each
+   item).  workCounter: one device uint64 of scratch, zeroed by this call.  Implemented for up to
+   EFE_PERSISTENT_MAX_GROUPS groups of each of the types Hexa20 3x3x3 and Quad8 2x2, total-Lagrangian
+   Neo-Hooke, in any order, precision EFE_K_FP64 / EFE_K_FP32; other types return
+   EFE_ERR_UNSUPPORTED. */
+#define EFE_PERSISTENT_MAX_GROUPS 8
 int32_t efe_compute_elements_persistent(const EfeWorkItem* items, int32_t nItems, int32_t kPrecision,
                                         uint64_t* workCounter, int32_t* status, void* stream);
 

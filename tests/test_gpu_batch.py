@@ -88,3 +88,42 @@ def test_batched_pass_matches_single_meshes(precision):
     for k, b in enumerate((b2, b3)):
         assert _rel(b.P.cpu().numpy(), results["persistent"][k][0]) <= 1e-12
         assert _rel(b.K.double().cpu().numpy(), results["persistent"][k][2]) <= ktol
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_persistent_pass_over_many_batches(precision):
+    """Five batches (three Hexa20, two Quad8) in ONE persistent launch give the per-batch results; a
+    CUDA-graph replay of it too; a batch of another element type is refused."""
+    from edelweissfe_gb300 import meshes
+    from edelweissfe_gb300.batch import BatchedPass, MeshBatch, persistent_capable
+
+    m2, m3 = _meshes(4)
+    m3 = m3 + _meshes(5)[1]
+    groups = [(m3[:1], "C3D20TL"), (m3[1:3], "C3D20TL"), (m3[3:], "C3D20TL"), (m2[:2], "CPE8RTL"),
+              (m2[2:], "CPE8RTL")]  # fmt: skip
+    batches = []
+    for ms, et in groups:
+        b = MeshBatch(ms, et, "neohookewa", precision)
+        b.U.copy_(torch.tensor(np.concatenate([m["U"] for m in ms])))
+        batches.append(b)
+    ktol = 1e-12 if precision == "fp64" else 2e-6
+    out = {}
+    for mode in ("perbatch", "persistent", "graph"):
+        bp = BatchedPass(batches, persistent=(mode != "perbatch"))
+        assert bp.persistent == (mode != "perbatch")
+        if mode == "graph":
+            bp.capture()
+            bp.replay()
+        else:
+            bp.step()
+        torch.cuda.synchronize()
+        bp.check_status()
+        out[mode] = [(b.P.cpu().numpy().copy(), b.K.double().cpu().numpy().copy()) for b in batches]
+    for mode in ("persistent", "graph"):
+        for (P, K), (Pr, Kr) in zip(out[mode], out["perbatch"]):
+            assert _rel(P, Pr) <= 1e-12 and _rel(K, Kr) <= ktol, mode
+    coords, conn, nodeDof, nDof = meshes.box(2, 2, 1, nNodes=8)
+    other = MeshBatch([dict(coords=coords, conn=conn, nodeDof=nodeDof, nDof=nDof, props=[100.0, 1000.0])],
+                      "C3D8TL", "neohookewa", precision)  # fmt: skip
+    assert not persistent_capable(batches + [other])
+    assert BatchedPass(batches + [other], persistent=True).persistent is False

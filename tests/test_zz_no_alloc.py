@@ -59,7 +59,7 @@ def test_noalloc_rejects_bad_arguments_without_a_gpu():
     except (RuntimeError, OSError) as e:
         pytest.skip(f"library not built: {e}")
     assert lib.efe_compute_elements_persistent_noalloc(None, 2, L.EFE_K_FP64, None, None) == L.EFE_ERR_ARGUMENT
-    assert b"two work items" in lib.efe_last_error()
+    assert b"work items" in lib.efe_last_error()
     items = (L.EfeWorkItem * 2)()
     status = (ctypes.c_int32 * 4)()
     rc = lib.efe_compute_elements_persistent_noalloc(items, 2, 7, ctypes.addressof(status), None)
