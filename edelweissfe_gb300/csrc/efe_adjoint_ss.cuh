@@ -48,7 +48,8 @@ __device__ inline void hypo3d_reverse(const VMConst& c, double E, double nu, boo
     const double sq23 = sqrt(2.0 / 3.0), sq6 = sqrt(6.0);
     const double fy_k0 = c.fy0 + c.H * k0 + vm_sat(c, k0);
     if (q - sq23 * fy_k0 > 0.0) {
-      // the forward's scalar Newton, step for step, for the same converged dK
+      // the scalar Newton of the FP64 form of the forward pass, step for step (the FP32-tangent form
+      // forms 1/|dev| and the step with reciprocals: its dK differs by rounding, immaterial here)
       double dK = 0.0;
       for (int counter = 0;; ++counter) {
         const double k = k0 + dK;

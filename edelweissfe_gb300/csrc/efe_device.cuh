@@ -275,6 +275,7 @@ struct VMConst {
   Iso Ei;
   double G, fy0, H, dfy, delta;
   double tfac;  // 1 / (1 + H / (3G)): the tangent factor of vonmises.py:247 when dfy == 0
+  double invdR; // 1 / (dR/d dK) of the return-map residual, constant per element when dfy == 0
 };
 __device__ __forceinline__ VMConst vm_const(const double* props, bool vonMises) {
   VMConst c;
@@ -285,8 +286,10 @@ __device__ __forceinline__ VMConst vm_const(const double* props, bool vonMises) 
   c.dfy = vonMises ? props[4] : 0.0;
   c.delta = vonMises ? props[5] : 0.0;
   c.tfac = 1.0 / (1.0 + c.H / (3.0 * c.G));
+  c.invdR = 1.0 / (-sqrt(6.0) * c.G - sqrt(2.0 / 3.0) * c.H);
   return c;
 }
+
 // dfy * (1 - exp(-delta k)); identical to the reference's expression, and exactly 0 when dfy == 0
 __device__ __forceinline__ double vm_sat(const VMConst& c, double k) {
   return c.dfy == 0.0 ? 0.0 : c.dfy * (1.0 - exp(-c.delta * k));
@@ -295,8 +298,27 @@ __device__ __forceinline__ double vm_dsat(const VMConst& c, double k) {
   return c.dfy == 0.0 ? 0.0 : c.dfy * c.delta * exp(-c.delta * k);
 }
 
+// |dev| with the shear terms doubled (vonmises.py:63-64) and its reciprocal from one reciprocal
+// square root (0 and inf for a zero deviator)
+__device__ __forceinline__ void vm_dev_norm(const double dev[6], double& norm, double& inv) {
+  const double q2 =
+      dev[0] * dev[0] + dev[1] * dev[1] + dev[2] * dev[2] + 2.0 * (dev[3] * dev[3] + dev[4] * dev[4] + dev[5] * dev[5]);
+  inv = rsqrt(q2);
+  norm = q2 > 0.0 ? q2 * inv : 0.0;
+}
+// Newton step of the return map: R / dR (the derivative is constant per element for linear hardening)
+__device__ __forceinline__ double vm_newton_step(const VMConst& c, double R, double k) {
+  if (c.dfy == 0.0) return R * c.invdR;
+  const double dR = -sqrt(6.0) * c.G - sqrt(2.0 / 3.0) * (c.H + vm_dsat(c, k));
+  return R / dR;
+}
+
 // von Mises radial return (vonmises.py:186-254).  Updates sig and kappa in place.
 // Returns false when the scalar Newton does not converge in 15 iterations (CutbackRequest).
+// FAST (used with an FP32 tangent): |dev| and 1/|dev| from one rsqrt and the Newton step as a product
+// with the per-element 1/dR; otherwise the reference's sqrt and divisions, whose rounding the FP64
+// mode keeps so that rounding-critical return maps fail (cut back) exactly where the reference's do.
+template <bool FAST = false>
 __device__ inline bool von_mises_3d(const VMConst& c, double sig[6], const double de[6], double& kappa, Tangent3& T) {
   const Iso& Ei = c.Ei;
   T.c11 = Ei.c11;
@@ -319,8 +341,14 @@ __device__ inline bool von_mises_3d(const VMConst& c, double sig[6], const doubl
   dev[3] = tr[3];
   dev[4] = tr[4];
   dev[5] = tr[5];
-  const double devNorm =
-      sqrt(dev[0] * dev[0] + dev[1] * dev[1] + dev[2] * dev[2] + 2.0 * (dev[3] * dev[3] + dev[4] * dev[4] + dev[5] * dev[5]));
+  double devNorm, inv;
+  if constexpr (FAST) {
+    vm_dev_norm(dev, devNorm, inv);
+  } else {
+    devNorm = sqrt(dev[0] * dev[0] + dev[1] * dev[1] + dev[2] * dev[2] +
+                   2.0 * (dev[3] * dev[3] + dev[4] * dev[4] + dev[5] * dev[5]));
+    inv = 1.0 / devNorm;
+  }
   const double k0 = kappa;
   const double sq23 = sqrt(2.0 / 3.0), sq6 = sqrt(6.0);
   const double fy_k0 = c.fy0 + c.H * k0 + vm_sat(c, k0);
@@ -336,13 +364,16 @@ __device__ inline bool von_mises_3d(const VMConst& c, double sig[6], const doubl
         ok = false;
         break;
       }
-      const double dR = -sq6 * G - sq23 * (c.H + vm_dsat(c, k));
-      dK -= R / dR;
+      if constexpr (FAST) {
+        dK -= vm_newton_step(c, R, k);
+      } else {
+        const double dR = -sq6 * G - sq23 * (c.H + vm_dsat(c, k));
+        dK -= R / dR;
+      }
       ++counter;
     }
     const double dLambda = sqrt(1.5) * dK;
     kappa = k0 + dK;
-    const double inv = 1.0 / devNorm;
     const double g2 = 2.0 * G * dLambda;
     for (int i = 0; i < 6; ++i) {
       T.n[i] = dev[i] * inv;
@@ -405,6 +436,7 @@ __device__ __forceinline__ void linear_elastic_plane_stress(const double* props,
 // local Newton on de[2]; every local step calls the 3D update with a zero stress vector and the
 // material state, so kappa accumulates the plastic increments of all local steps; the converged
 // 3D stress is added to sig.  Returns false on a cutback request.
+template <bool FAST = false>
 __device__ inline bool von_mises_plane_stress(const VMConst& vc, double sig[6], double de[6], double& kappa, Tangent2& C) {
   Tangent3 T;
   double s3[6];
@@ -413,7 +445,7 @@ __device__ inline bool von_mises_plane_stress(const VMConst& vc, double sig[6], 
   bool ok = true;
   while (true) {
     for (int i = 0; i < 6; ++i) s3[i] = 0.0;
-    if (!von_mises_3d(vc, s3, de, kappa, T)) {
+    if (!von_mises_3d<FAST>(vc, s3, de, kappa, T)) {
       ok = false;
       break;
     }

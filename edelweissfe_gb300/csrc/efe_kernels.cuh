@@ -186,6 +186,8 @@ template <int SHAPE, int RULE, int FORM, typename KT, int EPB, int NT, bool FF>
 __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t e0, unsigned char* smem) {
   using L = Layout<SHAPE, RULE, FORM, KT, EPB>;
   constexpr int DIM = L::DIM, NN = L::NN, NQ = L::NQ, NVEC = L::NVEC, NSCAL = L::NSCAL, NDOF = L::NDOF;
+  // the faster return-map arithmetic goes with the FP32 tangent (mixed modes)
+  constexpr bool FASTRM = std::is_same<KT, float>::value;
   double* su = reinterpret_cast<double*>(smem + L::u_off);
   double* sr = reinterpret_cast<double*>(smem + L::r_off);
   KT* ssc = reinterpret_cast<KT*>(smem + L::sc_off);
@@ -449,7 +451,7 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
       if constexpr (FORM == SS3) {
         Tangent3 T;
         if (g.material == EFE_MAT_VON_MISES)
-          ok = von_mises_3d(smc[le], sig, de, kappa, T);
+          ok = von_mises_3d<FASTRM>(smc[le], sig, de, kappa, T);
         else
           linear_elastic_3d(smc[le], sig, de, T);
         // residual r_a = s * sigma . G_a   (small-strain Voigt order 11,22,33,12,13,23)
@@ -515,13 +517,13 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
         Tangent2 C;
         if (g.plane == EFE_PLANE_STRESS) {
           if (g.material == EFE_MAT_VON_MISES)
-            ok = von_mises_plane_stress(smc[le], sig, de, kappa, C);
+            ok = von_mises_plane_stress<FASTRM>(smc[le], sig, de, kappa, C);
           else
             linear_elastic_plane_stress(props, sig, de, C);
         } else {
           Tangent3 T;
           if (g.material == EFE_MAT_VON_MISES)
-            ok = von_mises_3d(smc[le], sig, de, kappa, T);
+            ok = von_mises_3d<FASTRM>(smc[le], sig, de, kappa, T);
           else
             linear_elastic_3d(smc[le], sig, de, T);
           tangent2_from3(T, C);
@@ -590,7 +592,7 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
         if constexpr (FORM == TLV3) {
           Tangent3 T;
           if (g.material == EFE_MAT_VON_MISES)
-            ok = von_mises_3d(smc[le], sig, de, kappa, T);
+            ok = von_mises_3d<FASTRM>(smc[le], sig, de, kappa, T);
           else
             linear_elastic_3d(smc[le], sig, de, T);
           // TL Voigt order 11,22,33,12,23,13
@@ -622,13 +624,13 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
           Tangent2 C;
           if (g.plane == EFE_PLANE_STRESS) {
             if (g.material == EFE_MAT_VON_MISES)
-              ok = von_mises_plane_stress(smc[le], sig, de, kappa, C);
+              ok = von_mises_plane_stress<FASTRM>(smc[le], sig, de, kappa, C);
             else
               linear_elastic_plane_stress(props, sig, de, C);
           } else {
             Tangent3 T;
             if (g.material == EFE_MAT_VON_MISES)
-              ok = von_mises_3d(smc[le], sig, de, kappa, T);
+              ok = von_mises_3d<FASTRM>(smc[le], sig, de, kappa, T);
             else
               linear_elastic_3d(smc[le], sig, de, T);
             tangent2_from3(T, C);
