@@ -66,23 +66,22 @@ __global__ void adjoint_tl_kernel(int64_t nEl, const int32_t* __restrict__ conn,
   const double p[3] = {eta, xi, zeta};
   double D[DIM][NN];
   shape_derivatives<SHAPE>(p, D);
-  double X[NN][DIM], Ua[NN][DIM], La[NN][DIM];
-  for (int a = 0; a < NN; ++a) {
-    const int32_t n = conn[e * NN + a];
-    const int32_t dof = nodeDof[n];
-    for (int c = 0; c < DIM; ++c) {
-      X[a][c] = coords[(int64_t)n * DIM + c];
-      Ua[a][c] = U[dof + c];
-      La[a][c] = lam[dof + c];
-    }
-  }
+  // nodal coordinates, U and lambda are read where they are used (L1-resident) rather than held
+  // in registers across the whole point: fewer registers, no spills
+  const int32_t* en = conn + e * NN;
   // Jacobian table row 2 of Hexa20 carries (zeta - xi) * inv(A)[5] (the reference's _J3D20)
   const double quirk = (SHAPE == EFE_HEXA20) ? (zeta - xi) : 0.0;
   double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 1}};
   for (int r = 0; r < DIM; ++r)
     for (int c = 0; c < DIM; ++c) {
       double s = 0.0;
-      for (int a = 0; a < NN; ++a) s += (D[r][a] + (r == 2 ? quirk * fix.r[a % 20] : 0.0)) * X[a][c];
+      for (int a = 0; a < NN; ++a) {
+        double d = D[r][a];
+        if constexpr (SHAPE == EFE_HEXA20) {
+          if (r == 2) d += quirk * fix.r[a % 20];
+        }
+        s += d * coords[(int64_t)en[a] * DIM + c];
+      }
       J[r][c] = s;
     }
   double detJ, iJ[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 1}};
@@ -109,7 +108,7 @@ __global__ void adjoint_tl_kernel(int64_t nEl, const int32_t* __restrict__ conn,
   for (int i = 0; i < DIM; ++i)
     for (int j = 0; j < DIM; ++j) {
       double h = 0.0;
-      for (int a = 0; a < NN; ++a) h += Ua[a][i] * G[j][a];
+      for (int a = 0; a < NN; ++a) h += U[nodeDof[en[a]] + i] * G[j][a];
       F[i][j] += h;
     }
   const double Jf = det3(F);
@@ -122,7 +121,7 @@ __global__ void adjoint_tl_kernel(int64_t nEl, const int32_t* __restrict__ conn,
   for (int i = 0; i < DIM; ++i)
     for (int k = 0; k < DIM; ++k) {
       double v = 0.0;
-      for (int a = 0; a < NN; ++a) v += La[a][i] * G[k][a];
+      for (int a = 0; a < NN; ++a) v += lam[nodeDof[en[a]] + i] * G[k][a];
       Lam[i][k] = v;
     }
   double M[3][3];
@@ -171,12 +170,14 @@ __global__ void adjoint_tl_kernel(int64_t nEl, const int32_t* __restrict__ conn,
   const double sbar = -phi;
   // Gbar[k][a] = sum_i Fbar[i][k] U[a][i] + Lbar[i][k] lambda[a][i]
   double Gbar[DIM][NN];
-  for (int k = 0; k < DIM; ++k)
-    for (int a = 0; a < NN; ++a) {
+  for (int a = 0; a < NN; ++a) {
+    const int32_t dof = nodeDof[en[a]];
+    for (int k = 0; k < DIM; ++k) {
       double v = 0.0;
-      for (int i = 0; i < DIM; ++i) v += Fbar[i][k] * Ua[a][i] + Lbar[i][k] * La[a][i];
+      for (int i = 0; i < DIM; ++i) v += Fbar[i][k] * U[dof + i] + Lbar[i][k] * lam[dof + i];
       Gbar[k][a] = v;
     }
+  }
   // G = iJ D: iJbar[c][r] = sum_a Gbar[c][a] D[r][a]
   double iJbar[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
   for (int c = 0; c < DIM; ++c)
@@ -185,20 +186,33 @@ __global__ void adjoint_tl_kernel(int64_t nEl, const int32_t* __restrict__ conn,
       for (int a = 0; a < NN; ++a) v += Gbar[c][a] * D[r][a];
       iJbar[c][r] = v;
     }
-  // Jbar = -iJ^T iJbar iJ^T + sbar * w * t * detJ * iJ^T
+  // Jbar = -iJ^T iJbar iJ^T + sbar * w * t * detJ * iJ^T, as two 3x3 products (A = iJ^T iJbar first)
+  double A[3][3];
+  for (int r = 0; r < DIM; ++r)
+    for (int l = 0; l < DIM; ++l) {
+      double v = 0.0;
+      for (int k = 0; k < DIM; ++k) v += iJ[k][r] * iJbar[k][l];
+      A[r][l] = v;
+    }
+  const double sdet = sbar * w * th * detJ;
   double Jbar[3][3];
   for (int r = 0; r < DIM; ++r)
     for (int c = 0; c < DIM; ++c) {
       double v = 0.0;
-      for (int k = 0; k < DIM; ++k)
-        for (int l = 0; l < DIM; ++l) v += iJ[k][r] * iJbar[k][l] * iJ[c][l];
-      Jbar[r][c] = -v + sbar * w * th * detJ * iJ[c][r];
+      for (int l = 0; l < DIM; ++l) v += A[r][l] * iJ[c][l];
+      Jbar[r][c] = -v + sdet * iJ[c][r];
     }
   for (int a = 0; a < NN; ++a) {
-    const int32_t n = conn[e * NN + a];
+    const int32_t n = en[a];
     for (int c = 0; c < DIM; ++c) {
       double v = 0.0;
-      for (int r = 0; r < DIM; ++r) v += Jbar[r][c] * (D[r][a] + (r == 2 ? quirk * fix.r[a % 20] : 0.0));
+      for (int r = 0; r < DIM; ++r) {
+        double d = D[r][a];
+        if constexpr (SHAPE == EFE_HEXA20) {
+          if (r == 2) d += quirk * fix.r[a % 20];
+        }
+        v += Jbar[r][c] * d;
+      }
       atomicAdd(gX + (int64_t)n * DIM + c, v);
     }
   }
