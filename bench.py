@@ -121,15 +121,20 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(name):
-    """DRAM bytes per launch from the committed ncu summary (profiles/<name>.txt), or None."""
+def ncu_value(name, key):
+    """A figure recorded as `key: value` in the committed ncu summary profiles/<name>.txt, or None."""
     p = os.path.join(ROOT, "profiles", name + ".txt")
     if not os.path.exists(p):
         return None
     for line in open(p):
-        if line.startswith("traffic_bytes_per_launch_full_size:"):
+        if line.startswith(key + ":"):
             return float(line.split(":")[1])
     return None
+
+
+def ncu_traffic(name):
+    """DRAM bytes per launch from the committed ncu summary (profiles/<name>.txt), or None."""
+    return ncu_value(name, "traffic_bytes_per_launch_full_size")
 
 
 # ------------------------------------------------------------------ shared measurement helpers
@@ -956,6 +961,8 @@ def main():
             "peak_kind": peak_kind,
             "algorithmic_bytes_per_launch": abytes,
             "kernel_ms": mixed["kernel_ms"],
+            # what binds instead: FP64 issue (ncu, the same kernel on a 40^3 case)
+            "fp64_pipe_active_pct": ncu_value("assemble_c3d8_vm_64cube", "fp64_pipe_active_pct"),
         },
         "cpu_baseline": cpu,
         "e2e": {
