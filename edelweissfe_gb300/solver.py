@@ -377,9 +377,9 @@ class NISTGPU:
                 step = min(10, self.pcgMaxIter - k)
                 L.check(lib.efe_pcg_iterate(ctypes.byref(s), k, step, stream), "efe_pcg_iterate")
                 k += step
-                rr = float(work[2])
+                rr, pAp = work[2:4].tolist()  # one device-to-host read per batch of iterations
                 if not rr <= tol2:
-                    if rr != rr or float(work[3]) == 0.0:  # NaN or a breakdown (p.Ap = 0)
+                    if rr != rr or pAp == 0.0:  # NaN or a breakdown (p.Ap = 0)
                         break
                     continue
                 break
