@@ -485,7 +485,7 @@ def run_batched(args):
     batches = []
     for ms, et in ((m3, "C3D20TL"), (m2, "CPE8RTL")):
         for chunk in chunk_meshes(ms, et):
-            b = MeshBatch(chunk, et, "neohookewa", "mixed", keep_host_pattern=False)
+            b = MeshBatch(chunk, et, "neohookewa", args.batch_precision, keep_host_pattern=False)
             b.U.copy_(torch.tensor(np.concatenate([m["U"] for m in chunk])))
             batches.append(b)
     setup_s = time.perf_counter() - t0
@@ -523,7 +523,9 @@ def run_batched(args):
         "metric": "assembled elem/s (K+R), batched uneven meshes, one CUDA graph (persistent or per-batch launches, "
                   "autotuned)",
         "value": nEl / (ms * 1e-3), "unit": "elem/s", "ms_per_step": ms, "steps": args.steps, "warmup": args.warmup,
-        "dtype": "f64 residual/state + f32 tangent (mixed)", "data": "synthetic",
+        "dtype": {"mixed": "f64 residual/state + f32 tangent (mixed)", "fp64": "f64",
+                  "mixed-ff": "float-float F / residual, f64 Kirchhoff stress and state, f32 tangent (mixed-ff)"}[
+            args.batch_precision], "data": "synthetic",
         "config": {"workload": f"{args.batch_meshes} meshes, sizes log-uniform [1e3, 5e4] x {args.batch_scale}: "
                                "CPE8RTL + C3D20TL Neo-Hooke (a)",
                    "elements_quad8": n2, "elements_hexa20": nEl - n2, "meshes_2d": len(m2),
@@ -884,6 +886,8 @@ def main():
     ap.add_argument("--fd-directions", type=int, default=3)
     ap.add_argument("--batch-meshes", type=int, default=512)
     ap.add_argument("--batch-scale", type=float, default=1.0)
+    ap.add_argument("--batch-precision", default="mixed", choices=["mixed", "mixed-ff", "fp64"],
+                    help="batched workload: tangent/residual precision (mixed-ff: per-batch launches)")
     ap.add_argument("--batch-launch", default="persistent", choices=["persistent", "auto"],
                     help="batched workload: one persistent launch over all batches, or the autotuner's choice")
     ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64", "mixed-ff"],

@@ -97,7 +97,9 @@ def persistent_capable(batches):
         return False
     if kinds.count("heavy") > PERSISTENT_MAX_GROUPS or kinds.count("light") > PERSISTENT_MAX_GROUPS:
         return False
-    return len({b.K.dtype for b in batches}) == 1
+    # one precision for all, FP64 or the FP32 tangent (the persistent kernel has no float-float form)
+    precs = {b.asm.kPrecision for b in batches}
+    return len(precs) == 1 and precs <= {L.EFE_K_FP64, L.EFE_K_FP32}
 
 
 class BatchedPass:
@@ -120,8 +122,7 @@ class BatchedPass:
                               b.dU.data_ptr(), b.K.data_ptr(), b.P.data_ptr(), b.F.data_ptr())
                 for b in self.batches
             ])  # fmt: skip
-            prec = {torch.float32: L.EFE_K_FP32, torch.float64: L.EFE_K_FP64}[self.batches[0].K.dtype]
-            self._prec = prec
+            self._prec = self.batches[0].asm.kPrecision
 
     def _launch(self):
         stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)

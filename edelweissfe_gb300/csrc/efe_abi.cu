@@ -303,7 +303,8 @@ int32_t efe_compute_elements(const EfeMesh* mesh, const EfeGroup* groups, int32_
       return fail(EFE_ERR_ARGUMENT, "null group buffer");
     if (tl && (!U || !gr.auxTemp)) return fail(EFE_ERR_ARGUMENT, "total-Lagrangian group needs U and auxTemp");
     if (!tl && !dU) return fail(EFE_ERR_ARGUMENT, "small-strain group needs dU");
-    if (kPrecision == EFE_K_FP32_FF && form_of(gr) == efe::SS3 && (!gr.geomG32 || !gr.geomGlo))
+    if (kPrecision == EFE_K_FP32_FF && (form_of(gr) == efe::SS3 || form_of(gr) == efe::TLH) &&
+        (!gr.geomG32 || !gr.geomGlo))
       return fail(EFE_ERR_ARGUMENT, "EFE_K_FP32_FF needs geomG32 and geomGlo");
     const efe::GroupArgs a = make_args(mesh, gr, U, dU, Kdata, P, F, status);
     const int form = form_of(gr);

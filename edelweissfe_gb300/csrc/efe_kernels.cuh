@@ -160,14 +160,19 @@ struct Layout {
   static constexpr int NDOF = NN * DIM;
   // total-Lagrangian Neo-Hooke: per-point record between its sub-phases (F, F^-1, tau, B, c1-c3, s)
   // in FP64 and a copy of F, B, c1 s, c2 s, c3 s in the tangent's precision
-  static constexpr int NX = FORM == TLH ? 40 : 0, NXK = FORM == TLH ? 24 : 0;
+  // Per-point strides of the shared arrays are odd (in their element size): consecutive threads
+  // handle consecutive points, so an even stride would put several of them on one memory bank.
+  static constexpr int NX = FORM == TLH ? 41 : 0, NXK = FORM == TLH ? 25 : 0;
+  static constexpr int SR = (NN * DIM) | 1;                                           // doubles per point of r
+  static constexpr int SC = FormInfo<FORM, DIM>::NSCAL | 1;                           // KT per point of sc
+  static constexpr int SV = (NN * FormInfo<FORM, DIM>::NVEC * DIM) | 1;               // KT per point of v
   // offsets in bytes; doubles first for alignment
   static constexpr size_t u_off = 0;                                              // double [EPB][NN][DIM]
   static constexpr size_t x_off = u_off + sizeof(double) * EPB * NDOF;            // double [EPB][NQ][NX]
-  static constexpr size_t r_off = x_off + sizeof(double) * EPB * NQ * NX;         // double [EPB][NQ][NDOF]
-  static constexpr size_t sc_off = r_off + sizeof(double) * EPB * NQ * NDOF;      // KT [EPB][NQ][NSCAL]
-  static constexpr size_t v_off = sc_off + sizeof(KT) * EPB * NQ * NSCAL;         // KT [EPB][NQ][NN][NVEC][DIM]
-  static constexpr size_t xk_off = v_off + sizeof(KT) * EPB * NQ * NN * NVEC * DIM;  // KT [EPB][NQ][NXK]
+  static constexpr size_t r_off = x_off + sizeof(double) * EPB * NQ * NX;         // double [EPB][NQ][SR]
+  static constexpr size_t sc_off = r_off + sizeof(double) * EPB * NQ * SR;        // KT [EPB][NQ][SC]
+  static constexpr size_t v_off = sc_off + sizeof(KT) * EPB * NQ * SC;            // KT [EPB][NQ][SV: NN][NVEC][DIM]
+  static constexpr size_t xk_off = v_off + sizeof(KT) * EPB * NQ * SV;            // KT [EPB][NQ][NXK]
   static constexpr size_t mc_off = (xk_off + sizeof(KT) * EPB * NQ * NXK + 15) / 16 * 16;  // VMConst [EPB]
   static constexpr size_t rl_off = mc_off + sizeof(VMConst) * EPB;                                     // int [EPB][NN]
   static constexpr size_t bytes = rl_off + sizeof(int) * EPB * NN;
@@ -242,11 +247,21 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
       if (e >= nEl) continue;
       const int i = c / DIM, j = c % DIM;
       const int64_t pt = e * NQ + q;
-      const double* u = su + le * NN * DIM;
-      double h = 0.0;
-      for (int a = 0; a < NN; ++a) h += u[a * DIM + i] * g.geomG[(int64_t)(j * NN + a) * stride + pt];
       double f = (i == j) ? 1.0 : 0.0;
-      f += h;
+      if constexpr (FF) {
+        // displacements relative to node 0 (sum_a dN_a/dX = 0) times the float-float geometry
+        const ff* uf = reinterpret_cast<const ff*>(su) + le * NN * DIM;
+        ff acc{0, 0};
+        for (int a = 0; a < NN; ++a)
+          ff_fma(acc, uf[a * DIM + i],
+                 ff{g.geomG32[(int64_t)(j * NN + a) * stride + pt], g.geomGlo[(int64_t)(j * NN + a) * stride + pt]});
+        f += ff_to_double(acc);
+      } else {
+        const double* u = su + le * NN * DIM;
+        double h = 0.0;
+        for (int a = 0; a < NN; ++a) h += u[a * DIM + i] * g.geomG[(int64_t)(j * NN + a) * stride + pt];
+        f += h;
+      }
       sx[(le * NQ + q) * L::NX + i * 3 + j] = f;
     }
     __syncthreads();
@@ -296,7 +311,7 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
         eps[5] = 2.0 * Eg[0][2];
       }
       const double s = g.geomS[pt];
-      KT* sc = ssc + (le * NQ + q) * NSCAL;
+      KT* sc = ssc + (le * NQ + q) * L::SC;
       sc[0] = (KT)(o.c1 * s);
       sc[1] = (KT)(o.c4 * s);
       for (int i = 0; i < 3; ++i)
@@ -312,6 +327,16 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
       rec[37] = o.c2;
       rec[38] = o.c3;
       rec[39] = s;
+      if constexpr (FF) {
+        // the float-float sub-phase A2 reads F^-1, tau and s as (hi, lo) pairs from the same slots
+        ff* recf = reinterpret_cast<ff*>(rec);
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) {
+            recf[9 + i * 3 + j] = ff_split(iF[i][j]);
+            recf[18 + i * 3 + j] = ff_split(o.tau[i][j]);
+          }
+        recf[39] = ff_split(s);
+      }
       reck[18] = (KT)(o.c1 * s);
       reck[19] = (KT)(o.c2 * s);
       reck[20] = (KT)(o.c3 * s);
@@ -336,27 +361,47 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
       const int64_t pt = e * NQ + q;
       const double* rec = sx + (le * NQ + q) * L::NX;
       const KT* reck = sxk + (le * NQ + q) * L::NXK;
-      double G[3] = {0, 0, 0};
-      for (int j = 0; j < DIM; ++j) G[j] = g.geomG[(int64_t)(j * NN + a) * stride + pt];
-      double h[3] = {0, 0, 0};
-      for (int i = 0; i < DIM; ++i)
-        for (int I = 0; I < DIM; ++I) h[i] += G[I] * rec[9 + I * 3 + i];
-      const double s = rec[39];
-      double* rq = sr + (le * NQ + q) * NDOF;
-      double ths[3];
-      for (int j = 0; j < DIM; ++j) {
-        double th = 0.0;
-        for (int i = 0; i < DIM; ++i) th += rec[18 + j * 3 + i] * h[i];
-        ths[j] = th * s;
-        rq[a * DIM + j] = ths[j];
-      }
-      KT Gk[3], hk[3], gg[3], bh[3];
-      for (int j = 0; j < DIM; ++j) {
-        if constexpr (std::is_same<KT, float>::value)
-          Gk[j] = g.geomG32 ? (KT)g.geomG32[(int64_t)(j * NN + a) * stride + pt] : (KT)G[j];
-        else
-          Gk[j] = (KT)G[j];
-        hk[j] = (KT)h[j];
+      KT Gk[3], hk[3], gg[3], bh[3], thk[3];
+      if constexpr (FF) {
+        // h_a = F^-T G_a, tau h_a and s tau h_a in float-float arithmetic (FP32 pipe)
+        const ff* recf = reinterpret_cast<const ff*>(rec);
+        ff Gf[3] = {{0, 0}, {0, 0}, {0, 0}}, h[3] = {{0, 0}, {0, 0}, {0, 0}};
+        for (int j = 0; j < DIM; ++j)
+          Gf[j] = ff{g.geomG32[(int64_t)(j * NN + a) * stride + pt], g.geomGlo[(int64_t)(j * NN + a) * stride + pt]};
+        for (int i = 0; i < DIM; ++i)
+          for (int I = 0; I < DIM; ++I) ff_fma(h[i], Gf[I], recf[9 + I * 3 + i]);
+        ff* rf = reinterpret_cast<ff*>(sr + (le * NQ + q) * L::SR);
+        for (int j = 0; j < DIM; ++j) {
+          ff th{0, 0}, ths{0, 0};
+          for (int i = 0; i < DIM; ++i) ff_fma(th, recf[18 + j * 3 + i], h[i]);
+          ff_fma(ths, th, recf[39]);
+          rf[a * DIM + j] = ths;
+          Gk[j] = (KT)Gf[j].h;
+          hk[j] = (KT)h[j].h;
+          thk[j] = (KT)ths.h;
+        }
+      } else {
+        double G[3] = {0, 0, 0};
+        for (int j = 0; j < DIM; ++j) G[j] = g.geomG[(int64_t)(j * NN + a) * stride + pt];
+        double h[3] = {0, 0, 0};
+        for (int i = 0; i < DIM; ++i)
+          for (int I = 0; I < DIM; ++I) h[i] += G[I] * rec[9 + I * 3 + i];
+        const double s = rec[39];
+        double* rq = sr + (le * NQ + q) * L::SR;
+        for (int j = 0; j < DIM; ++j) {
+          double th = 0.0;
+          for (int i = 0; i < DIM; ++i) th += rec[18 + j * 3 + i] * h[i];
+          const double ths = th * s;
+          rq[a * DIM + j] = ths;
+          thk[j] = (KT)ths;
+        }
+        for (int j = 0; j < DIM; ++j) {
+          if constexpr (std::is_same<KT, float>::value)
+            Gk[j] = g.geomG32 ? (KT)g.geomG32[(int64_t)(j * NN + a) * stride + pt] : (KT)G[j];
+          else
+            Gk[j] = (KT)G[j];
+          hk[j] = (KT)h[j];
+        }
       }
       for (int i = 0; i < DIM; ++i) {
         KT v1 = KT(0), v2 = KT(0);
@@ -368,12 +413,12 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
         bh[i] = v2;
       }
       const KT c1s = reck[18], c2s = reck[19], c3s = reck[20];
-      KT* v = sv + ((size_t)(le * NQ + q) * NN + a) * NVEC * DIM;
+      KT* v = sv + (size_t)(le * NQ + q) * L::SV + a * NVEC * DIM;
       for (int j = 0; j < DIM; ++j) {
         v[0 * DIM + j] = Gk[j];
         v[1 * DIM + j] = hk[j];
         v[2 * DIM + j] = gg[j];
-        v[3 * DIM + j] = c1s * gg[j] - (KT)ths[j];
+        v[3 * DIM + j] = c1s * gg[j] - thk[j];
         v[4 * DIM + j] = c2s * hk[j] + c3s * bh[j];
       }
     }
@@ -393,9 +438,9 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
     const double s = g.geomS[pt];
     const double* u = su + le * NN * DIM;
     const double* props = g.props + e * g.nProps;
-    double* rq = sr + (le * NQ + q) * NDOF;
-    KT* sc = ssc + (le * NQ + q) * NSCAL;
-    KT* vq = sv + (size_t)(le * NQ + q) * NN * NVEC * DIM;
+    double* rq = sr + (le * NQ + q) * L::SR;
+    KT* sc = ssc + (le * NQ + q) * L::SC;
+    KT* vq = sv + (size_t)(le * NQ + q) * L::SV;
     bool ok = true;
     double sig[6], eps[6], kappa = 0.0;
     for (int f = 0; f < 6; ++f) {
@@ -683,10 +728,10 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
     if constexpr (FF) {
       const ff* rf = reinterpret_cast<const ff*>(sr);
       ff acc{0, 0};
-      for (int q = 0; q < NQ; ++q) ff_add(acc, rf[(le * NQ + q) * NDOF + k]);
+      for (int q = 0; q < NQ; ++q) ff_add(acc, rf[(le * NQ + q) * L::SR + k]);
       pe = -ff_to_double(acc);
     } else {
-      for (int q = 0; q < NQ; ++q) pe -= sr[(le * NQ + q) * NDOF + k];
+      for (int q = 0; q < NQ; ++q) pe -= sr[(le * NQ + q) * L::SR + k];
     }
     const int a = k / DIM, c = k % DIM;
     const int32_t node = g.conn[e * NN + a];
@@ -716,9 +761,9 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
 #pragma unroll
       for (int k = 0; k < DIM; ++k) acc[j][k] = KT(0);
     for (int q = 0; q < NQ; ++q) {
-      const KT* sc = ssc + (le * NQ + q) * NSCAL;
-      const KT* va = sv + (size_t)((le * NQ + q) * NN + a) * NVEC * DIM;
-      const KT* vb = sv + (size_t)((le * NQ + q) * NN + b) * NVEC * DIM;
+      const KT* sc = ssc + (le * NQ + q) * L::SC;
+      const KT* va = sv + (size_t)(le * NQ + q) * L::SV + a * NVEC * DIM;
+      const KT* vb = sv + (size_t)(le * NQ + q) * L::SV + b * NVEC * DIM;
       if constexpr (FORM == SS3) {
         const KT Lq = sc[0], Mq = sc[1], Aq = sc[2];
         const KT dot = va[0] * vb[0] + va[1] * vb[1] + va[2 % DIM] * vb[2 % DIM];

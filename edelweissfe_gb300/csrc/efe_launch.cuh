@@ -121,13 +121,13 @@ cudaError_t launch_form(int form, const GroupArgs& g, cudaStream_t st) {
   if constexpr (DIM == 3) {
     switch (form) {
       case SS3: return launch_assemble<SHAPE, RULE, SS3, KT, FF>(g, st);
-      case TLH: return launch_assemble<SHAPE, RULE, TLH, KT>(g, st);
+      case TLH: return launch_assemble<SHAPE, RULE, TLH, KT, FF>(g, st);
       case TLV3: return launch_assemble<SHAPE, RULE, TLV3, KT>(g, st);
     }
   } else {
     switch (form) {
       case SS2: return launch_assemble<SHAPE, RULE, SS2, KT>(g, st);
-      case TLH: return launch_assemble<SHAPE, RULE, TLH, KT>(g, st);
+      case TLH: return launch_assemble<SHAPE, RULE, TLH, KT, FF>(g, st);
       case TLV2: return launch_assemble<SHAPE, RULE, TLV2, KT>(g, st);
     }
   }

@@ -74,9 +74,10 @@ enum {
   EFE_K_FP32 = 1, /* tangent formed and accumulated in FP32 (Kdata is float*); residual, state
                      and the return map stay FP64                                              */
   EFE_K_FP32_FF = 2 /* as EFE_K_FP32, and for small-strain solids the strain increment and the
+                     element residual, for total-Lagrangian Neo-Hooke F, F^-T dN/dX and the
                      element residual are formed in float-float arithmetic (~48-bit significand,
-                     needs geomG32 and geomGlo); the return map, state and the global residual
-                     accumulation stay FP64                                                    */
+                     needs geomG32 and geomGlo); the return map / Kirchhoff stress, state and the
+                     global residual accumulation stay FP64                                    */
 };
 /* status words (int32[3], zeroed by the caller): status[0] = OR of EFE_STATUS_* bits,
    status[1] = INT32_MAX - (global index of the first failing element), 0 if none,
