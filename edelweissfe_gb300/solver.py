@@ -149,7 +149,7 @@ class NISTGPU:
     def __init__(self, assembler, linsolver="pcg", extrapolation="linear", maxIter=10, criticalIter=5,
                  maxGrowingIter=10, fluxResidualTolerance=1e-8, fluxResidualToleranceAlternative=5e-3,
                  fieldCorrectionTolerance=1e-8, pcgTolerance=1e-12, pcgMaxIter=20000, fluxResidualFloor=1e-7,
-                 pcgPreconditioner="jacobi"):  # fmt: skip
+                 pcgPreconditioner="jacobi", pcgGraphs=True):  # fmt: skip
         self.asm = assembler
         self.linsolver = linsolver
         self.extrapolation = extrapolation
@@ -166,6 +166,9 @@ class NISTGPU:
         # displacement components) -- on near-regular hexahedral meshes of isotropic material the
         # same-node couplings nearly cancel and both need the same iterations
         self.pcgPreconditioner = pcgPreconditioner
+        # replay the PCG iteration batches of long solves as one CUDA graph (same kernels and
+        # arguments as the direct launches, so the same results bit for bit)
+        self.pcgGraphs = pcgGraphs
         self.nAccumulatedFluxes = sum(len(g.conn) * len(g.conn[0]) * assembler.dim for g in assembler.groups if len(g.conn))
         dev = assembler.device
         ip, ix = assembler.indptr_host, assembler.indices_host
@@ -329,7 +332,13 @@ class NISTGPU:
         side gives the same solution from the symmetric positive-definite system on the free DOFs:
         x = x_d + y with x_d = R on the prescribed DOFs and K_ff y_f = R_f - K_fd x_d.  K is used as
         assembled (FP32 or FP64 values).  Converged when |r| <= pcgTolerance |b| (checked every
-        10 iterations, as b's norm includes the prescribed values)."""
+        10 iterations, as b's norm includes the prescribed values).  The check of a batch is read
+        while the next batch already runs (its r.r copied to pinned memory behind the batch), so the
+        device never waits for the host; a converged solve therefore runs one batch past the batch
+        that met the tolerance (the kernels stop moving x when p.Ap or r.z reach zero).  With pcgGraphs, a solve still
+        running after its first 20 iterations captures one batch of 10 iterations (30 launches) as a
+        CUDA graph and replays it: the kernels read the iteration number only for its parity, which
+        is even at the start of every batch."""
         import ctypes
 
         from . import _lib as L
@@ -372,16 +381,50 @@ class NISTGPU:
         L.check(lib.efe_pcg_start(ctypes.byref(s), ctypes.c_void_p(b.data_ptr()), stream), "efe_pcg_start")
         tol2 = (self.pcgTolerance * bnorm) ** 2
         k = 0
+        graph = None
         if bnorm > 0.0 and float(work[2]) > tol2:
+            seen = torch.empty((2, 2), dtype=torch.float64, pin_memory=True)  # r.r, p.Ap of two batches
+            done = [torch.cuda.Event(), torch.cuda.Event()]
+            batch = 0
             while k < self.pcgMaxIter:
                 step = min(10, self.pcgMaxIter - k)
-                L.check(lib.efe_pcg_iterate(ctypes.byref(s), k, step, stream), "efe_pcg_iterate")
+                if self.pcgGraphs and step == 10 and k >= 20:
+                    if graph is None:
+                        graph = self._capture_pcg_batch(lib, s, k, step)
+                    graph.replay()
+                else:
+                    L.check(lib.efe_pcg_iterate(ctypes.byref(s), k, step, stream), "efe_pcg_iterate")
                 k += step
-                rr, pAp = work[2:4].tolist()  # one device-to-host read per batch of iterations
-                if not rr <= tol2:
-                    if rr != rr or pAp == 0.0:  # NaN or a breakdown (p.Ap = 0)
-                        break
+                seen[batch % 2].copy_(work[2:4], non_blocking=True)
+                done[batch % 2].record()
+                batch += 1
+                if batch < 2:
+                    continue
+                done[batch % 2].synchronize()  # the previous batch (the one just queued still runs)
+                rr, pAp = seen[batch % 2].tolist()
+                if not rr <= tol2 and rr == rr and pAp != 0.0:  # not converged, no NaN, no breakdown
                     continue
                 break
         self.linearIterations.append(k)
         return vec[0] + xd
+
+    def _capture_pcg_batch(self, lib, s, k, step):
+        """One batch of `step` PCG iterations starting at iteration k (even) as a CUDA graph, captured
+        on a side stream; replay() runs it on the current stream."""
+        import ctypes
+
+        from . import _lib as L
+
+        dev = self.asm.device
+        graph = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            graph.capture_begin()
+            try:
+                rc = lib.efe_pcg_iterate(ctypes.byref(s), k, step, ctypes.c_void_p(side.cuda_stream))
+            finally:
+                graph.capture_end()
+        L.check(rc, "efe_pcg_iterate (graph capture)")
+        torch.cuda.current_stream(dev).wait_stream(side)
+        return graph

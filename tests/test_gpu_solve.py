@@ -59,3 +59,26 @@ def test_pcg_matches_direct_solve(elType, precision, preconditioner):
     torch.cuda.synchronize()
     yr = A @ v.cpu().numpy()
     assert np.abs(y.cpu().numpy() - yr).max() <= 1e-12 * np.abs(yr).max()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_pcg_graph_replay_matches_direct_launches(precision):
+    """Long solves replay their iteration batches as a CUDA graph: same iterations, same bits as the
+    directly launched batches."""
+    from edelweissfe_gb300 import ElementGroup, GPUAssembler, meshes
+    from edelweissfe_gb300.solver import NISTGPU
+
+    coords, conn, nodeDof, nDof = meshes.box(6, 5, 4, nNodes=8)
+    asm = GPUAssembler(coords, nodeDof, nDof, [ElementGroup("C3D8", "vonmises", [210e3, 0.3, 250, 1000, 0, 0], conn)],
+                       precision=precision)  # fmt: skip
+    graphs = NISTGPU(asm, pcgTolerance=1e-14)
+    direct = NISTGPU(asm, pcgTolerance=1e-14, pcgGraphs=False)
+    rng = np.random.default_rng(3)
+    K = graphs.tangentAt(torch.tensor(rng.normal(0, 1e-3, nDof), device=asm.device))
+    dir_idx = torch.as_tensor(nodeDof[coords[:, 2] < 1e-9][:, None] + np.arange(3), device=asm.device).ravel()
+    R = torch.tensor(rng.normal(0, 1, nDof), device=asm.device)
+    xg = graphs._solve_pcg(K, R, dir_idx)
+    xd = direct._solve_pcg(K, R, dir_idx)
+    assert graphs.linearIterations == direct.linearIterations
+    assert graphs.linearIterations[-1] >= 40  # at least two graph replays
+    assert torch.equal(xg, xd)
