@@ -559,6 +559,7 @@ def run_newton(args):
     for precision in ("fp64", "mixed"):
         asm = GPUAssembler(coords, nodeDof, nDof, [ElementGroup("C3D8", "vonmises", VM, conn)], precision=precision)
         solver = NISTGPU(asm, linsolver="pcg", extrapolation="off", maxIter=15, fluxResidualTolerance=1e-10,
+                         pcgPreconditioner=args.pcg_preconditioner,
                          fieldCorrectionTolerance=1e-10, fluxResidualFloor=0.0, pcgTolerance=1e-13)  # fmt: skip
         torch.cuda.synchronize()
         t = time.perf_counter()
@@ -579,7 +580,8 @@ def run_newton(args):
         "value": max(extra) if extra else None, "unit": "max extra iterations per increment (mixed - fp64)",
         "higher_is_better": False, "data": "synthetic",
         "config": {"workload": f"C3D8 von Mises J2 {args.n}^3 unit cube (jitter 5%), 20 uniaxial increments to "
-                               "0.5% strain, device Jacobi-PCG (rel. tol 1e-13)", "dofs": nDof, "elements": len(conn)},
+                               f"0.5% strain, device PCG (rel. tol 1e-13, preconditioner {args.pcg_preconditioner})",
+                   "dofs": nDof, "elements": len(conn)},
         "fp64": {k: v for k, v in f.items() if k != "U"},
         "mixed": {k: v for k, v in m.items() if k != "U"},
         "U_rel_diff_mixed_vs_fp64": float(np.abs(m["U"] - f["U"]).max() / np.abs(f["U"]).max()),
@@ -783,7 +785,8 @@ def run_plastic(args):
     def forward(pr, precision="mixed"):
         asm = GPUAssembler(coords, nodeDof, nDof, [ElementGroup("C3D20", "vonmises", pr, conn)], precision=precision)
         solver = NISTGPU(asm, linsolver="pcg", extrapolation="linear", maxIter=15, fluxResidualTolerance=1e-10,
-                         fieldCorrectionTolerance=1e-10, fluxResidualFloor=0.0, pcgTolerance=args.pcg_tol)  # fmt: skip
+                         fieldCorrectionTolerance=1e-10, fluxResidualFloor=0.0, pcgTolerance=args.pcg_tol,
+                         pcgPreconditioner=args.pcg_preconditioner)  # fmt: skip
         adj = PathAdjoint(solver)
         torch.cuda.synchronize()
         t = time.perf_counter()
@@ -877,6 +880,7 @@ def run_plastic(args):
         "increments": nInc, "adjoint_pcg_iterations": pcg_adj,
         "forward_wall_s": fwd_s, "forward_newton_iterations": newton, "forward_pcg_iterations": pcg_fwd,
         "pcg_tolerance": {"forward": args.pcg_tol, "adjoint": args.pcg_tol_adjoint},
+        "pcg_preconditioner": args.pcg_preconditioner,
         "J": J, "plastic_point_fraction": plastic,
         "grad_norm": {"fy0": float(np.linalg.norm(gy)), "H": float(np.linalg.norm(gH))},
         "element_pass": passes, "mixed_over_fp64": passes["fp64"]["ms"] / passes["mixed"]["ms"],
@@ -901,6 +905,8 @@ def main():
                          "plastic: Hexa20 J2 96x96x48 path adjoint")
     ap.add_argument("--plastic-fd", type=int, default=0, help="FD directions for the plastic workload")
     ap.add_argument("--pcg-tol", type=float, default=1e-8, help="forward Newton PCG tolerance (plastic)")
+    ap.add_argument("--pcg-preconditioner", default="jacobi", choices=["jacobi", "block", "amg"],
+                    help="device CG preconditioner of the newton and plastic workloads (amg: aggregation multigrid)")
     ap.add_argument("--pcg-tol-adjoint", type=float, default=1e-10, help="adjoint PCG tolerance (plastic)")
     ap.add_argument("--fd-directions", type=int, default=50, help="central-difference directions (adjoint)")
     ap.add_argument("--batch-meshes", type=int, default=512)

@@ -37,6 +37,10 @@ EXPORTS = [
     "efe_csr_spmv",
     "efe_pcg_start",
     "efe_pcg_iterate",
+    "efe_csr_gemv",
+    "efe_csr_gemv_pairs",
+    "efe_chebyshev_step",
+    "efe_split_pairs",
     "efe_body_force",
     "efe_adjoint_tl",
     "efe_adjoint_small_strain",
@@ -103,6 +107,21 @@ class EfePcg(ctypes.Structure):
         ("work", ctypes.c_void_p),
         ("pFF", ctypes.c_void_p),
         ("blockSize", ctypes.c_int32),
+        ("patternBlock", ctypes.c_int32),
+    ]
+
+
+class EfeCsr(ctypes.Structure):
+    _fields_ = [
+        ("nRows", ctypes.c_int64),
+        ("nCols", ctypes.c_int64),
+        ("nnz", ctypes.c_int64),
+        ("indptr", ctypes.c_void_p),
+        ("indices", ctypes.c_void_p),
+        ("values", ctypes.c_void_p),
+        ("kPrecision", ctypes.c_int32),
+        ("freeMask", ctypes.c_void_p),
+        ("rowBlock", ctypes.c_int32),
     ]
 
 
@@ -184,6 +203,14 @@ def load(build_if_missing=False):
     lib.efe_pcg_start.argtypes = [ctypes.POINTER(EfePcg), P, P]
     lib.efe_pcg_iterate.restype = i32
     lib.efe_pcg_iterate.argtypes = [ctypes.POINTER(EfePcg), i64, i32, P]
+    lib.efe_csr_gemv.restype = i32
+    lib.efe_csr_gemv.argtypes = [ctypes.POINTER(EfeCsr), P, f64, f64, P, P]
+    lib.efe_csr_gemv_pairs.restype = i32
+    lib.efe_csr_gemv_pairs.argtypes = [ctypes.POINTER(EfeCsr), P, f64, f64, P, P]
+    lib.efe_chebyshev_step.restype = i32
+    lib.efe_chebyshev_step.argtypes = [i64, P, P, f64, f64, i32, P, P, P, P]
+    lib.efe_split_pairs.restype = i32
+    lib.efe_split_pairs.argtypes = [i64, P, P, P]
     lib.efe_accept_state.restype = i32
     lib.efe_accept_state.argtypes = [ctypes.POINTER(EfeGroup), i32, P]
     lib.efe_pattern_count.restype = i64

@@ -80,6 +80,11 @@ class GPUAssembler:
         self.kPrecision = {"fp64": L.EFE_K_FP64, "mixed": L.EFE_K_FP32, "mixed-ff": L.EFE_K_FP32_FF}[precision]
         self.kdtype = torch.float64 if precision == "fp64" else torch.float32
         self._build_pattern()
+        # rows come in aligned groups of dim (a node's DOF rows, one shared column list) when every
+        # node's first DOF is a multiple of dim and the nodes' DOFs fill 0 .. nDof-1
+        used = self.nodeDof_host[self.nodeDof_host >= 0]
+        self.rowGroup = self.dim if (self.nDof == self.dim * len(np.unique(used)) and np.all(used % self.dim == 0)
+                                     and self.dim in (2, 3)) else 1  # fmt: skip
         dev = self.device
         self.coords = _upload(coords, np.float64, dev)
         self.nodeDof = _upload(self.nodeDof_host, np.int32, dev)

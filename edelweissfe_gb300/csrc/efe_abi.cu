@@ -487,6 +487,7 @@ int32_t check_pcg(const EfePcg* s) {
                    !s->Ap || !s->work))
     return fail(EFE_ERR_ARGUMENT, "null solver buffer");
   if (reinterpret_cast<uintptr_t>(s->pFF) % 8 != 0) return fail(EFE_ERR_ARGUMENT, "pFF must be 8-byte aligned");
+  if (s->patternBlock < 0 || s->patternBlock > 3) return fail(EFE_ERR_ARGUMENT, "patternBlock must be 0 to 3");
   if (s->blockSize < 1 || s->blockSize > 3 || s->n % s->blockSize != 0)
     return fail(EFE_ERR_ARGUMENT, "blockSize must be 1, 2 or 3 and divide n");
   return EFE_OK;
@@ -509,6 +510,60 @@ int32_t efe_pcg_start(const EfePcg* s, const double* b, void* stream) {
   if (s->n == 0) return EFE_OK;
   cudaError_t e = efe::pcg_start(*s, b, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "efe_pcg_start");
+  return EFE_OK;
+}
+
+int32_t efe_csr_gemv(const EfeCsr* a, const double* x, double alpha, double beta, double* y, void* stream) {
+  if (!a) return fail(EFE_ERR_ARGUMENT, "null matrix");
+  if (a->nRows < 0 || a->nCols < 0 || a->nnz < 0) return fail(EFE_ERR_ARGUMENT, "negative matrix size");
+  if (a->kPrecision != EFE_K_FP64 && a->kPrecision != EFE_K_FP32 && a->kPrecision != EFE_K_FP32_FF)
+    return fail(EFE_ERR_ARGUMENT, "unknown value precision");
+  if (a->freeMask && a->nCols != a->nRows) return fail(EFE_ERR_ARGUMENT, "a masked matrix must be square");
+  if (a->nRows == 0) return EFE_OK;
+  if (!a->indptr || (a->nCols > 0 && (!a->indices || !a->values)) || !y || (a->nCols > 0 && !x))
+    return fail(EFE_ERR_ARGUMENT, "null matrix or vector");
+  cudaError_t e = efe::csr_gemv(*a, x, alpha, beta, y, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "efe_csr_gemv");
+  return EFE_OK;
+}
+
+int32_t efe_csr_gemv_pairs(const EfeCsr* a, const float* xPairs, double alpha, double beta, double* y,
+                           void* stream) {
+  if (!a) return fail(EFE_ERR_ARGUMENT, "null matrix");
+  if (a->nRows < 0 || a->nCols < 0 || a->nnz < 0) return fail(EFE_ERR_ARGUMENT, "negative matrix size");
+  if (a->kPrecision != EFE_K_FP32 && a->kPrecision != EFE_K_FP32_FF)
+    return fail(EFE_ERR_ARGUMENT, "float-float products need float values");
+  if (a->rowBlock < 0 || a->rowBlock > 3) return fail(EFE_ERR_ARGUMENT, "rowBlock must be 0 to 3");
+  if (a->freeMask && a->nCols != a->nRows) return fail(EFE_ERR_ARGUMENT, "a masked matrix must be square");
+  if (reinterpret_cast<uintptr_t>(xPairs) % 8 != 0) return fail(EFE_ERR_ARGUMENT, "xPairs must be 8-byte aligned");
+  if (a->nRows == 0) return EFE_OK;
+  if (!a->indptr || (a->nCols > 0 && (!a->indices || !a->values || !xPairs)) || !y)
+    return fail(EFE_ERR_ARGUMENT, "null matrix or vector");
+  cudaError_t e = efe::csr_gemv_pairs(*a, reinterpret_cast<const float2*>(xPairs), alpha, beta, y,
+                                      (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "efe_csr_gemv_pairs");
+  return EFE_OK;
+}
+
+int32_t efe_chebyshev_step(int64_t n, const double* dinv, const double* r, double c1, double c2, int32_t accumulate,
+                           double* d, double* z, float* dPairs, void* stream) {
+  if (n < 0) return fail(EFE_ERR_ARGUMENT, "negative vector size");
+  if (reinterpret_cast<uintptr_t>(dPairs) % 8 != 0) return fail(EFE_ERR_ARGUMENT, "dPairs must be 8-byte aligned");
+  if (n == 0) return EFE_OK;
+  if (!dinv || !r || !d || !z) return fail(EFE_ERR_ARGUMENT, "null vector");
+  cudaError_t e = efe::chebyshev_step(n, dinv, r, c1, c2, accumulate, d, z, reinterpret_cast<float2*>(dPairs),
+                                      (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "efe_chebyshev_step");
+  return EFE_OK;
+}
+
+int32_t efe_split_pairs(int64_t n, const double* x, float* pairs, void* stream) {
+  if (n < 0) return fail(EFE_ERR_ARGUMENT, "negative vector size");
+  if (reinterpret_cast<uintptr_t>(pairs) % 8 != 0) return fail(EFE_ERR_ARGUMENT, "pairs must be 8-byte aligned");
+  if (n == 0) return EFE_OK;
+  if (!x || !pairs) return fail(EFE_ERR_ARGUMENT, "null vector");
+  cudaError_t e = efe::split_pairs(n, x, reinterpret_cast<float2*>(pairs), (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "efe_split_pairs");
   return EFE_OK;
 }
 

@@ -164,6 +164,12 @@ cudaError_t persistent_groups_noalloc(int kprec, const GroupArgs* heavy, int nHe
                                       int nLight, int64_t* needed, cudaStream_t st);
 // device linear solve (efe_solve.cu)
 cudaError_t csr_spmv(const EfePcg& s, const double* x, double* y, cudaStream_t st);
+cudaError_t csr_gemv(const EfeCsr& a, const double* x, double alpha, double beta, double* y, cudaStream_t st);
+cudaError_t csr_gemv_pairs(const EfeCsr& a, const float2* xf, double alpha, double beta, double* y,
+                           cudaStream_t st);
+cudaError_t chebyshev_step(int64_t n, const double* dinv, const double* r, double c1, double c2, int accumulate,
+                           double* d, double* z, float2* dff, cudaStream_t st);
+cudaError_t split_pairs(int64_t n, const double* x, float2* xf, cudaStream_t st);
 cudaError_t pcg_start(const EfePcg& s, const double* b, cudaStream_t st);
 cudaError_t pcg_iterate(const EfePcg& s, int64_t k0, int nIter, cudaStream_t st);
 cudaError_t adjoint_ss_quad4(int rule, const SSAdjointArgs& a, cudaStream_t st);

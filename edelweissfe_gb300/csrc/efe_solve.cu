@@ -21,6 +21,9 @@
 //
 // Preconditioner: the inverse of the diagonal (blockSize 1) or of the nodal diagonal blocks
 // (blockSize = 2 or 3 consecutive DOFs, the node's displacement components), built by the caller.
+// The building blocks of a multilevel preconditioner are here too: a general CSR product
+// y = alpha A x + beta y (rectangular for the transfer operators, masked for the tangent) and the
+// vector step of a Chebyshev smoother; the host composes them into V-cycles.
 //
 // One iteration is three kernels: (1) Ap = A p with the partial sums of p.Ap per block, (2) alpha,
 // x += alpha p, r -= alpha Ap, z = M^-1 r with the partial sums of r.z and r.r, (3) beta,
@@ -113,25 +116,111 @@ __device__ __forceinline__ double row_product(int32_t b, int32_t e, const int32_
   return group_sum((s0 + s1) + (s2 + s3));
 }
 
-// (K x)_r with float values and x = xh + xl in float-float arithmetic (FP32 pipe only)
+// (K x)_r with float values and x = xh + xl in float-float arithmetic (FP32 pipe only); four
+// independent entries per lane and step keep enough gathers in flight to approach DRAM speed
 __device__ __forceinline__ double row_product_ff(int32_t b, int32_t e, const int32_t* __restrict__ indices,
                                                  const float* __restrict__ K, const float2* __restrict__ xf, int sl) {
-  float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f;
-  for (int32_t j = b + sl; j < e; j += 2 * G) {
-    const bool p1 = j + G < e;
+  float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f, h3 = 0.f, l3 = 0.f;
+  for (int32_t j = b + sl; j < e; j += 4 * G) {
+    const bool p1 = j + G < e, p2 = j + 2 * G < e, p3 = j + 3 * G < e;
     const int32_t c0 = indices[j];
-    const int32_t c1 = p1 ? indices[j + G] : c0;
-    const float k0 = K[j], k1 = p1 ? K[j + G] : 0.f;
-    const float2 x0 = xf[c0], x1 = xf[c1];
+    const int32_t c1 = p1 ? indices[j + G] : c0, c2 = p2 ? indices[j + 2 * G] : c0, c3 = p3 ? indices[j + 3 * G] : c0;
+    const float k0 = K[j], k1 = p1 ? K[j + G] : 0.f, k2 = p2 ? K[j + 2 * G] : 0.f, k3 = p3 ? K[j + 3 * G] : 0.f;
+    const float2 x0 = xf[c0], x1 = xf[c1], x2 = xf[c2], x3 = xf[c3];
     ff_madd(h0, l0, k0, x0.x, x0.y);
     ff_madd(h1, l1, k1, x1.x, x1.y);
+    ff_madd(h2, l2, k2, x2.x, x2.y);
+    ff_madd(h3, l3, k3, x3.x, x3.y);
   }
   ff_acc(h0, l0, h1, l1);
+  ff_acc(h2, l2, h3, l3);
+  ff_acc(h0, l0, h2, l2);
   for (int o = 4; o > 0; o >>= 1) {
     const float oh = __shfl_xor_sync(0xffffffffu, h0, o), ol = __shfl_xor_sync(0xffffffffu, l0, o);
     ff_acc(h0, l0, oh, ol);
   }
   return (double)h0 + (double)l0;
+}
+
+// (K x) for the PB rows r0 .. r0+PB-1 of one node, which share one column list (the nodal DOF
+// rows of an assembled tangent): each column index and x pair is read once for the PB rows, so a
+// stored entry costs 4 + 4/PB bytes instead of 8.  Float values, x as float-float pairs, sums in
+// float-float arithmetic.  Values of a row are read only within that row's own length, so a
+// pattern without the shared-column property still reads inside the arrays.
+template <int PB>
+__device__ __forceinline__ void group_product_ff(const int32_t* __restrict__ indptr, int64_t r0, bool live,
+                                                 const int32_t* __restrict__ indices, const float* __restrict__ K,
+                                                 const float2* __restrict__ xf, int sl, double out[PB]) {
+  int32_t bc[PB], lc[PB];
+#pragma unroll
+  for (int c = 0; c < PB; ++c) {
+    bc[c] = live ? indptr[r0 + c] : 0;
+    lc[c] = live ? indptr[r0 + c + 1] - bc[c] : 0;
+  }
+  float h0[PB], l0[PB], h1[PB], l1[PB];
+#pragma unroll
+  for (int c = 0; c < PB; ++c) h0[c] = l0[c] = h1[c] = l1[c] = 0.f;
+  const int32_t len = lc[0];
+  for (int32_t t = sl; t < len; t += 2 * G) {
+    const bool p1 = t + G < len;
+    const int32_t c0 = indices[bc[0] + t];
+    const int32_t c1 = p1 ? indices[bc[0] + t + G] : c0;
+    const float2 x0 = xf[c0], x1 = xf[c1];
+#pragma unroll
+    for (int c = 0; c < PB; ++c) {
+      const float k0 = t < lc[c] ? K[bc[c] + t] : 0.f;
+      const float k1 = (p1 && t + G < lc[c]) ? K[bc[c] + t + G] : 0.f;
+      ff_madd(h0[c], l0[c], k0, x0.x, x0.y);
+      ff_madd(h1[c], l1[c], k1, x1.x, x1.y);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < PB; ++c) {
+    float h = h0[c], l = l0[c];
+    ff_acc(h, l, h1[c], l1[c]);
+    for (int o = 4; o > 0; o >>= 1) {
+      const float oh = __shfl_xor_sync(0xffffffffu, h, o), ol = __shfl_xor_sync(0xffffffffu, l, o);
+      ff_acc(h, l, oh, ol);
+    }
+    out[c] = (double)h + (double)l;
+  }
+}
+
+// The float-float CG product over node row groups of PB rows (spmv_kernel<float, true> otherwise).
+template <int PB>
+__global__ void __launch_bounds__(NT) spmv_group_ff_kernel(int64_t n, const int32_t* __restrict__ indptr,
+                                                           const int32_t* __restrict__ indices,
+                                                           const float* __restrict__ K,
+                                                           const uint8_t* __restrict__ freeMask,
+                                                           const double* __restrict__ x, const float2* __restrict__ xf,
+                                                           double* __restrict__ y, double* part) {
+  __shared__ double sh[WARPS + 1];
+  const int lane = threadIdx.x % 32, g = lane / G, sl = lane % G;
+  constexpr int GPW = 32 / G;  // row groups per warp and step
+  const int64_t warp = ((int64_t)blockIdx.x * NT + threadIdx.x) / 32;
+  const int64_t nw = (int64_t)gridDim.x * WARPS;
+  const int64_t nGroups = n / PB;
+  double acc = 0.0;
+  // the loop condition depends on the warp only: all 32 lanes reach every shuffle
+  for (int64_t gb = warp * GPW; gb < nGroups; gb += nw * GPW) {
+    const int64_t gi = gb + g;
+    const bool live = gi < nGroups;
+    double v[PB];
+    group_product_ff<PB>(indptr, gi * PB, live, indices, K, xf, sl, v);
+    if (live && sl == 0) {
+#pragma unroll
+      for (int c = 0; c < PB; ++c) {
+        const int64_t r = gi * PB + c;
+        const double yr = (!freeMask || freeMask[r]) ? v[c] : x[r];
+        y[r] = yr;
+        acc = fma(x[r], yr, acc);
+      }
+    }
+  }
+  if (part) {
+    const double s = block_sum(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+  }
 }
 
 // y_r = free_r ? (K x)_r : x_r for rows r; with part != null also the block partials of x.y.
@@ -297,6 +386,130 @@ __global__ void __launch_bounds__(NT) pcg_direction_kernel(int64_t n, int cur, i
   }
 }
 
+// y = alpha A x + beta y over the rows of a CSR matrix with FP64 arithmetic (rectangular allowed);
+// with freeMask, row r is the identity where freeMask[r] == 0 (then A is square).  beta == 0: y is
+// not read.
+template <typename KT>
+__global__ void __launch_bounds__(NT) gemv_kernel(int64_t nRows, const int32_t* __restrict__ indptr,
+                                                  const int32_t* __restrict__ indices, const KT* __restrict__ A,
+                                                  const uint8_t* __restrict__ freeMask, const double* __restrict__ x,
+                                                  double alpha, double beta, double* __restrict__ y) {
+  const int lane = threadIdx.x % 32, g = lane / G, sl = lane % G;
+  constexpr int RPW = 32 / G;
+  const int64_t warp = ((int64_t)blockIdx.x * NT + threadIdx.x) / 32;
+  const int64_t nw = (int64_t)gridDim.x * WARPS;
+  // the loop condition depends on the warp only: all 32 lanes reach every shuffle
+  for (int64_t rb = warp * RPW; rb < nRows; rb += nw * RPW) {
+    const int64_t r = rb + g;
+    const bool live = r < nRows;
+    const int32_t b = live ? indptr[r] : 0, e = live ? indptr[r + 1] : 0;
+    const double v = row_product(b, e, indices, A, x, sl);
+    if (live && sl == 0) {
+      const double ax = (!freeMask || freeMask[r]) ? v : x[r];
+      y[r] = beta == 0.0 ? alpha * ax : fma(alpha, ax, beta * y[r]);
+    }
+  }
+}
+
+// y = alpha A x + beta y with float values and x given as float-float pairs xf[i] = (hi, lo):
+// products and row sums in float-float arithmetic on the FP32 pipe (as the CG products of FP32
+// tangents), one conversion to double per row.  Masked rows are the identity (x_r = hi + lo).
+__global__ void __launch_bounds__(NT) gemv_pairs_kernel(int64_t nRows, const int32_t* __restrict__ indptr,
+                                                        const int32_t* __restrict__ indices,
+                                                        const float* __restrict__ A,
+                                                        const uint8_t* __restrict__ freeMask,
+                                                        const float2* __restrict__ xf, double alpha, double beta,
+                                                        double* __restrict__ y) {
+  const int lane = threadIdx.x % 32, g = lane / G, sl = lane % G;
+  constexpr int RPW = 32 / G;
+  const int64_t warp = ((int64_t)blockIdx.x * NT + threadIdx.x) / 32;
+  const int64_t nw = (int64_t)gridDim.x * WARPS;
+  for (int64_t rb = warp * RPW; rb < nRows; rb += nw * RPW) {
+    const int64_t r = rb + g;
+    const bool live = r < nRows;
+    const int32_t b = live ? indptr[r] : 0, e = live ? indptr[r + 1] : 0;
+    const double v = row_product_ff(b, e, indices, A, xf, sl);
+    if (live && sl == 0) {
+      double ax = v;
+      if (freeMask && !freeMask[r]) {
+        const float2 xr = xf[r];
+        ax = (double)xr.x + (double)xr.y;
+      }
+      y[r] = beta == 0.0 ? alpha * ax : fma(alpha, ax, beta * y[r]);
+    }
+  }
+}
+
+// The same product with one thread per row, for matrices whose rows hold a few entries (the
+// prolongation between levels: one entry per row), where eight lanes per row would mostly idle.
+template <typename KT>
+__global__ void __launch_bounds__(NT) gemv_rows_kernel(int64_t nRows, const int32_t* __restrict__ indptr,
+                                                       const int32_t* __restrict__ indices, const KT* __restrict__ A,
+                                                       const uint8_t* __restrict__ freeMask,
+                                                       const double* __restrict__ x, double alpha, double beta,
+                                                       double* __restrict__ y) {
+  for (int64_t r = (int64_t)blockIdx.x * NT + threadIdx.x; r < nRows; r += (int64_t)gridDim.x * NT) {
+    double v = 0.0;
+    const int32_t e = indptr[r + 1];
+    for (int32_t j = indptr[r]; j < e; ++j) v = fma((double)A[j], x[indices[j]], v);
+    const double ax = (!freeMask || freeMask[r]) ? v : x[r];
+    y[r] = beta == 0.0 ? alpha * ax : fma(alpha, ax, beta * y[r]);
+  }
+}
+
+// gemv_pairs_kernel over node row groups of PB rows sharing one column list.
+template <int PB>
+__global__ void __launch_bounds__(NT) gemv_pairs_group_kernel(int64_t nRows, const int32_t* __restrict__ indptr,
+                                                              const int32_t* __restrict__ indices,
+                                                              const float* __restrict__ A,
+                                                              const uint8_t* __restrict__ freeMask,
+                                                              const float2* __restrict__ xf, double alpha, double beta,
+                                                              double* __restrict__ y) {
+  const int lane = threadIdx.x % 32, g = lane / G, sl = lane % G;
+  constexpr int GPW = 32 / G;
+  const int64_t warp = ((int64_t)blockIdx.x * NT + threadIdx.x) / 32;
+  const int64_t nw = (int64_t)gridDim.x * WARPS;
+  const int64_t nGroups = nRows / PB;
+  for (int64_t gb = warp * GPW; gb < nGroups; gb += nw * GPW) {
+    const int64_t gi = gb + g;
+    const bool live = gi < nGroups;
+    double v[PB];
+    group_product_ff<PB>(indptr, gi * PB, live, indices, A, xf, sl, v);
+    if (live && sl == 0) {
+#pragma unroll
+      for (int c = 0; c < PB; ++c) {
+        const int64_t r = gi * PB + c;
+        double ax = v[c];
+        if (freeMask && !freeMask[r]) {
+          const float2 xr = xf[r];
+          ax = (double)xr.x + (double)xr.y;
+        }
+        y[r] = beta == 0.0 ? alpha * ax : fma(alpha, ax, beta * y[r]);
+      }
+    }
+  }
+}
+
+// One Chebyshev smoother step on point-Jacobi-scaled residuals: d = c1 d + c2 dinv r (d not read
+// when c1 == 0), then z += d (accumulate) or z = d; with dff, also d as float-float pairs.
+__global__ void __launch_bounds__(NT) chebyshev_kernel(int64_t n, const double* __restrict__ dinv,
+                                                       const double* __restrict__ r, double c1, double c2,
+                                                       int accumulate, double* __restrict__ d,
+                                                       double* __restrict__ z, float2* __restrict__ dff) {
+  for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
+    const double s = c2 * (dinv[i] * r[i]);
+    const double di = c1 == 0.0 ? s : fma(c1, d[i], s);
+    d[i] = di;
+    z[i] = accumulate ? z[i] + di : di;
+    if (dff) split_ff(di, dff, i);
+  }
+}
+
+// xf[i] = (hi, lo) with hi = fl32(x_i), lo = fl32(x_i - hi)
+__global__ void __launch_bounds__(NT) split_kernel(int64_t n, const double* __restrict__ x, float2* __restrict__ xf) {
+  for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) split_ff(x[i], xf, i);
+}
+
 int vec_blocks(int64_t n, int sms) {
   int64_t b = (n + NT - 1) / NT;
   const int64_t cap = (int64_t)sms * 4;
@@ -334,6 +547,19 @@ cudaError_t spmv_t(const EfePcg& s, const double* x, const float2* xf, double* y
   return cudaGetLastError();
 }
 
+// float-float product of an FP32 tangent, over node row groups where the pattern has them
+cudaError_t spmv_pairs(const EfePcg& s, const double* x, const float2* xf, double* y, double* part, int nb,
+                       cudaStream_t st) {
+  const float* K = static_cast<const float*>(s.Kdata);
+  if (s.patternBlock == 3 && s.n % 3 == 0)
+    spmv_group_ff_kernel<3><<<nb, NT, 0, st>>>(s.n, s.indptr, s.indices, K, s.freeMask, x, xf, y, part);
+  else if (s.patternBlock == 2 && s.n % 2 == 0)
+    spmv_group_ff_kernel<2><<<nb, NT, 0, st>>>(s.n, s.indptr, s.indices, K, s.freeMask, x, xf, y, part);
+  else
+    return spmv_t<float, true>(s, x, xf, y, part, nb, st);
+  return cudaGetLastError();
+}
+
 // FP64 arithmetic product (any x)
 cudaError_t spmv(const EfePcg& s, const double* x, double* y, double* part, int nb, cudaStream_t st) {
   return s.kPrecision == EFE_K_FP64 ? spmv_t<double, false>(s, x, nullptr, y, part, nb, st)
@@ -341,6 +567,55 @@ cudaError_t spmv(const EfePcg& s, const double* x, double* y, double* part, int 
 }
 
 }  // namespace
+
+cudaError_t csr_gemv(const EfeCsr& a, const double* x, double alpha, double beta, double* y, cudaStream_t st) {
+  if (a.nRows == 0) return cudaSuccess;
+  if (a.nnz <= 2 * a.nRows) {  // short rows: one thread per row
+    const int nv = vec_blocks(a.nRows, sm_count());
+    if (a.kPrecision == EFE_K_FP64)
+      gemv_rows_kernel<double><<<nv, NT, 0, st>>>(a.nRows, a.indptr, a.indices, static_cast<const double*>(a.values),
+                                                  a.freeMask, x, alpha, beta, y);
+    else
+      gemv_rows_kernel<float><<<nv, NT, 0, st>>>(a.nRows, a.indptr, a.indices, static_cast<const float*>(a.values),
+                                                 a.freeMask, x, alpha, beta, y);
+    return cudaGetLastError();
+  }
+  const int nb = spmv_blocks(a.nRows, sm_count());
+  if (a.kPrecision == EFE_K_FP64)
+    gemv_kernel<double><<<nb, NT, 0, st>>>(a.nRows, a.indptr, a.indices, static_cast<const double*>(a.values),
+                                           a.freeMask, x, alpha, beta, y);
+  else
+    gemv_kernel<float><<<nb, NT, 0, st>>>(a.nRows, a.indptr, a.indices, static_cast<const float*>(a.values),
+                                          a.freeMask, x, alpha, beta, y);
+  return cudaGetLastError();
+}
+
+cudaError_t csr_gemv_pairs(const EfeCsr& a, const float2* xf, double alpha, double beta, double* y,
+                           cudaStream_t st) {
+  if (a.nRows == 0) return cudaSuccess;
+  const int nb = spmv_blocks(a.nRows, sm_count());
+  const float* A = static_cast<const float*>(a.values);
+  if (a.rowBlock == 3 && a.nRows % 3 == 0 && a.nRows == a.nCols)
+    gemv_pairs_group_kernel<3><<<nb, NT, 0, st>>>(a.nRows, a.indptr, a.indices, A, a.freeMask, xf, alpha, beta, y);
+  else if (a.rowBlock == 2 && a.nRows % 2 == 0 && a.nRows == a.nCols)
+    gemv_pairs_group_kernel<2><<<nb, NT, 0, st>>>(a.nRows, a.indptr, a.indices, A, a.freeMask, xf, alpha, beta, y);
+  else
+    gemv_pairs_kernel<<<nb, NT, 0, st>>>(a.nRows, a.indptr, a.indices, A, a.freeMask, xf, alpha, beta, y);
+  return cudaGetLastError();
+}
+
+cudaError_t chebyshev_step(int64_t n, const double* dinv, const double* r, double c1, double c2, int accumulate,
+                           double* d, double* z, float2* dff, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  chebyshev_kernel<<<vec_blocks(n, sm_count()), NT, 0, st>>>(n, dinv, r, c1, c2, accumulate, d, z, dff);
+  return cudaGetLastError();
+}
+
+cudaError_t split_pairs(int64_t n, const double* x, float2* xf, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  split_kernel<<<vec_blocks(n, sm_count()), NT, 0, st>>>(n, x, xf);
+  return cudaGetLastError();
+}
 
 cudaError_t csr_spmv(const EfePcg& s, const double* x, double* y, cudaStream_t st) {
   if (s.n == 0) return cudaSuccess;
@@ -366,7 +641,7 @@ cudaError_t pcg_iterate(const EfePcg& s, int64_t k0, int nIter, cudaStream_t st)
   float2* pf = pff(s);
   for (int k = 0; k < nIter; ++k) {
     const int cur = (int)((k0 + k) & 1);
-    cudaError_t e = pf ? spmv_t<float, true>(s, s.p, pf, s.Ap, s.work + PART0, nbS, st)
+    cudaError_t e = pf ? spmv_pairs(s, s.p, pf, s.Ap, s.work + PART0, nbS, st)
                        : spmv(s, s.p, s.Ap, s.work + PART0, nbS, st);
     if (e != cudaSuccess) return e;
     switch (s.blockSize) {

@@ -149,7 +149,7 @@ class NISTGPU:
     def __init__(self, assembler, linsolver="pcg", extrapolation="linear", maxIter=10, criticalIter=5,
                  maxGrowingIter=10, fluxResidualTolerance=1e-8, fluxResidualToleranceAlternative=5e-3,
                  fieldCorrectionTolerance=1e-8, pcgTolerance=1e-12, pcgMaxIter=20000, fluxResidualFloor=1e-7,
-                 pcgPreconditioner="jacobi", pcgGraphs=True):  # fmt: skip
+                 pcgPreconditioner="jacobi", pcgGraphs=True, amgOptions=None):  # fmt: skip
         self.asm = assembler
         self.linsolver = linsolver
         self.extrapolation = extrapolation
@@ -169,6 +169,10 @@ class NISTGPU:
         # replay the PCG iteration batches of long solves as one CUDA graph (same kernels and
         # arguments as the direct launches, so the same results bit for bit)
         self.pcgGraphs = pcgGraphs
+        # "amg": aggregation multigrid V-cycles (amg.AggregationAMG, built once per set of
+        # prescribed DOFs, its level operators once per tangent)
+        self.amgOptions = dict(amgOptions or {})
+        self._amg = None
         self.nAccumulatedFluxes = sum(len(g.conn) * len(g.conn[0]) * assembler.dim for g in assembler.groups if len(g.conn))
         dev = assembler.device
         ip, ix = assembler.indptr_host, assembler.indices_host
@@ -343,6 +347,8 @@ class NISTGPU:
 
         from . import _lib as L
 
+        if self.pcgPreconditioner == "amg":
+            return self._solve_pcg_amg(K, R, dir_idx)
         asm = self.asm
         dev = asm.device
         n = asm.nDof
@@ -370,7 +376,7 @@ class NISTGPU:
         split = torch.empty((n, 2), dtype=torch.float32, device=dev) if kp == L.EFE_K_FP32 else None
         s = L.EfePcg(n, asm.indptr.data_ptr(), asm.indices.data_ptr(), K.data_ptr(), kp, m.data_ptr(), dinv.data_ptr(),
                      *[vec[i].data_ptr() for i in range(5)], work.data_ptr(),
-                     split.data_ptr() if split is not None else None, bs)  # fmt: skip
+                     split.data_ptr() if split is not None else None, bs, asm.rowGroup)  # fmt: skip
         stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
         xd = (1.0 - mf) * R
         Kxd = torch.empty_like(R)
@@ -408,13 +414,101 @@ class NISTGPU:
         self.linearIterations.append(k)
         return vec[0] + xd
 
+    def _solve_pcg_amg(self, K, R, dir_idx):
+        """CG on the same system as _solve_pcg, preconditioned by one aggregation-multigrid V-cycle
+        per iteration (amg.AggregationAMG).  Same convergence test, checked once per batch of 10
+        iterations one batch behind; with pcgGraphs, from the third batch on a batch (its products,
+        V-cycles and reductions: ~50 launches per iteration) is replayed as one CUDA graph."""
+        from .amg import AggregationAMG
+
+        asm = self.asm
+        dev = asm.device
+        n = asm.nDof
+        m = torch.ones(n, dtype=torch.uint8, device=dev)
+        if dir_idx is not None:
+            m[dir_idx] = 0
+        h = self._amg
+        if h is None or not torch.equal(h.levels[0].mask, m):
+            self._amg = h = None  # release the previous hierarchy before building the next
+            h = AggregationAMG(asm.indptr, asm.indices, m, asm.dim, rowGroup=asm.rowGroup, **self.amgOptions)
+            self._amg = h
+        h.update(K, self._diag_pos)
+        A = h.levels[0].A
+        mf = m.to(torch.float64)
+        xd = (1.0 - mf) * R
+        Kxd = torch.empty_like(R)
+        h._gemv(A, xd, 1.0, 0.0, Kxd)
+        r = mf * (R - Kxd)
+        bnorm = float(torch.linalg.vector_norm(r + xd))
+        tol2 = (self.pcgTolerance * bnorm) ** 2
+        x = torch.zeros_like(R)
+        k = 0
+        if bnorm > 0.0 and float(torch.dot(r, r)) > tol2:
+            z = torch.empty_like(R)
+            Ap = torch.empty_like(R)
+            pairs = torch.empty((n, 2), dtype=torch.float32, device=dev)
+            h.apply(r, z)
+            p = z.clone()
+            rz = torch.dot(r, z)  # the scalars live on the device and are updated in place
+            pApLast = torch.zeros((), dtype=torch.float64, device=dev)
+            rrLast = torch.zeros((), dtype=torch.float64, device=dev)
+            zero = torch.zeros((), dtype=torch.float64, device=dev)
+
+            def iterate(count):
+                for _ in range(count):
+                    h.product(p, Ap, pairs)
+                    pAp = torch.dot(p, Ap)
+                    alpha = torch.where(pAp != 0.0, rz / pAp, zero)
+                    x.addcmul_(alpha, p)
+                    r.addcmul_(alpha, Ap, value=-1.0)
+                    h.apply(r, z)
+                    rzNew = torch.dot(r, z)
+                    beta = torch.where(rz != 0.0, rzNew / rz, zero)
+                    p.mul_(beta).add_(z)
+                    rz.copy_(rzNew)
+                pApLast.copy_(pAp)
+                rrLast.copy_(torch.dot(r, r))
+
+            seen = torch.empty((2, 2), dtype=torch.float64, pin_memory=True)  # r.r, p.Ap of two batches
+            done = [torch.cuda.Event(), torch.cuda.Event()]
+            graph = None
+            batch = 0
+            while k < self.pcgMaxIter:
+                step = min(10, self.pcgMaxIter - k)
+                if self.pcgGraphs and step == 10 and k >= 20:
+                    if graph is None:
+                        graph = self._capture(lambda: iterate(10))
+                    graph.replay()
+                else:
+                    iterate(step)
+                k += step
+                seen[batch % 2, 0].copy_(rrLast, non_blocking=True)
+                seen[batch % 2, 1].copy_(pApLast, non_blocking=True)
+                done[batch % 2].record()
+                batch += 1
+                if batch < 2:
+                    continue
+                done[batch % 2].synchronize()  # the previous batch (the one just queued still runs)
+                rr, pApSeen = seen[batch % 2].tolist()
+                if not rr <= tol2 and rr == rr and pApSeen != 0.0:  # not converged, no NaN, no breakdown
+                    continue
+                break
+        self.linearIterations.append(k)
+        return x + xd
+
     def _capture_pcg_batch(self, lib, s, k, step):
-        """One batch of `step` PCG iterations starting at iteration k (even) as a CUDA graph, captured
-        on a side stream; replay() runs it on the current stream."""
+        """One batch of `step` PCG iterations starting at iteration k (even) as a CUDA graph."""
         import ctypes
 
         from . import _lib as L
 
+        dev = self.asm.device
+        return self._capture(lambda: L.check(lib.efe_pcg_iterate(ctypes.byref(s), k, step, ctypes.c_void_p(
+            torch.cuda.current_stream(dev).cuda_stream)), "efe_pcg_iterate (graph capture)"))  # fmt: skip
+
+    def _capture(self, fn):
+        """The launches of fn() as a CUDA graph, captured on a side stream (fn launches on the
+        current stream); replay() runs them on the current stream."""
         dev = self.asm.device
         graph = torch.cuda.CUDAGraph()
         side = torch.cuda.Stream(dev)
@@ -422,9 +516,8 @@ class NISTGPU:
         with torch.cuda.stream(side):
             graph.capture_begin()
             try:
-                rc = lib.efe_pcg_iterate(ctypes.byref(s), k, step, ctypes.c_void_p(side.cuda_stream))
+                fn()
             finally:
                 graph.capture_end()
-        L.check(rc, "efe_pcg_iterate (graph capture)")
         torch.cuda.current_stream(dev).wait_stream(side)
         return graph

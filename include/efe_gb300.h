@@ -269,11 +269,48 @@ typedef struct EfePcg {
                               float-float arithmetic on p = pFF[i][0] + pFF[i][1] (FP32 pipe);
                               NULL: FP64 arithmetic                                            */
   int32_t blockSize;       /* 1, 2 or 3 DOFs per preconditioner block (n a multiple of it)     */
+  int32_t patternBlock;    /* 2 or 3: rows come in aligned groups of that many that share one
+                              column list (a node's DOF rows; efe_pattern_fill's pattern when
+                              every node's first DOF is a multiple of it): the float-float
+                              product reads each column index once per group; 0 or 1: none */
 } EfePcg;
 /* y_i = free_i ? (K x)_i : x_i */
 int32_t efe_csr_spmv(const EfePcg* solver, const double* x, double* y, void* stream);
 int32_t efe_pcg_start(const EfePcg* solver, const double* b, void* stream);
 int32_t efe_pcg_iterate(const EfePcg* solver, int64_t firstIteration, int32_t nIterations, void* stream);
+
+/* Building blocks of a multilevel (aggregation) preconditioner for the same systems; the reference
+   reaches multilevel methods only through external solvers behind linearSolve
+   (solvers/nonlinearimplicitstatic.py:727-751), so these have no counterpart of their own.
+   efe_csr_gemv: y = alpha A x + beta y for an int32 CSR matrix of nRows rows (rectangular allowed:
+   the transfer operators between levels); values double or float per kPrecision (EFE_K_FP32 and
+   EFE_K_FP32_FF both mean float values here), FP64 arithmetic in a fixed order per row.  With
+   freeMask (then nCols == nRows), row r is the identity where freeMask[r] == 0.  beta == 0: y is
+   only written.  x and y must not overlap.
+   efe_csr_gemv_pairs: the same for float values (EFE_K_FP32 / EFE_K_FP32_FF) with x given as n
+   float-float pairs xPairs[i] = (hi, lo), x_i = hi + lo (8-byte aligned): products and row sums in
+   float-float arithmetic on the FP32 pipe, ~2^-48 relative to sum |A_ij x_j|.
+   efe_chebyshev_step: d = c1 d + c2 dinv r (d not read when c1 == 0), then z += d (accumulate != 0)
+   or z = d, for vectors of n doubles: the vector part of one step of a Chebyshev smoother in the
+   point-Jacobi-scaled operator; dPairs (optional, 8-byte aligned) receives d as float-float pairs.
+   efe_split_pairs: pairs[i] = (fl32(x_i), fl32(x_i - fl32(x_i))). */
+typedef struct EfeCsr {
+  int64_t nRows;
+  int64_t nCols;
+  int64_t nnz;             /* indptr[nRows]; rows of at most two entries on average take a
+                              one-thread-per-row kernel */
+  const int32_t* indptr;   /* [nRows + 1] */
+  const int32_t* indices;  /* [nnz], each < nCols */
+  const void* values;      /* [nnz] double or float */
+  int32_t kPrecision;
+  const uint8_t* freeMask; /* [nRows] or NULL */
+  int32_t rowBlock;        /* as EfePcg.patternBlock, for efe_csr_gemv_pairs of a square matrix */
+} EfeCsr;
+int32_t efe_csr_gemv(const EfeCsr* A, const double* x, double alpha, double beta, double* y, void* stream);
+int32_t efe_csr_gemv_pairs(const EfeCsr* A, const float* xPairs, double alpha, double beta, double* y, void* stream);
+int32_t efe_chebyshev_step(int64_t n, const double* dinv, const double* r, double c1, double c2, int32_t accumulate,
+                           double* d, double* z, float* dPairs, void* stream);
+int32_t efe_split_pairs(int64_t n, const double* x, float* pairs, void* stream);
 
 /* acceptLastState: stateTemp -> stateRef and auxTemp -> auxRef for every group. */
 int32_t efe_accept_state(const EfeGroup* groups, int32_t nGroups, void* stream);

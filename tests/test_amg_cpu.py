@@ -1,0 +1,103 @@
+"""Set-up of the aggregation multigrid preconditioner on the CPU (the functions are device-agnostic
+torch code; the cycle itself runs through the CUDA kernels and is tested in test_gpu_amg.py):
+the point graph against the CSR pattern, the aggregation (an independent set of roots, every point
+next to its root), the Galerkin map S against SciPy's P^T A P, and the Chebyshev smoother's
+polynomial against the min-max bound 1 / T_k."""
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+torch = pytest.importorskip("torch")
+
+from edelweissfe_gb300 import amg, meshes  # noqa: E402
+from edelweissfe_gb300.pattern import build_pattern  # noqa: E402
+
+
+def _box_pattern(nx, ny, nz, nNodes=8):
+    coords, conn, nodeDof, nDof = meshes.box(nx, ny, nz, nNodes=nNodes)
+    indptr, indices = build_pattern(3, len(coords), nodeDof, nDof, [conn])[:2]
+    return coords, np.asarray(indptr), np.asarray(indices), nDof
+
+
+def test_point_graph_matches_pattern():
+    _, ip, ix, n = _box_pattern(3, 2, 2)
+    src, dst = amg.point_graph(torch.from_numpy(ip), torch.from_numpy(ix), 3)
+    got = set(zip(src.tolist(), dst.tolist()))
+    want = {(p, int(c) // 3) for p in range(n // 3) for c in ix[ip[3 * p] : ip[3 * p + 1]]}
+    assert got == want
+    assert all((p, p) in got for p in range(n // 3))
+
+
+@pytest.mark.parametrize("nNodes", [8, 20])
+def test_aggregation_is_a_maximal_independent_set(nNodes):
+    _, ip, ix, n = _box_pattern(5, 4, 3, nNodes)
+    src, dst = amg.point_graph(torch.from_numpy(ip), torch.from_numpy(ix), 3)
+    points = n // 3
+    agg, nAgg, roots = amg.mis_aggregate(src, dst, points, seed=3)
+    agg2, nAgg2, _ = amg.mis_aggregate(src, dst, points, seed=3)
+    assert torch.equal(agg, agg2) and nAgg == nAgg2
+    s, d = src.numpy(), dst.numpy()
+    r = roots.numpy()
+    off = s != d
+    assert not np.any(r[s[off]] & r[d[off]])  # no two roots adjacent
+    a = agg.numpy()
+    assert sorted(set(a.tolist())) == list(range(nAgg))
+    rootOfAgg = np.empty(nAgg, np.int64)
+    rootOfAgg[a[r]] = np.nonzero(r)[0]
+    adj = set(zip(s.tolist(), d.tolist()))
+    for p in range(points):  # every point is its aggregate's root or next to it
+        q = rootOfAgg[a[p]]
+        assert p == q or (p, q) in adj
+    assert 1.5 < points / nAgg < 40
+
+
+def test_galerkin_map_and_transfer_match_scipy():
+    coords, ip, ix, n = _box_pattern(4, 3, 3)
+    rng = np.random.default_rng(0)
+    vals = rng.normal(size=len(ix))
+    A = sp.csr_matrix((vals, ix, ip), shape=(n, n))
+    A = (A + A.T).tocsr()  # symmetric values on the same pattern
+    A.sort_indices()
+    ipT, ixT = torch.from_numpy(A.indptr.astype(np.int32)), torch.from_numpy(A.indices.astype(np.int32))
+    src, dst = amg.point_graph(ipT, ixT, 3)
+    agg, nAgg, _ = amg.mis_aggregate(src, dst, n // 3, seed=1)
+    nc = nAgg * 3
+    mask = torch.ones(n, dtype=torch.float64)
+    mask[torch.from_numpy(np.arange(0, n, 7))] = 0.0  # some prescribed DOFs
+    coarseOfDof = torch.repeat_interleave(agg, 3) * 3 + torch.arange(n) % 3
+    cnt = torch.zeros(nc, dtype=torch.float64).index_add_(0, coarseOfDof, mask)
+    w = mask / torch.sqrt(torch.clamp(cnt, min=1.0))[coarseOfDof]
+    (Pp, Pi, Pv), (Rp, Ri, Rv) = amg.transfer(coarseOfDof, w, nc)
+    P = sp.csr_matrix((Pv.numpy(), Pi.numpy(), Pp.numpy()), shape=(n, nc))
+    R = sp.csr_matrix((Rv.numpy(), Ri.numpy(), Rp.numpy()), shape=(nc, n))
+    assert abs(R - P.T).max() == 0.0
+    # columns of P are orthonormal on the aggregates that hold a free DOF
+    G = (P.T @ P).toarray()
+    assert np.allclose(G, np.diag((cnt.numpy() > 0).astype(float)), atol=1e-15)
+    (cp, ci), (Sp, Si, Sv), diag = amg.galerkin_map(ipT, ixT, coarseOfDof, w, nc)
+    S = sp.csr_matrix((Sv.numpy(), Si.numpy(), Sp.numpy()), shape=(len(Sp) - 1, A.nnz))
+    Ac = sp.csr_matrix((S @ A.data, ci.numpy(), cp.numpy()), shape=(nc, nc))
+    ref = (P.T @ A @ P).tocsr()
+    assert abs(Ac - ref).max() <= 1e-13 * abs(ref).max()
+    assert np.all(ci.numpy()[diag.numpy()] == np.arange(nc))
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3, 4])
+def test_chebyshev_polynomial_meets_the_minmax_bound(degree):
+    lmax = 3.7
+    coeffs = amg.chebyshev_coefficients(lmax, degree)
+    a, b = lmax / 30.0, 1.1 * lmax
+    theta, delta = 0.5 * (a + b), 0.5 * (b - a)
+    bound = 1.0 / np.cosh(degree * np.arccosh(theta / delta))
+    lam = np.linspace(a, b, 2001)
+    # scalar run of the smoother from z = 0 on A = lam, D = 1, r = 1 (as the kernels do it)
+    res, d, z = np.ones_like(lam), np.zeros_like(lam), np.zeros_like(lam)
+    for k, (c1, c2) in enumerate(coeffs):
+        if k > 0:
+            res = res - lam * d
+        d = c1 * d + c2 * res
+        z = z + d
+    err = 1.0 - lam * z
+    assert np.max(np.abs(err)) <= bound * (1 + 1e-12)
+    assert np.max(np.abs(err)) >= bound * (1 - 1e-9)  # equioscillation: the bound is attained
