@@ -12,7 +12,7 @@ Hierarchy.  Level 0 is the tangent as assembled (double or float CSR data, int32
 identity rows on the prescribed DOFs.  A point is a block of `bs` consecutive DOFs (a node's
 displacement components, the DofManager's node-major numbering).  Points are aggregated around
 the roots of a maximal independent set of the point graph (random priorities, one neighbour-max
-per round, every other point joins its highest-priority root neighbour); the coarse space holds
+per sweep, every other point joins its highest-priority root neighbour); the coarse space holds
 the translations of every aggregate: coarse DOF I = aggregate * bs + component, prolongation
 P[i, I] = 1 / sqrt(number of free fine DOFs in I) on free DOFs, 0 on prescribed ones.  The
 coarse operator is the Galerkin product P^T A P, summed in a fixed order through a precomputed
@@ -34,7 +34,6 @@ the point-Jacobi CG products do; coarse levels hold FP64 values.
 
 import ctypes
 
-import numpy as np
 import torch
 
 from . import _lib as L
@@ -58,14 +57,14 @@ def point_graph(indptr, indices, bs):
     return src, dst
 
 
-def mis_aggregate(src, dst, points, seed=0, maxRounds=200):
+def mis_aggregate(src, dst, points, seed=0, maxSweeps=200):
     """Aggregates around the roots of a maximal independent set of the point graph.  Returns
     (agg [points] int64, nAgg, roots [points] bool).  Deterministic for a given seed."""
     dev = src.device
     g = torch.Generator().manual_seed(seed)
     prio = torch.randperm(points, generator=g).to(dev)
     state = torch.full((points,), _UNDECIDED, dtype=torch.int64, device=dev)
-    for _ in range(maxRounds):
+    for _ in range(maxSweeps):
         und = state == _UNDECIDED
         if not bool(und.any()):
             break
@@ -76,7 +75,7 @@ def mis_aggregate(src, dst, points, seed=0, maxRounds=200):
         out = und & ((mx >> _PRIO_BITS) == _ROOT)
         state[newRoot] = _ROOT
         state[out] = _OUT
-    state[state == _UNDECIDED] = _ROOT  # after maxRounds: the rest are roots of their own (each round adds >= 1)
+    state[state == _UNDECIDED] = _ROOT  # after maxSweeps: the rest are roots of their own (each sweep adds >= 1)
     roots = state == _ROOT
     aggOfRoot = torch.cumsum(roots.to(torch.int64), 0) - 1
     nAgg = int(roots.sum())
@@ -109,7 +108,9 @@ def transfer(coarseOfDof, w, nc):
 def galerkin_map(indptr, indices, coarseOfDof, w, nc):
     """Pattern of P^T A P and the map S that sums it: coarse CSR (indptr, indices int32), S as CSR
     (nnz_c x nnz_f: indptr, indices int32, values w_i w_j in fine-entry order per coarse entry),
-    and the position of every coarse diagonal entry."""
+    and the position of every coarse diagonal entry.  Transient memory: a few int64 arrays of the
+    fine entry count and one sort of them (tens of GB at 10^9 entries); S keeps 12 bytes per fine
+    entry."""
     n = indptr.numel() - 1
     dev = indices.device
     ip = indptr.to(torch.int64)
