@@ -290,6 +290,12 @@ class GPUAssembler:
             )
         return torch.sparse_csr_tensor(self.indptr, self.indices, K, size=(self.nDof, self.nDof))
 
+    def computeDistributedLoad(self, loadType, P, K, faceID, load, U, time, dTime):
+        """Surface loads: the reference's displacement elements of this provider do not support them
+        and raise (`elements/displacementelement/element.py:255-288`,
+        `elements/displacementtlelement/element.py:311-344`); so does this."""
+        raise Exception("Applying a distributed load is currently not possible with this element provider.")
+
     def computeBodyForce(self, P, force, elements=None):
         """Add the body force `force` [dim] of the given global element indices (default: all) to P
         (NIST.computeBodyForces, nonlinearimplicitstatic.py:520-557)."""

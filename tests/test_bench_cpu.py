@@ -57,3 +57,4 @@ def test_roofline_fraction_is_achieved_over_peak():
     assert r["achieved"] == pytest.approx(2000.0)
     assert r["frac"] == pytest.approx(2000.0 / peak)
     assert r["traffic"] == 3.0e9
+

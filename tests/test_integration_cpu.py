@@ -79,3 +79,12 @@ def test_arrays_from_reference_reproduce_compute_elements(ref, dim, gen, lines, 
     assert np.array_equal(om.indptr, Kc.indptr) and np.array_equal(om.indices, Kc.indices)
     assert np.abs(r["P"] - P).max() <= 1e-12 * np.abs(P).max()
     assert np.abs(r["Kdata"] - Kc.data).max() <= 1e-12 * np.abs(Kc.data).max()
+
+
+def test_distributed_loads_raise_like_the_reference():
+    """The reference's displacement elements of the edelweiss provider raise on surface loads; the
+    assembler's computeDistributedLoad does the same (no device needed to reach the raise)."""
+    from edelweissfe_gb300.assembly import GPUAssembler
+
+    with pytest.raises(Exception, match="distributed load is currently not possible"):
+        GPUAssembler.computeDistributedLoad(None, "pressure", None, None, 1, [1.0], None, (0.0, 0.0), 0.1)
