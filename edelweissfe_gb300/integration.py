@@ -86,14 +86,37 @@ def arrays_from_reference(elements, dofManager):
     return coords, nodeDof, int(dofManager.nDof), groups
 
 
-def make_nist_gpu(NIST, precision="fp64"):
+def write_back_state(asm, elements):
+    """Copy the assembler's accepted quadrature-point state into the reference element objects, in
+    place: `_stateVarsRef` and the rows of `_stateVarsTemp` ([nInt][12 + m] per element,
+    `elements/displacementelement/element.py:222-235`, `elements/displacementtlelement/element.py`
+    likewise), whose rows hold the same [stress, strain, material state] in the element family's
+    Voigt order as the device state.  Everything that reads results from the element objects --
+    the persistent views of `getResultArray` (element.py:386-409), the reference's
+    ElementResultCollector and field outputs, the output managers -- then sees the GPU solution.
+    `elements`: the reference elements in the assembler's element order."""
+    elements = list(elements)
+    for gi, g in enumerate(asm.groups):
+        off = g._dev["offset"]
+        S = asm.group_state(gi, "ref")  # [E, nInt, 12 + m]
+        for k in range(S.shape[0]):
+            el = elements[off + k]
+            if el._stateVarsRef.shape != S.shape[1:]:
+                raise ValueError(f"element {off + k}: state shape {el._stateVarsRef.shape} != {S.shape[1:]}")
+            el._stateVarsRef[...] = S[k]
+            for q in range(S.shape[1]):  # an array, or a list of rows once computeYourself ran (element.py:320)
+                el._stateVarsTemp[q][...] = S[k, q]
+
+
+def make_nist_gpu(NIST, precision="fp64", writeBackState=True):
     """A NIST subclass whose element loop and CSR assembly run on the GPU.
 
     The reference's solveIncrement keeps its host DOF vectors: computeElements copies U_np and dU to
     the device, runs the element pass, and adds P and |P_e| back into the host vectors; the
     tangent stays on the device until assembleStiffnessCSR returns it as the scipy CSR matrix the
     linear solvers expect.  Accepting a converged increment (FEModel.advanceToTime) also accepts
-    the device state."""
+    the device state and, with writeBackState, copies it into the reference element objects
+    (write_back_state) before the field outputs and output managers of that increment read them."""
     import torch
 
     from .assembly import GPUAssembler
@@ -106,6 +129,7 @@ def make_nist_gpu(NIST, precision="fp64"):
                 coords, nodeDof, nDof, groups = arrays_from_reference(elements.values(), self.theDofManager)
                 self._gpuAssembler = GPUAssembler(coords, nodeDof, nDof, groups, precision=precision)
                 self._gpuDofManager = self.theDofManager
+                self._gpuElements = list(elements.values())
             return self._gpuAssembler
 
         def computeElements(self, elements, U_np, dU, P, K, F, timeStep):
@@ -128,6 +152,8 @@ def make_nist_gpu(NIST, precision="fp64"):
                 advance(time)
                 if getattr(self, "_gpuAssembler", None) is not None:
                     self._gpuAssembler.acceptLastState()
+                    if writeBackState:
+                        write_back_state(self._gpuAssembler, self._gpuElements)
 
             model.advanceToTime = advanceToTime
             try:
