@@ -95,6 +95,7 @@ def test_distributed_loads_raise_like_the_reference():
     [
         (3, "boxGen", ["nX=2", "nY=2", "nZ=1"], "C3D8", "vonmises", [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0]),
         (2, "planeRectQuad", ["nX=3", "nY=2"], "CPE8RTL", "neohookewa", [1000.0, 10000.0]),
+        (3, "boxGen", ["nX=2", "nY=1", "nZ=1"], "C3D8TL", "neohookewb", [1000.0, 10000.0]),
     ],
 )
 def test_write_back_reproduces_the_reference_state(ref, dim, gen, lines, et, kind, props):
