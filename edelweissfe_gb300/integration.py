@@ -108,6 +108,27 @@ def write_back_state(asm, elements):
                 el._stateVarsTemp[q][...] = S[k, q]
 
 
+def read_state_from_reference(asm, elements):
+    """The inverse of write_back_state: every reference element's `_stateVarsRef` into the
+    assembler's accepted state (stateRef and stateTemp, [field][element * nInt + qp]).  With the
+    write-back on, the element objects hold the accepted state at every step boundary, so reading
+    them at a step start picks up exactly what the reference's own elements would compute from,
+    including states set by step actions (`stepactions/setfield.py:95`, through the field outputs'
+    setResults)."""
+    import torch
+
+    elements = list(elements)
+    for g in asm.groups:
+        d = g._dev
+        off, n, nInt = d["offset"], len(g.conn), d["type"].nInt
+        host = np.stack([np.asarray(elements[off + k]._stateVarsRef, float) for k in range(n)])  # [E, nInt, S]
+        if host.shape[1] != nInt or host.shape[2] != d["stateRef"].shape[0]:
+            raise ValueError(f"reference state shape {host.shape[1:]} != device ({nInt}, {d['stateRef'].shape[0]})")
+        soa = torch.from_numpy(np.ascontiguousarray(host.reshape(n * nInt, -1).T)).to(d["stateRef"])
+        d["stateRef"].copy_(soa)
+        d["stateTemp"].copy_(soa)
+
+
 def make_nist_gpu(NIST, precision="fp64", writeBackState=True):
     """A NIST subclass whose element loop and CSR assembly run on the GPU.
 
@@ -116,7 +137,9 @@ def make_nist_gpu(NIST, precision="fp64", writeBackState=True):
     tangent stays on the device until assembleStiffnessCSR returns it as the scipy CSR matrix the
     linear solvers expect.  Accepting a converged increment (FEModel.advanceToTime) also accepts
     the device state and, with writeBackState, copies it into the reference element objects
-    (write_back_state) before the field outputs and output managers of that increment read them."""
+    (write_back_state) before the field outputs and output managers of that increment read them;
+    each later step then starts from the element objects' state (read_state_from_reference), as
+    the reference's own elements would."""
     import torch
 
     from .assembly import GPUAssembler
@@ -156,6 +179,8 @@ def make_nist_gpu(NIST, precision="fp64", writeBackState=True):
                         write_back_state(self._gpuAssembler, self._gpuElements)
 
             model.advanceToTime = advanceToTime
+            if writeBackState and getattr(self, "_gpuAssembler", None) is not None:
+                read_state_from_reference(self._gpuAssembler, self._gpuElements)
             try:
                 return super().solveStep(step, model, fieldOutputController, outputmanagers)
             finally:

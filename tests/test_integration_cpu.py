@@ -112,7 +112,7 @@ def test_write_back_reproduces_the_reference_state(ref, dim, gen, lines, et, kin
     from edelweissfe.timesteppers.timestep import TimeStep
 
     from edelweissfe_gb300.assembly import GPUAssembler
-    from edelweissfe_gb300.integration import arrays_from_reference, write_back_state
+    from edelweissfe_gb300.integration import arrays_from_reference, read_state_from_reference, write_back_state
     from oracle.assembly import Model
 
     h = [1.0 / 3] * dim
@@ -159,3 +159,13 @@ def test_write_back_reproduces_the_reference_state(ref, dim, gen, lines, et, kin
     if collector is not None:  # the reference's field-output path reads the written-back state
         got = np.asarray(collector.getCurrentResults())
         assert np.abs(got - np.array([w[:, 0:6] for w in want])).max() <= 1e-12 * scale
+    # and back: a state set on the element objects (as a step action does) reaches the device layout
+    for el in elements:
+        el._stateVarsRef[:, 0] = 7.0
+    g0 = fake.groups[0]._dev
+    g0["stateTemp"] = torch.zeros_like(g0["stateRef"])
+    read_state_from_reference(fake, elements)
+    assert torch.equal(g0["stateRef"], g0["stateTemp"])
+    back = GPUAssembler.group_state(fake, 0, "ref")
+    assert np.array_equal(back, np.stack([el._stateVarsRef for el in elements]))
+    assert bool((g0["stateRef"][0] == 7.0).all())
