@@ -129,7 +129,7 @@ def read_state_from_reference(asm, elements):
         d["stateTemp"].copy_(soa)
 
 
-def make_nist_gpu(NIST, precision="fp64", writeBackState=True):
+def make_nist_gpu(NIST, precision="fp64", writeBackState=True, assemblerClass=None):
     """A NIST subclass whose element loop and CSR assembly run on the GPU.
 
     The reference's solveIncrement keeps its host DOF vectors: computeElements copies U_np and dU to
@@ -139,10 +139,20 @@ def make_nist_gpu(NIST, precision="fp64", writeBackState=True):
     the device state and, with writeBackState, copies it into the reference element objects
     (write_back_state) before the field outputs and output managers of that increment read them;
     each later step then starts from the element objects' state (read_state_from_reference), as
-    the reference's own elements would."""
+    the reference's own elements would.  A material point's cutback request reaches the reference's
+    solveStep as the CutbackRequest class that NIST's module catches
+    (`solvers/nonlinearimplicitstatic.py:48-50, 247`), with the same message and cutback size.
+    assemblerClass: the assembler built from the extracted arrays (default GPUAssembler; the CPU
+    tests substitute one with the same interface to run the subclass's control flow)."""
+    import sys
+
     import torch
 
     from .assembly import GPUAssembler
+    from .exceptions import CutbackRequest
+
+    Assembler = assemblerClass or GPUAssembler
+    RefCutbackRequest = getattr(sys.modules.get(NIST.__module__), "CutbackRequest", None)
 
     class NISTGPU(NIST):
         identification = "NISTGPU"
@@ -150,7 +160,7 @@ def make_nist_gpu(NIST, precision="fp64", writeBackState=True):
         def _gpu(self, elements):
             if getattr(self, "_gpuAssembler", None) is None or self._gpuDofManager is not self.theDofManager:
                 coords, nodeDof, nDof, groups = arrays_from_reference(elements.values(), self.theDofManager)
-                self._gpuAssembler = GPUAssembler(coords, nodeDof, nDof, groups, precision=precision)
+                self._gpuAssembler = Assembler(coords, nodeDof, nDof, groups, precision=precision)
                 self._gpuDofManager = self.theDofManager
                 self._gpuElements = list(elements.values())
             return self._gpuAssembler
@@ -159,8 +169,13 @@ def make_nist_gpu(NIST, precision="fp64", writeBackState=True):
             asm = self._gpu(elements)
             Pd, Fd = asm.constructDofVector(), asm.constructDofVector()
             self._gpuK = asm.constructSystemMatrix()
-            asm.computeElements(elements, torch.as_tensor(np.asarray(U_np)), torch.as_tensor(np.asarray(dU)), Pd,
-                                self._gpuK, Fd, timeStep)  # fmt: skip
+            try:
+                asm.computeElements(elements, torch.as_tensor(np.asarray(U_np)), torch.as_tensor(np.asarray(dU)), Pd,
+                                    self._gpuK, Fd, timeStep)  # fmt: skip
+            except CutbackRequest as e:
+                if RefCutbackRequest is None:
+                    raise
+                raise RefCutbackRequest(str(e), e.cutbackSize) from e
             P += Pd.cpu().numpy()
             F += Fd.cpu().numpy()
             return P, K, F

@@ -1,0 +1,240 @@
+"""The NIST subclass of the integration layer (make_nist_gpu) inside complete reference simulations,
+on the CPU.
+
+The reference's finiteElementSimulation runs an input file with ``*solver, solver=NISTGPU``, the
+subclass registered as a maintainer would (a solver module plus a solverLibrary entry; both in
+memory here, nothing is written to the reference tree), with the oracle behind GPUAssembler's
+interface as its assembler (test infrastructure: this exercises the subclass's control flow --
+array extraction, element pass hand-off, CSR hand-off, acceptance, state write-back and read-back,
+cutback translation -- not the CUDA kernels, which the GPU tests cover).  The run must reproduce the
+reference's own NIST run of the same input: final displacements, every increment's Newton
+iterations, and the history of an element field output that reads the written-back state.
+Needs the reference source tree; skipped when it is not present.
+"""
+
+import os
+import sys
+import types
+from types import SimpleNamespace
+
+import numpy as np
+import pytest
+
+REF = os.environ.get("EDELWEISSFE_ROOT", "/root/reference")
+pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "edelweissfe")), reason="reference not present")
+torch = pytest.importorskip("torch")
+
+J2_CUBE = """
+*material, name=vonmises, id=vonmises, provider=edelweiss
+210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0
+*job, name=j2job, domain=3d
+*solver, solver={solver}, name=theSolver
+*modelGenerator, generator=boxGen, name=gen
+nX=3
+nY=3
+nZ=2
+lX=1
+lY=1
+lZ=1
+elProvider=edelweiss
+elType=C3D8
+*section, name=section1, material=vonmises, type=solid
+all
+*fieldOutput
+create=perElement, name=stress, elSet=gen_all, result=stress, quadraturePoint=0:8
+*step, solver=theSolver, maxInc=0.25, minInc=1e-6, maxNumInc=1000, maxIter=25, stepLength=1
+options, category=NISTSolver, extrapolation=linear, linsolver=superlu
+dirichlet, name=bot, nSet=gen_bottom, field=displacement, 2=0.0
+dirichlet, name=left, nSet=gen_left, field=displacement, 1=0.0
+dirichlet, name=back, nSet=gen_back, field=displacement, 3=0.0
+dirichlet, name=top, nSet=gen_top, field=displacement, 2=0.006
+"""
+
+NH_BLOCK = """
+*material, name=neohookewa, id=nh, provider=edelweiss
+384.6153846, 833.3333333
+*job, name=nhjob, domain=3d
+*solver, solver={solver}, name=theSolver
+*modelGenerator, generator=boxGen, name=gen
+nX=2
+nY=3
+nZ=2
+lX=1
+lY=1
+lZ=1
+elProvider=edelweiss
+elType=C3D8TL
+*section, name=section1, material=nh, type=solid
+all
+*fieldOutput
+create=perElement, name=stress, elSet=gen_all, result=stress, quadraturePoint=0:8
+*step, solver=theSolver, maxInc=0.34, minInc=1e-6, maxNumInc=1000, maxIter=25, stepLength=1
+options, category=NISTSolver, extrapolation=off, linsolver=superlu
+dirichlet, name=bot, nSet=gen_bottom, field=displacement, 1=0.0, 2=0.0, 3=0.0
+dirichlet, name=top, nSet=gen_top, field=displacement, 2=-0.08
+"""
+
+
+class OracleAssembler:
+    """GPUAssembler's interface over the oracle: device-layout state tensors ([field][element * nInt
+    + qp]) in `groups[i]._dev`, torch DOF vectors and CSR data, the reference's CSR pattern."""
+
+    def __init__(self, coords, nodeDof, nDof, groups, precision="fp64"):
+        from oracle.assembly import Model
+        from oracle import library
+
+        self.nDof = int(nDof)
+        recs, off = [], 0
+        self.groups = []
+        for g in groups:
+            n = len(g.conn)
+            recs.append(dict(elType=g.elType, kind=g.material, props=g.props, conn=g.conn, thickness=g.thickness,
+                             order=np.arange(off, off + n)))  # fmt: skip
+            nInt = library.get(g.elType)["nInt"]
+            self.groups.append(SimpleNamespace(conn=g.conn, _dev={"offset": off, "type": SimpleNamespace(nInt=nInt)}))
+            off += n
+        self.model = Model(coords, nodeDof, nDof, recs)
+        init = self.model.initial_state()
+        self._eold = [st.get("Eold") for st in init]
+        self._enew = list(self._eold)
+        for g, st in zip(self.groups, init):
+            E, nInt, S = st["state"].shape
+            g._dev["stateRef"] = torch.zeros((S, E * nInt), dtype=torch.float64)
+            g._dev["stateTemp"] = torch.zeros((S, E * nInt), dtype=torch.float64)
+
+    def constructDofVector(self):
+        return torch.zeros(self.nDof, dtype=torch.float64)
+
+    def constructSystemMatrix(self):
+        return torch.zeros(len(self.model.indices), dtype=torch.float64)
+
+    def group_state(self, i, which="temp"):
+        from edelweissfe_gb300.assembly import GPUAssembler
+
+        return GPUAssembler.group_state(self, i, which)
+
+    def computeElements(self, elements, U_np, dU, P, K, F, timeStep=None):
+        from edelweissfe_gb300.exceptions import CutbackRequest
+        from oracle.exceptions import CutbackRequest as OracleCutback
+
+        ref = []
+        for i, g in enumerate(self.groups):
+            d = dict(state=self.group_state(i, "ref").copy())
+            if self._eold[i] is not None:
+                d["Eold"] = self._eold[i]
+            ref.append(d)
+        try:
+            r = self.model.compute_elements_or_raise(U_np.numpy(), dU.numpy(), ref)
+        except OracleCutback as e:  # what the device status word turns into on the GPU path
+            raise CutbackRequest(str(e), e.cutbackSize) from e
+        P += torch.from_numpy(r["P"])
+        F += torch.from_numpy(r["F"])
+        K += torch.from_numpy(r["Kdata"])
+        for i, (g, st) in enumerate(zip(self.groups, r["stateTemp"])):
+            E, nInt, S = st["state"].shape
+            g._dev["stateTemp"].copy_(torch.from_numpy(st["state"].reshape(E * nInt, S).T.copy()))
+            self._enew[i] = st.get("Enew")
+        return P, K, F
+
+    def assembleStiffnessCSR(self, K, host=True):
+        import scipy.sparse as sp
+
+        return sp.csr_matrix((K.numpy().copy(), self.model.indices.copy(), self.model.indptr.copy()),
+                             shape=(self.nDof, self.nDof))  # fmt: skip
+
+    def acceptLastState(self):
+        for i, g in enumerate(self.groups):
+            g._dev["stateRef"].copy_(g._dev["stateTemp"])
+            if self._enew[i] is not None:
+                self._eold[i] = self._enew[i]
+
+
+@pytest.fixture(scope="module")
+def ref():
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    import make_golden
+
+    make_golden.setup_reference(REF)
+    return make_golden
+
+
+def _simulate(inp, tmp_path):
+    import edelweissfe.solvers.nonlinearimplicitstatic as nis
+    from edelweissfe.drivers.inputfiledrivensimulation import finiteElementSimulation
+    from edelweissfe.utils.inputfileparser import parseInputFile
+
+    its = []
+    orig = nis.NIST.solveIncrement
+
+    def counted(self, *a, **k):  # the Newton iterations of every accepted increment
+        out = orig(self, *a, **k)
+        its.append(out[3])
+        return out
+
+    nis.NIST.solveIncrement = counted
+    path = os.path.join(tmp_path, "job.inp")
+    with open(path, "w") as f:
+        f.write(inp)
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        model, foc = finiteElementSimulation(parseInputFile(path), verbose=False, suppressPlots=True)
+    finally:
+        os.chdir(cwd)
+        nis.NIST.solveIncrement = orig
+    U = np.hstack([f["U"].flatten() for f in model.nodeFields.values()])
+    return U, its, np.asarray(foc.fieldOutputs["stress"].getResultHistory())
+
+
+@pytest.mark.parametrize("inp", [J2_CUBE, NH_BLOCK], ids=["c3d8-vonmises", "c3d8tl-neohooke"])
+def test_subclass_reproduces_the_reference_simulation(ref, inp, tmp_path):
+    import edelweissfe.config.solvers as solvers
+    from edelweissfe.solvers.nonlinearimplicitstatic import NIST
+
+    from edelweissfe_gb300.integration import make_nist_gpu
+
+    U0, its0, S0 = _simulate(inp.format(solver="NIST"), tmp_path)
+    module = types.ModuleType("edelweissfe.solvers.nonlinearimplicitstaticgpu")
+    module.NISTGPU = make_nist_gpu(NIST, precision="fp64", assemblerClass=OracleAssembler)
+    sys.modules[module.__name__] = module
+    solvers.solverLibrary["NISTGPU"] = "nonlinearimplicitstaticgpu"
+    try:
+        U1, its1, S1 = _simulate(inp.format(solver="NISTGPU"), tmp_path)
+    finally:
+        solvers.solverLibrary.pop("NISTGPU", None)
+        sys.modules.pop(module.__name__, None)
+    assert its1 == its0 and len(its0) >= 3
+    assert np.abs(U1 - U0).max() <= 1e-10 * np.abs(U0).max()
+    assert S1.shape == S0.shape and np.abs(S0).max() > 0
+    assert np.abs(S1 - S0).max() <= 1e-9 * np.abs(S0).max()  # field output through the written-back state
+
+
+def test_cutback_reaches_the_reference_as_its_own_exception(ref):
+    """A material point's cutback on the GPU path (this package's CutbackRequest) is raised into the
+    reference's solveStep as the CutbackRequest class NIST's module catches."""
+    import edelweissfe.utils.exceptions as refexc
+    from edelweissfe.solvers.nonlinearimplicitstatic import NIST
+
+    from edelweissfe_gb300.exceptions import CutbackRequest
+    from edelweissfe_gb300.integration import make_nist_gpu
+
+    class Failing:
+        def __init__(self, *a, **k):
+            pass
+
+        def constructDofVector(self):
+            return torch.zeros(3, dtype=torch.float64)
+
+        def constructSystemMatrix(self):
+            return torch.zeros(1, dtype=torch.float64)
+
+        def computeElements(self, *a, **k):
+            raise CutbackRequest("material point failed in element 0", 0.5)
+
+    cls = make_nist_gpu(NIST, assemblerClass=Failing)
+    solver = cls.__new__(cls)
+    solver._gpuAssembler, solver.theDofManager = Failing(), None
+    solver._gpuDofManager, solver._gpuElements = None, []
+    with pytest.raises(refexc.CutbackRequest) as e:
+        solver.computeElements({}, np.zeros(3), np.zeros(3), np.zeros(3), None, np.zeros(3), None)
+    assert e.value.cutbackSize == 0.5 and "element 0" in str(e.value)
