@@ -129,13 +129,27 @@ def read_state_from_reference(asm, elements):
         d["stateTemp"].copy_(soa)
 
 
+def same_layout(asm, nodeDof, nDof, groups):
+    """True when an assembler was built for the same DOF map, elements, materials and properties as
+    freshly extracted arrays (NIST builds a new DofManager every step, nonlinearimplicitstatic.py:134,
+    usually for the same numbering)."""
+    if asm.nDof != nDof or not np.array_equal(asm.nodeDof_host, nodeDof) or len(asm.groups) != len(groups):
+        return False
+    return all(a.elType == b.elType and a.material == b.material and np.array_equal(a.conn, b.conn)
+               and np.array_equal(np.asarray(a.props), np.asarray(b.props))
+               and np.array_equal(np.asarray(a.thickness), np.asarray(b.thickness))
+               for a, b in zip(asm.groups, groups))  # fmt: skip
+
+
 def make_nist_gpu(NIST, precision="fp64", writeBackState=True, assemblerClass=None):
     """A NIST subclass whose element loop and CSR assembly run on the GPU.
 
     The reference's solveIncrement keeps its host DOF vectors: computeElements copies U_np and dU to
     the device, runs the element pass, and adds P and |P_e| back into the host vectors; the
     tangent stays on the device until assembleStiffnessCSR returns it as the scipy CSR matrix the
-    linear solvers expect.  Accepting a converged increment (FEModel.advanceToTime) also accepts
+    linear solvers expect.  The assembler (pattern, geometry, device state) is kept across steps
+    while the extracted mesh, DOF map and materials stay the same (NIST builds a new DofManager
+    every step).  Accepting a converged increment (FEModel.advanceToTime) also accepts
     the device state and, with writeBackState, copies it into the reference element objects
     (write_back_state) before the field outputs and output managers of that increment read them;
     each later step then starts from the element objects' state (read_state_from_reference), as
@@ -158,9 +172,16 @@ def make_nist_gpu(NIST, precision="fp64", writeBackState=True, assemblerClass=No
         identification = "NISTGPU"
 
         def _gpu(self, elements):
-            if getattr(self, "_gpuAssembler", None) is None or self._gpuDofManager is not self.theDofManager:
+            old = getattr(self, "_gpuAssembler", None)
+            if old is None or self._gpuDofManager is not self.theDofManager:
                 coords, nodeDof, nDof, groups = arrays_from_reference(elements.values(), self.theDofManager)
-                self._gpuAssembler = Assembler(coords, nodeDof, nDof, groups, precision=precision)
+                if old is None or not same_layout(old, nodeDof, nDof, groups):
+                    if old is not None and not writeBackState:
+                        raise NotImplementedError("the model changed between steps; carrying the GPU state over "
+                                                  "needs writeBackState=True")  # fmt: skip
+                    self._gpuAssembler = Assembler(coords, nodeDof, nDof, groups, precision=precision)
+                    if old is not None:  # the element objects hold the accepted state (write-back)
+                        read_state_from_reference(self._gpuAssembler, elements.values())
                 self._gpuDofManager = self.theDofManager
                 self._gpuElements = list(elements.values())
             return self._gpuAssembler

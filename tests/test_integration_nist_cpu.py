@@ -5,8 +5,8 @@ The reference's finiteElementSimulation runs an input file with ``*solver, solve
 subclass registered as a maintainer would (a solver module plus a solverLibrary entry; both in
 memory here, nothing is written to the reference tree), with the oracle behind GPUAssembler's
 interface as its assembler (test infrastructure: this exercises the subclass's control flow --
-array extraction, element pass hand-off, CSR hand-off, acceptance, state write-back and read-back,
-cutback translation -- not the CUDA kernels, which the GPU tests cover).  The run must reproduce the
+array extraction, element pass hand-off, CSR hand-off, acceptance, state write-back and, in the
+second step of the von Mises case, read-back, cutback translation -- not the CUDA kernels, which the GPU tests cover).  The run must reproduce the
 reference's own NIST run of the same input: final displacements, every increment's Newton
 iterations, and the history of an element field output that reads the written-back state.
 Needs the reference source tree; skipped when it is not present.
@@ -48,6 +48,9 @@ dirichlet, name=bot, nSet=gen_bottom, field=displacement, 2=0.0
 dirichlet, name=left, nSet=gen_left, field=displacement, 1=0.0
 dirichlet, name=back, nSet=gen_back, field=displacement, 3=0.0
 dirichlet, name=top, nSet=gen_top, field=displacement, 2=0.006
+*step, solver=theSolver, maxInc=0.5, minInc=1e-6, maxNumInc=1000, maxIter=25, stepLength=1
+options, category=NISTSolver, extrapolation=linear, linsolver=superlu
+dirichlet, name=top, nSet=gen_top, field=displacement, 2=0.009
 """
 
 NH_BLOCK = """
@@ -84,6 +87,7 @@ class OracleAssembler:
         from oracle import library
 
         self.nDof = int(nDof)
+        self.nodeDof_host = np.asarray(nodeDof)
         recs, off = [], 0
         self.groups = []
         for g in groups:
@@ -91,7 +95,9 @@ class OracleAssembler:
             recs.append(dict(elType=g.elType, kind=g.material, props=g.props, conn=g.conn, thickness=g.thickness,
                              order=np.arange(off, off + n)))  # fmt: skip
             nInt = library.get(g.elType)["nInt"]
-            self.groups.append(SimpleNamespace(conn=g.conn, _dev={"offset": off, "type": SimpleNamespace(nInt=nInt)}))
+            self.groups.append(SimpleNamespace(elType=g.elType, material=g.material, props=g.props, conn=g.conn,
+                                               thickness=g.thickness,
+                                               _dev={"offset": off, "type": SimpleNamespace(nInt=nInt)}))  # fmt: skip
             off += n
         self.model = Model(coords, nodeDof, nDof, recs)
         init = self.model.initial_state()
@@ -238,3 +244,35 @@ def test_cutback_reaches_the_reference_as_its_own_exception(ref):
     with pytest.raises(refexc.CutbackRequest) as e:
         solver.computeElements({}, np.zeros(3), np.zeros(3), np.zeros(3), None, np.zeros(3), None)
     assert e.value.cutbackSize == 0.5 and "element 0" in str(e.value)
+
+
+def test_assembler_is_kept_across_steps_and_rebuilt_with_the_state_on_changes(ref):
+    """NIST builds a new DofManager every step: the same numbering keeps the assembler (and its device
+    state); a changed model (here a material property) builds a new one that starts from the state
+    the element objects hold."""
+    from edelweissfe.numerics.dofmanager import DofManager
+    from edelweissfe.solvers.nonlinearimplicitstatic import NIST
+    from test_integration_cpu import _prepared
+
+    from edelweissfe_gb300.integration import make_nist_gpu
+
+    model, dm = _prepared(ref, 3, "boxGen", ["nX=2", "nY=1", "nZ=1"], "C3D8", "vonmises",
+                          [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0], 0.0, [0.5, 1.0, 1.0], 1, [0] * 3, [1] * 3)  # fmt: skip
+
+    def new_dof_manager():
+        return DofManager(model.nodeFields.values(), [], model.elements.values(), [], model.nodeSets.values())
+
+    cls = make_nist_gpu(NIST, assemblerClass=OracleAssembler)
+    solver = cls.__new__(cls)
+    solver.theDofManager = dm
+    first = solver._gpu(model.elements)
+    solver.theDofManager = new_dof_manager()
+    assert solver._gpu(model.elements) is first
+    elements = list(model.elements.values())
+    for k, el in enumerate(elements):
+        el._stateVarsRef[:, 0] = 3.0 + k
+    elements[0].material._E = 200000.0  # the section's shared material object
+    solver.theDofManager = new_dof_manager()
+    second = solver._gpu(model.elements)
+    assert second is not first and second.groups[0].props[0][0] == 200000.0
+    assert np.array_equal(second.group_state(0, "ref"), np.stack([el._stateVarsRef for el in elements]))
