@@ -8,7 +8,8 @@ interface as its assembler (test infrastructure: this exercises the subclass's c
 array extraction, element pass hand-off, CSR hand-off, acceptance, state write-back and, in the
 second step of the von Mises case, read-back, cutback translation -- not the CUDA kernels, which the GPU tests cover).  The run must reproduce the
 reference's own NIST run of the same input: final displacements, every increment's Newton
-iterations, and the history of an element field output that reads the written-back state.
+iterations, and the field outputs that read the written-back state -- on inputs written here and
+on all 17 edelweiss-provider test inputs of the reference (`testfiles/`).
 Needs the reference source tree; skipped when it is not present.
 """
 
@@ -21,7 +22,10 @@ import numpy as np
 import pytest
 
 REF = os.environ.get("EDELWEISSFE_ROOT", "/root/reference")
-pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "edelweissfe")), reason="reference not present")
+pytestmark = [
+    pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "edelweissfe")), reason="reference not present"),
+    pytest.mark.filterwarnings("ignore::PendingDeprecationWarning"),  # numpy.matrix inside the reference
+]
 torch = pytest.importorskip("torch")
 
 J2_CUBE = """
@@ -276,3 +280,92 @@ def test_assembler_is_kept_across_steps_and_rebuilt_with_the_state_on_changes(re
     second = solver._gpu(model.elements)
     assert second is not first and second.groups[0].props[0][0] == 200000.0
     assert np.array_equal(second.group_state(0, "ref"), np.stack([el._stateVarsRef for el in elements]))
+
+
+REFERENCE_CASES = [
+    "CantileverBeamQuad4", "CantileverBeamQuad8", "CantileverBeamHexa8", "CantileverBeamVonMisesPE",
+    "CantileverBeamQuad8NeoHookeWa", "CantileverBeamQuad8NeoHookeWb", "CantileverBeamQuad8NeoHookeWc",
+    "FixedDisplacementQuad4", "FixedDisplacementQuad8", "SimpleBeamHexa8", "SimpleBeamQuad4", "SimpleBeamQuad8",
+    "TensionBarHexa8", "TensionBarQuad4", "TensionBarQuad8", "WallShearHexa8", "WallShearHexa20",
+]  # fmt: skip
+
+
+@pytest.fixture(scope="module")
+def superlu_for_pardiso():
+    """The reference's default linear solver is PARDISO (not installed): SciPy's SuperLU in its place,
+    in memory, for both runs of a comparison."""
+    import scipy.sparse.linalg as sla
+
+    name = "edelweissfe.linsolve.pardiso.pardiso"
+    saved = sys.modules.get(name)
+    stub = types.ModuleType(name)
+    stub.pardisoSolve = lambda A, b: sla.spsolve(A, b, use_umfpack=False)
+    sys.modules[name] = stub
+    yield
+    if saved is None:
+        sys.modules.pop(name, None)
+    else:
+        sys.modules[name] = saved
+
+
+def _run_case(case, solver, tmp_path):
+    import shutil
+
+    import edelweissfe.solvers.nonlinearimplicitstatic as nis
+    from edelweissfe.drivers.inputfiledrivensimulation import finiteElementSimulation
+    from edelweissfe.utils.inputfileparser import parseInputFile
+
+    wd = os.path.join(tmp_path, f"{case}_{solver}")
+    shutil.copytree(os.path.join(REF, "testfiles", case), wd)
+    path = os.path.join(wd, "test.inp")
+    with open(path) as f:
+        text = f.read()
+    with open(path, "w") as f:
+        f.write(text.replace("solver=NIST,", f"solver={solver},"))
+    its = []
+    orig = nis.NIST.solveIncrement
+
+    def counted(self, *a, **k):
+        out = orig(self, *a, **k)
+        its.append(out[3])
+        return out
+
+    nis.NIST.solveIncrement = counted
+    cwd = os.getcwd()
+    os.chdir(wd)
+    try:
+        model, foc = finiteElementSimulation(parseInputFile(path), verbose=False, suppressPlots=True)
+    finally:
+        os.chdir(cwd)
+        nis.NIST.solveIncrement = orig
+    U = np.hstack([f["U"].flatten() for f in model.nodeFields.values()])
+    results = {name: np.asarray(fo.getLastResult(), float) for name, fo in foc.fieldOutputs.items()}
+    return U, its, results
+
+
+@pytest.mark.parametrize("case", REFERENCE_CASES)
+def test_subclass_runs_the_reference_test_inputs(ref, superlu_for_pardiso, case, tmp_path):
+    """The reference's own edelweiss-provider test inputs (testfiles/<case>/test.inp) with the
+    solver switched to the GPU subclass: same displacements, Newton iterations and field outputs
+    (per-element and per-node, through the written-back state) as with NIST."""
+    import edelweissfe.config.solvers as solvers
+    from edelweissfe.solvers.nonlinearimplicitstatic import NIST
+
+    from edelweissfe_gb300.integration import make_nist_gpu
+
+    U0, its0, R0 = _run_case(case, "NIST", tmp_path)
+    module = types.ModuleType("edelweissfe.solvers.nonlinearimplicitstaticgpu")
+    module.NISTGPU = make_nist_gpu(NIST, precision="fp64", assemblerClass=OracleAssembler)
+    sys.modules[module.__name__] = module
+    solvers.solverLibrary["NISTGPU"] = "nonlinearimplicitstaticgpu"
+    try:
+        U1, its1, R1 = _run_case(case, "NISTGPU", tmp_path)
+    finally:
+        solvers.solverLibrary.pop("NISTGPU", None)
+        sys.modules.pop(module.__name__, None)
+    assert its1 == its0
+    assert np.abs(U1 - U0).max() <= 1e-9 * np.abs(U0).max()
+    assert R1.keys() == R0.keys()
+    for name in R0:
+        scale = max(np.abs(R0[name]).max(), 1e-300)
+        assert np.abs(R1[name] - R0[name]).max() <= 1e-8 * scale, name
