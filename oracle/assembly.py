@@ -145,6 +145,25 @@ class Model:
         Kdata = update_csr(self.x, V, len(self.indices))
         return dict(P=P, F=F, Kdata=Kdata, V=V, stateTemp=stateTemp, fail=fails, first_failed_element=first)
 
+    def body_force(self, load, elements=None):
+        """External load vector of a body force `load` on the given global element indices (all by
+        default): NIST.computeBodyForces (`solvers/nonlinearimplicitstatic.py:520-557`) scattering
+        each element's computeBodyForce (`elem.body_force`) into the DOF vector."""
+        P = np.zeros(self.nDof)
+        wanted = None if elements is None else set(int(e) for e in elements)
+        for g in self.groups:
+            order = np.asarray(g["order"])
+            pick = np.arange(len(order)) if wanted is None else np.array(
+                [k for k, e in enumerate(order) if int(e) in wanted], np.int64)  # fmt: skip
+            if len(pick) == 0:
+                continue
+            X = self.coords[np.asarray(g["conn"])[pick]]
+            th = np.broadcast_to(np.asarray(g["thickness"], float), (len(order),))[pick]
+            Pe = elem.body_force(g["elType"], X, load, th)
+            for j, e in enumerate(order[pick]):
+                P[self.dofs[e]] += Pe[j]
+        return P
+
     def compute_elements_or_raise(self, U_np, dU, stateRef, time=None, dT=1.0):
         r = self.compute_elements(U_np, dU, stateRef, time, dT)
         if r["first_failed_element"] is not None:

@@ -34,6 +34,27 @@ def _geometry(lib, X):
     return J, detJ, G
 
 
+def body_force(elType, X, load, thickness):
+    """P_e [E, nDof] of a body force `load` [dim] for a batch of elements of one type
+    (computeBodyForce, `displacementelement/element.py:348-371`, identical in
+    `displacementtlelement/element.py:429-452`): at every quadrature point, in the reference's
+    order, P_e += outer(N_i, load).flatten() * det J_i * t * w_i, with N at the library point
+    (computeNOperator, `_elementcomputationmatrices.py:106-212`) and J as computeJacobian forms it
+    (including the Hexa20 fit)."""
+    lib = library.get(elType)
+    dim = lib["nSpatialDimensions"]
+    X = np.asarray(X, float)
+    E = X.shape[0]
+    N = shapes.shape_table(lib)  # [q, nN]
+    _, detJ, _ = _geometry(lib, X)
+    t = np.ones(E) if dim == 3 else np.asarray(thickness, float)
+    load = np.asarray(load, float)[:dim]
+    P = np.zeros((E, lib["nNodes"] * dim))
+    for i in range(lib["nInt"]):
+        P += ((np.outer(N[i], load).reshape(-1)[None, :] * detJ[:, i][:, None]) * t[:, None]) * lib["w"][i]
+    return P
+
+
 def small_strain_B(G, dim):
     """Small-strain B operator [E, nV, nDof] for one quadrature point (e.g. _B3D8, :679-817).
 

@@ -169,3 +169,44 @@ def test_write_back_reproduces_the_reference_state(ref, dim, gen, lines, et, kin
     back = GPUAssembler.group_state(fake, 0, "ref")
     assert np.array_equal(back, np.stack([el._stateVarsRef for el in elements]))
     assert bool((g0["stateRef"][0] == 7.0).all())
+
+
+@pytest.mark.parametrize(
+    "dim,gen,lines,et",
+    [
+        (2, "planeRectQuad", ["nX=3", "nY=2"], "CPE4"),
+        (2, "planeRectQuad", ["nX=3", "nY=2"], "CPS8R"),
+        (3, "boxGen", ["nX=2", "nY=2", "nZ=1"], "C3D8"),
+        (3, "boxGen", ["nX=2", "nY=1", "nZ=1"], "C3D20"),
+        (3, "boxGen", ["nX=2", "nY=1", "nZ=1"], "C3D20TL"),
+    ],
+)
+def test_oracle_body_force_matches_reference(ref, dim, gen, lines, et):
+    """oracle.elements.body_force / Model.body_force against the reference's computeBodyForce of
+    every element of a jittered mesh (computeNOperator at the library points, J as the reference
+    forms it -- the Hexa20 fit included -- section thickness in 2D), scattered as
+    NIST.computeBodyForces does."""
+    from edelweissfe_gb300.integration import arrays_from_reference
+    from oracle.assembly import Model
+
+    kind, props = ("linearelastic", [210000.0, 0.3]) if not et.endswith("TL") else ("neohookewa", [1000.0, 10000.0])
+    model, dm = _prepared(ref, dim, gen, lines, et, kind, props, 0.15, [1.0 / 3] * dim, 7, [0] * dim, [1] * dim)
+    elements = list(model.elements.values())
+    load = np.array([1.5, -2.0, 0.7][:dim])
+    want = dm.constructDofVector()
+    for el in elements:
+        Pe = np.zeros(el.nDof)
+        el.computeBodyForce(Pe, None, load, None, np.array([0.0, 0.0]), 1.0)
+        want[dm.idcsOfElementsInDofVector[el]] += Pe
+    coords, nodeDof, nDof, groups = arrays_from_reference(elements, dm)
+    om = Model(coords, nodeDof, nDof, [dict(elType=g.elType, kind=g.material, props=g.props, conn=g.conn,
+                                            thickness=g.thickness, order=np.arange(len(g.conn))) for g in groups])  # fmt: skip
+    got = om.body_force(load)
+    assert np.abs(got - np.asarray(want)).max() <= 1e-14 * np.abs(np.asarray(want)).max()
+    half = om.body_force(load, elements=range(0, len(elements), 2))  # a subset, as an element set
+    want_half = dm.constructDofVector()
+    for el in elements[0::2]:
+        Pe = np.zeros(el.nDof)
+        el.computeBodyForce(Pe, None, load, None, np.array([0.0, 0.0]), 1.0)
+        want_half[dm.idcsOfElementsInDofVector[el]] += Pe
+    assert np.abs(half - np.asarray(want_half)).max() <= 1e-14 * np.abs(np.asarray(want)).max()
