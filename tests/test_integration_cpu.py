@@ -210,3 +210,50 @@ def test_oracle_body_force_matches_reference(ref, dim, gen, lines, et):
         el.computeBodyForce(Pe, None, load, None, np.array([0.0, 0.0]), 1.0)
         want_half[dm.idcsOfElementsInDofVector[el]] += Pe
     assert np.abs(half - np.asarray(want_half)).max() <= 1e-14 * np.abs(np.asarray(want)).max()
+
+
+def test_result_collector_matches_the_reference_collector(ref):
+    """results.ElementResultCollector over a state in the device layout against the reference's own
+    ElementResultCollector (utils/elementresultcollector.pyx) over element objects holding the same
+    state: stress and strain tables for a scattered element list and all points, and the material
+    state against the element arrays."""
+    from types import SimpleNamespace
+
+    import torch
+
+    from edelweissfe.config.timing import createTimingDict
+    from edelweissfe.solvers.nonlinearimplicitstatic import NIST
+    from edelweissfe.timesteppers.timestep import TimeStep
+
+    from edelweissfe_gb300.integration import arrays_from_reference
+    from edelweissfe_gb300.results import ElementResultCollector
+
+    try:
+        from edelweissfe.utils.elementresultcollector import ElementResultCollector as RefCollector
+    except ImportError:
+        pytest.skip("the reference's compiled collector is not importable")
+    model, dm = _prepared(ref, 3, "boxGen", ["nX=3", "nY=2", "nZ=2"], "C3D8", "vonmises",
+                          [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0], 0.1, [1 / 3, 0.5, 0.5], 4, [0] * 3, [1] * 3)  # fmt: skip
+    elements = list(model.elements.values())
+    rng = np.random.default_rng(3)
+    U = dm.constructDofVector()
+    U[:] = rng.uniform(-1, 1, dm.nDof) * 6e-3
+    P, F, K = dm.constructDofVector(), dm.constructDofVector(), dm.constructVIJSystemMatrix()
+    s = type("S", (), {"computationTimes": createTimingDict()})()
+    NIST.computeElements(s, model.elements, U, U, P, K, F, TimeStep(1, 1.0, 1.0, 1.0, 1.0, 1.0))
+    for el in elements:
+        el.acceptLastState()
+    _, _, _, groups = arrays_from_reference(elements, dm)
+    g = groups[0]
+    nInt = elements[0]._nInt
+    host = np.stack([el._stateVarsRef for el in elements])  # [E, nInt, S]
+    soa = torch.from_numpy(np.ascontiguousarray(host.reshape(len(elements) * nInt, -1).T))
+    g._dev.update(offset=0, type=SimpleNamespace(nInt=nInt), stateRef=soa, stateTemp=soa.clone())
+    fake = SimpleNamespace(groups=[g], device=torch.device("cpu"))
+    pick = rng.permutation(len(elements))[:7]
+    for result in ("stress", "strain"):
+        ours = ElementResultCollector(fake, pick, range(nInt), result).getCurrentResults()
+        theirs = np.asarray(RefCollector([elements[i] for i in pick], range(nInt), result).getCurrentResults())
+        assert ours.shape == theirs.shape and np.array_equal(ours, theirs)
+    kappa = ElementResultCollector(fake, pick, range(nInt), "kappa").getCurrentResults()
+    assert np.array_equal(kappa[..., 0], host[pick][:, :, 12]) and kappa.max() > 0
