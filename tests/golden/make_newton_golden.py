@@ -75,6 +75,33 @@ dirichlet, name=bot, nSet=gen_bottom, field=displacement, 1=0.0, 2=0.0, 3=0.0
 dirichlet, name=top, nSet=gen_top, field=displacement, 2=-0.05
 """
 
+# a 2x2x2 von Mises cube pulled to 10 % in one increment: a material point of the reference asks for
+# a cutback (CutbackRequest) and the stepper retries with a smaller increment.  Recorded under
+# golden/newton_cutback/ (the standalone Newton driver's host logic on the CPU).
+J2_CUTBACK = """
+*material, name=vonmises, id=vonmises, provider=edelweiss
+210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0
+*job, name=j2job, domain=3d
+*solver, solver=NIST, name=theSolver
+*modelGenerator, generator=boxGen, name=gen
+nX=2
+nY=2
+nZ=2
+lX=1
+lY=1
+lZ=1
+elProvider=edelweiss
+elType=C3D8
+*section, name=section1, material=vonmises, type=solid
+all
+*step, solver=theSolver, maxInc=1.0, minInc=1e-6, maxNumInc=1000, maxIter=25, stepLength=1
+options, category=NISTSolver, extrapolation=linear, linsolver=superlu
+dirichlet, name=bot, nSet=gen_bottom, field=displacement, 2=0.0
+dirichlet, name=left, nSet=gen_left, field=displacement, 1=0.0
+dirichlet, name=back, nSet=gen_back, field=displacement, 3=0.0
+dirichlet, name=top, nSet=gen_top, field=displacement, 2=0.1
+"""
+
 
 def element_type_name(el):
     from edelweissfe.elements.library import elLibrary
@@ -105,7 +132,7 @@ def material_of(m):
     raise KeyError(n)
 
 
-def run(name, inp_text, wd, ref_root):
+def run(name, inp_text, wd, ref_root, subdir="newton"):
     import edelweissfe.solvers.nonlinearimplicitstatic as nis
     from edelweissfe.drivers.inputfiledrivensimulation import finiteElementSimulation
     from edelweissfe.utils.inputfileparser import parseInputFile
@@ -201,13 +228,14 @@ def run(name, inp_text, wd, ref_root):
         out[f"bodyforce{k}_values"] = rec["bodyforce_values"][k]
     if os.path.exists(os.path.join(wd, "U.ref")):
         out["U_ref"] = np.loadtxt(os.path.join(wd, "U.ref"))
-    path = os.path.join(HERE, "newton", f"{name}.npz")
+    os.makedirs(os.path.join(HERE, subdir), exist_ok=True)
+    path = os.path.join(HERE, subdir, f"{name}.npz")
     np.savez_compressed(path, **out)
     its = [int(i[6]) for i in incs]
     print(f"{name:32s} el={len(elements):5d} nDof={dm.nDof:6d} incs={len(incs):3d} iters={its}", flush=True)
 
 
-def main(ref_root):
+def main(ref_root, only=None):
     setup_reference(ref_root)
     # the default linear solver (PARDISO) is not available: SuperLU through scipy, as linsolver=superlu
     import scipy.sparse.linalg as sla
@@ -217,6 +245,8 @@ def main(ref_root):
     sys.modules[pm.__name__] = pm
     os.makedirs(os.path.join(HERE, "newton"), exist_ok=True)
     for case in CASES:
+        if only and case not in only:
+            continue
         wd = tempfile.mkdtemp()
         shutil.copytree(os.path.join(ref_root, "testfiles", case), wd, dirs_exist_ok=True)
         with open(os.path.join(wd, "test.inp")) as f:
@@ -226,12 +256,17 @@ def main(ref_root):
         from edelweissfe.utils.inputfileparser import parseInputFile  # noqa: F401
 
         run(case, inp, wd, ref_root)
-    for name, tmpl, n in (("J2Cube6", J2_CUBE, 6), ("NeoHookeCube4", NH_CUBE, 4)):
+    written = (("J2Cube6", J2_CUBE.format(n=6), "newton"), ("NeoHookeCube4", NH_CUBE.format(n=4), "newton"),
+               ("J2CutbackCube2", J2_CUTBACK, "newton_cutback"))  # fmt: skip
+    for name, text, subdir in written:
+        if only and name not in only:
+            continue
         wd = tempfile.mkdtemp()
         with open(os.path.join(wd, "test.inp"), "w") as f:
-            f.write(tmpl.format(n=n))
-        run(name, os.path.join(wd, "test.inp"), wd, ref_root)
+            f.write(text)
+        run(name, os.path.join(wd, "test.inp"), wd, ref_root, subdir)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("EDELWEISSFE_ROOT", ""))
+    # python make_newton_golden.py /path/to/EdelweissFE [case names: regenerate only those]
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("EDELWEISSFE_ROOT", ""), set(sys.argv[2:]) or None)

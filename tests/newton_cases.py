@@ -5,15 +5,16 @@ import os
 
 import numpy as np
 
-GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "newton")
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+GOLDEN = os.path.join(HERE, "newton")
 
 
-def names():
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+def names(subdir="newton"):
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, subdir, "*.npz")))
 
 
-def load(name):
-    with np.load(os.path.join(GOLDEN, name + ".npz")) as d:
+def load(name, subdir="newton"):
+    with np.load(os.path.join(HERE, subdir, name + ".npz")) as d:
         return {k: d[k] for k in d.files}
 
 

@@ -57,6 +57,32 @@ options, category=NISTSolver, extrapolation=linear, linsolver=superlu
 dirichlet, name=top, nSet=gen_top, field=displacement, 2=0.009
 """
 
+J2_CUTBACK = """
+*material, name=vonmises, id=vonmises, provider=edelweiss
+210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0
+*job, name=j2job, domain=3d
+*solver, solver={solver}, name=theSolver
+*modelGenerator, generator=boxGen, name=gen
+nX=2
+nY=2
+nZ=2
+lX=1
+lY=1
+lZ=1
+elProvider=edelweiss
+elType=C3D8
+*section, name=section1, material=vonmises, type=solid
+all
+*fieldOutput
+create=perElement, name=stress, elSet=gen_all, result=stress, quadraturePoint=0:8
+*step, solver=theSolver, maxInc=1.0, minInc=1e-6, maxNumInc=1000, maxIter=25, stepLength=1
+options, category=NISTSolver, extrapolation=linear, linsolver=superlu
+dirichlet, name=bot, nSet=gen_bottom, field=displacement, 2=0.0
+dirichlet, name=left, nSet=gen_left, field=displacement, 1=0.0
+dirichlet, name=back, nSet=gen_back, field=displacement, 3=0.0
+dirichlet, name=top, nSet=gen_top, field=displacement, 2=0.1
+"""
+
 NH_BLOCK = """
 *material, name=neohookewa, id=nh, provider=edelweiss
 384.6153846, 833.3333333
@@ -176,8 +202,12 @@ def _simulate(inp, tmp_path):
     its = []
     orig = nis.NIST.solveIncrement
 
-    def counted(self, *a, **k):  # the Newton iterations of every accepted increment
-        out = orig(self, *a, **k)
+    def counted(self, *a, **k):  # Newton iterations of accepted increments, exception names of the others
+        try:
+            out = orig(self, *a, **k)
+        except Exception as e:
+            its.append(type(e).__name__)
+            raise
         its.append(out[3])
         return out
 
@@ -196,7 +226,8 @@ def _simulate(inp, tmp_path):
     return U, its, np.asarray(foc.fieldOutputs["stress"].getResultHistory())
 
 
-@pytest.mark.parametrize("inp", [J2_CUBE, NH_BLOCK], ids=["c3d8-vonmises", "c3d8tl-neohooke"])
+@pytest.mark.parametrize("inp", [J2_CUBE, J2_CUTBACK, NH_BLOCK], ids=["c3d8-vonmises", "c3d8-vonmises-cutback",
+                                                                      "c3d8tl-neohooke"])  # fmt: skip
 def test_subclass_reproduces_the_reference_simulation(ref, inp, tmp_path):
     import edelweissfe.config.solvers as solvers
     from edelweissfe.solvers.nonlinearimplicitstatic import NIST
@@ -214,6 +245,8 @@ def test_subclass_reproduces_the_reference_simulation(ref, inp, tmp_path):
         solvers.solverLibrary.pop("NISTGPU", None)
         sys.modules.pop(module.__name__, None)
     assert its1 == its0 and len(its0) >= 3
+    if inp is J2_CUTBACK:  # a material point's cutback request, handled by the reference's solveStep
+        assert "CutbackRequest" in its0
     assert np.abs(U1 - U0).max() <= 1e-10 * np.abs(U0).max()
     assert S1.shape == S0.shape and np.abs(S0).max() > 0
     assert np.abs(S1 - S0).max() <= 1e-9 * np.abs(S0).max()  # field output through the written-back state

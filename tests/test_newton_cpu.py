@@ -1,7 +1,8 @@
 """The standalone Newton driver (solver.NISTGPU) on the CPU, against complete reference simulations.
 
 The same Newton fixtures the GPU suite replays (tests/golden/newton: 17 of the reference's own test
-inputs and two written for this purpose, recorded by running the reference) with the oracle behind
+inputs and two written for this purpose, recorded by running the reference), plus a run in which a
+material point of the reference asks for a cutback (tests/golden/newton_cutback), with the oracle behind
 GPUAssembler's interface (test infrastructure; the status word of a failed material point goes
 through the product's own GPUAssembler.check_status) and SuperLU solves: the same increments,
 Newton iterations per increment (cutbacks included) and converged displacements as the reference
@@ -81,11 +82,14 @@ class OracleDeviceAssembler:
                              shape=(self.nDof, self.nDof))  # fmt: skip
 
 
-@pytest.mark.parametrize("name", nc.names())
-def test_newton_driver_replays_the_reference_simulation(name):
+CASES = [(n, "newton") for n in nc.names()] + [(n, "newton_cutback") for n in nc.names("newton_cutback")]
+
+
+@pytest.mark.parametrize("name,subdir", CASES)
+def test_newton_driver_replays_the_reference_simulation(name, subdir):
     from edelweissfe_gb300.solver import NISTGPU
 
-    case = nc.load(name)
+    case = nc.load(name, subdir)
     asm = OracleDeviceAssembler(case["coords"], case["node_dof"], int(case["nDof"]), nc.groups(case))
     stepper, dirichlets, nodeforces, bodyforces, ctl = nc.step_inputs(case)
     solver = NISTGPU(asm, linsolver="superlu", extrapolation=str(case["extrapolation"]), maxIter=ctl["maxIter"],
