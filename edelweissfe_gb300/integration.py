@@ -91,7 +91,9 @@ def write_back_state(asm, elements):
     place: `_stateVarsRef` and the rows of `_stateVarsTemp` ([nInt][12 + m] per element,
     `elements/displacementelement/element.py:222-235`, `elements/displacementtlelement/element.py`
     likewise), whose rows hold the same [stress, strain, material state] in the element family's
-    Voigt order as the device state.  Everything that reads results from the element objects --
+    Voigt order as the device state; total-Lagrangian elements also get the accepted Green-Lagrange
+    strain (`_Eold` and `_E`, displacementtlelement/element.py:215-216, 454-461) from the device's
+    aux fields.  Everything that reads results from the element objects --
     the persistent views of `getResultArray` (element.py:386-409), the reference's
     ElementResultCollector and field outputs, the output managers -- then sees the GPU solution.
     `elements`: the reference elements in the assembler's element order."""
@@ -99,6 +101,7 @@ def write_back_state(asm, elements):
     for gi, g in enumerate(asm.groups):
         off = g._dev["offset"]
         S = asm.group_state(gi, "ref")  # [E, nInt, 12 + m]
+        Eold = _aux_tensors(g, S.shape[0], S.shape[1])
         for k in range(S.shape[0]):
             el = elements[off + k]
             if el._stateVarsRef.shape != S.shape[1:]:
@@ -106,11 +109,34 @@ def write_back_state(asm, elements):
             el._stateVarsRef[...] = S[k]
             for q in range(S.shape[1]):  # an array, or a list of rows once computeYourself ran (element.py:320)
                 el._stateVarsTemp[q][...] = S[k, q]
+            if Eold is not None and hasattr(el, "_Eold"):  # TL: E_old = E after acceptance (:454-461)
+                d = el._Eold.shape[-1]
+                el._Eold = Eold[k, :, :d, :d].copy()
+                el._E = Eold[k, :, :d, :d].copy()
+
+
+# device aux fields of total-Lagrangian groups: the accepted Green-Lagrange strain per point as
+# [E11, E22, E33, E12, E23, E13] (tensor components), [6][element * nInt + qp]
+_AUX = ((0, 0), (1, 1), (2, 2), (0, 1), (1, 2), (0, 2))
+
+
+def _aux_tensors(g, nEl, nInt):
+    """[E, nInt, 3, 3] accepted Green-Lagrange strains of a total-Lagrangian group, or None."""
+    aux = g._dev.get("auxRef")
+    if aux is None:
+        return None
+    a = aux.cpu().numpy().T.reshape(nEl, nInt, 6)
+    T = np.zeros((nEl, nInt, 3, 3))
+    for f, (i, j) in enumerate(_AUX):
+        T[:, :, i, j] = a[:, :, f]
+        T[:, :, j, i] = a[:, :, f]
+    return T
 
 
 def read_state_from_reference(asm, elements):
-    """The inverse of write_back_state: every reference element's `_stateVarsRef` into the
-    assembler's accepted state (stateRef and stateTemp, [field][element * nInt + qp]).  With the
+    """The inverse of write_back_state: every reference element's `_stateVarsRef` (and, for
+    total-Lagrangian elements, `_Eold`) into the assembler's accepted state (stateRef and stateTemp,
+    [field][element * nInt + qp]; auxRef and auxTemp).  With the
     write-back on, the element objects hold the accepted state at every step boundary, so reading
     them at a step start picks up exactly what the reference's own elements would compute from,
     including states set by step actions (`stepactions/setfield.py:95`, through the field outputs'
@@ -127,6 +153,16 @@ def read_state_from_reference(asm, elements):
         soa = torch.from_numpy(np.ascontiguousarray(host.reshape(n * nInt, -1).T)).to(d["stateRef"])
         d["stateRef"].copy_(soa)
         d["stateTemp"].copy_(soa)
+        if d.get("auxRef") is not None and hasattr(elements[off], "_Eold"):  # TL: the accepted E_old
+            a = np.zeros((n, nInt, 6))
+            for k in range(n):
+                Eo = np.asarray(elements[off + k]._Eold, float)  # [nInt, d, d]
+                for f, (i, j) in enumerate(_AUX):
+                    if i < Eo.shape[-1] and j < Eo.shape[-1]:
+                        a[k, :, f] = Eo[:, i, j]
+            aux = torch.from_numpy(np.ascontiguousarray(a.reshape(n * nInt, 6).T)).to(d["auxRef"])
+            d["auxRef"].copy_(aux)
+            d["auxTemp"].copy_(aux)
 
 
 def same_layout(asm, nodeDof, nDof, groups):

@@ -96,6 +96,7 @@ def test_distributed_loads_raise_like_the_reference():
         (3, "boxGen", ["nX=2", "nY=2", "nZ=1"], "C3D8", "vonmises", [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0]),
         (2, "planeRectQuad", ["nX=3", "nY=2"], "CPE8RTL", "neohookewa", [1000.0, 10000.0]),
         (3, "boxGen", ["nX=2", "nY=1", "nZ=1"], "C3D8TL", "neohookewb", [1000.0, 10000.0]),
+        (3, "boxGen", ["nX=2", "nY=1", "nZ=1"], "C3D8TL", "vonmises", [210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0]),
     ],
 )
 def test_write_back_reproduces_the_reference_state(ref, dim, gen, lines, et, kind, props):
@@ -128,6 +129,7 @@ def test_write_back_reproduces_the_reference_state(ref, dim, gen, lines, et, kin
     for el in elements:
         el.acceptLastState()
     want = [el._stateVarsRef.copy() for el in elements]
+    want_E = [np.array(el._Eold, copy=True) for el in elements] if et.endswith("TL") else None
     assert max(np.abs(w).max() for w in want) > 0
     views = [el.getResultArray("stress", 0) for el in elements]
     collector = None
@@ -144,13 +146,28 @@ def test_write_back_reproduces_the_reference_state(ref, dim, gen, lines, et, kin
     g = groups[0]
     om = Model(coords, nodeDof, nDof, [dict(elType=g.elType, kind=g.material, props=g.props, conn=g.conn,
                                             thickness=g.thickness, order=np.arange(len(g.conn)))])  # fmt: skip
-    st = om.compute_elements(np.asarray(U), np.asarray(U), om.initial_state())["stateTemp"][0]["state"]
+    temp = om.compute_elements(np.asarray(U), np.asarray(U), om.initial_state())["stateTemp"][0]
+    st = temp["state"]
     E, nInt, S = st.shape
     fake = SimpleNamespace(groups=[SimpleNamespace(conn=g.conn, _dev={"offset": 0, "type": SimpleNamespace(nInt=nInt),
                                                                        "stateRef": torch.from_numpy(
                                                                            st.reshape(E * nInt, S).T.copy())})])  # fmt: skip
     fake.group_state = lambda i, which: GPUAssembler.group_state(fake, i, which)
+    if want_E is not None:  # the device's aux fields: accepted E as [E11, E22, E33, E12, E23, E13]
+        En = temp["Enew"]  # [E, nInt, d, d]
+        d = En.shape[-1]
+        aux = np.zeros((E * nInt, 6))
+        for f, (i, j) in enumerate(((0, 0), (1, 1), (2, 2), (0, 1), (1, 2), (0, 2))):
+            if i < d and j < d:
+                aux[:, f] = En[:, :, i, j].reshape(-1)
+        fake.groups[0]._dev["auxRef"] = torch.from_numpy(aux.T.copy())
+        fake.groups[0]._dev["auxTemp"] = torch.from_numpy(aux.T.copy())
+        for el in elements:
+            el._Eold = np.zeros_like(el._Eold)
     write_back_state(fake, elements)
+    if want_E is not None:
+        for el, w in zip(elements, want_E):
+            assert np.abs(el._Eold - w).max() <= 1e-14 * max(np.abs(np.array(want_E)).max(), 1e-300)
     scale = max(np.abs(w).max() for w in want)
     for el, w, v in zip(elements, want, views):
         assert np.abs(el._stateVarsRef - w).max() <= 1e-12 * scale
@@ -164,7 +181,12 @@ def test_write_back_reproduces_the_reference_state(ref, dim, gen, lines, et, kin
         el._stateVarsRef[:, 0] = 7.0
     g0 = fake.groups[0]._dev
     g0["stateTemp"] = torch.zeros_like(g0["stateRef"])
+    if want_E is not None:  # and the accepted E back into the aux fields
+        aux_before = g0["auxRef"].clone()
+        g0["auxRef"].zero_()
     read_state_from_reference(fake, elements)
+    if want_E is not None:
+        assert torch.allclose(g0["auxRef"], aux_before, rtol=0, atol=0)
     assert torch.equal(g0["stateRef"], g0["stateTemp"])
     back = GPUAssembler.group_state(fake, 0, "ref")
     assert np.array_equal(back, np.stack([el._stateVarsRef for el in elements]))
