@@ -52,20 +52,27 @@ def test_aggregation_is_a_maximal_independent_set(nNodes):
     assert 1.5 < points / nAgg < 40
 
 
-def test_galerkin_map_and_transfer_match_scipy():
-    coords, ip, ix, n = _box_pattern(4, 3, 3)
+def _rect_pattern(nx, ny, nNodes=8):
+    coords, conn, nodeDof, nDof = meshes.rect(nx, ny, lX=1.0, lY=0.7, nNodes=nNodes)
+    indptr, indices = build_pattern(2, len(coords), nodeDof, nDof, [conn])[:2]
+    return coords, np.asarray(indptr), np.asarray(indices), nDof
+
+
+@pytest.mark.parametrize("dim", [3, 2])
+def test_galerkin_map_and_transfer_match_scipy(dim):
+    coords, ip, ix, n = _box_pattern(4, 3, 3) if dim == 3 else _rect_pattern(6, 4)
     rng = np.random.default_rng(0)
     vals = rng.normal(size=len(ix))
     A = sp.csr_matrix((vals, ix, ip), shape=(n, n))
     A = (A + A.T).tocsr()  # symmetric values on the same pattern
     A.sort_indices()
     ipT, ixT = torch.from_numpy(A.indptr.astype(np.int32)), torch.from_numpy(A.indices.astype(np.int32))
-    src, dst = amg.point_graph(ipT, ixT, 3)
-    agg, nAgg, _ = amg.mis_aggregate(src, dst, n // 3, seed=1)
-    nc = nAgg * 3
+    src, dst = amg.point_graph(ipT, ixT, dim)
+    agg, nAgg, _ = amg.mis_aggregate(src, dst, n // dim, seed=1)
+    nc = nAgg * dim
     mask = torch.ones(n, dtype=torch.float64)
     mask[torch.from_numpy(np.arange(0, n, 7))] = 0.0  # some prescribed DOFs
-    coarseOfDof = torch.repeat_interleave(agg, 3) * 3 + torch.arange(n) % 3
+    coarseOfDof = torch.repeat_interleave(agg, dim) * dim + torch.arange(n) % dim
     cnt = torch.zeros(nc, dtype=torch.float64).index_add_(0, coarseOfDof, mask)
     w = mask / torch.sqrt(torch.clamp(cnt, min=1.0))[coarseOfDof]
     (Pp, Pi, Pv), (Rp, Ri, Rv) = amg.transfer(coarseOfDof, w, nc)
