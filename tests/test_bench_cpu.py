@@ -58,3 +58,23 @@ def test_roofline_fraction_is_achieved_over_peak():
     assert r["frac"] == pytest.approx(2000.0 / peak)
     assert r["traffic"] == 3.0e9
 
+
+
+def test_reference_arm_under_torchrun_prints_one_line():
+    """Launched as the multi-GPU runs are (torch.distributed.run, two ranks, 127.0.0.1): rank 0
+    alone runs the reference arm and prints its line; the other rank exits 0 without work."""
+    import socket
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    env = dict(os.environ, PYTHONDONTWRITEBYTECODE="1")
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
+           "127.0.0.1", "--master-port", str(port), "bench.py", "--gpus", "2", "--impl", "reference", "--steps", "1",
+           "--warmup", "1"]  # the driver's own arguments (torchrun would claim an abbreviated --n)  # fmt: skip
+    out = subprocess.run(cmd, cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
