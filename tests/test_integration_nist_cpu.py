@@ -83,6 +83,36 @@ dirichlet, name=back, nSet=gen_back, field=displacement, 3=0.0
 dirichlet, name=top, nSet=gen_top, field=displacement, 2=0.1
 """
 
+TWO_SECTIONS = """
+*material, name=vonmises, id=vonmises, provider=edelweiss
+210000.0, 0.3, 250.0, 1000.0, 0.0, 0.0
+*material, name=linearelastic, id=soft, provider=edelweiss
+70000.0, 0.25
+*job, name=j2job, domain=3d
+*solver, solver={solver}, name=theSolver
+*modelGenerator, generator=boxGen, name=gen
+nX=3
+nY=2
+nZ=2
+lX=1
+lY=1
+lZ=1
+elProvider=edelweiss
+elType=C3D8
+*section, name=section1, material=vonmises, type=solid
+gen_bottom
+*section, name=section2, material=soft, type=solid
+gen_top
+*fieldOutput
+create=perElement, name=stress, elSet=gen_all, result=stress, quadraturePoint=0:8
+*step, solver=theSolver, maxInc=0.25, minInc=1e-6, maxNumInc=1000, maxIter=25, stepLength=1
+options, category=NISTSolver, extrapolation=linear, linsolver=superlu
+dirichlet, name=bot, nSet=gen_bottom, field=displacement, 2=0.0
+dirichlet, name=left, nSet=gen_left, field=displacement, 1=0.0
+dirichlet, name=back, nSet=gen_back, field=displacement, 3=0.0
+dirichlet, name=top, nSet=gen_top, field=displacement, 2=0.006
+"""
+
 NH_BLOCK = """
 *material, name=neohookewa, id=nh, provider=edelweiss
 384.6153846, 833.3333333
@@ -226,8 +256,8 @@ def _simulate(inp, tmp_path):
     return U, its, np.asarray(foc.fieldOutputs["stress"].getResultHistory())
 
 
-@pytest.mark.parametrize("inp", [J2_CUBE, J2_CUTBACK, NH_BLOCK], ids=["c3d8-vonmises", "c3d8-vonmises-cutback",
-                                                                      "c3d8tl-neohooke"])  # fmt: skip
+@pytest.mark.parametrize("inp", [J2_CUBE, J2_CUTBACK, TWO_SECTIONS, NH_BLOCK],
+                         ids=["c3d8-vonmises", "c3d8-vonmises-cutback", "two-sections", "c3d8tl-neohooke"])  # fmt: skip
 def test_subclass_reproduces_the_reference_simulation(ref, inp, tmp_path):
     import edelweissfe.config.solvers as solvers
     from edelweissfe.solvers.nonlinearimplicitstatic import NIST
