@@ -10,7 +10,7 @@ import os
 from . import _build
 
 # constants of include/efe_gb300.h
-EFE_ABI_VERSION = 1
+EFE_ABI_VERSION = 2
 EFE_QUAD4, EFE_QUAD8, EFE_HEXA8, EFE_HEXA20 = 0, 1, 2, 3
 EFE_RULE_2D_1, EFE_RULE_2D_2X2, EFE_RULE_2D_3X3 = 0, 1, 2
 EFE_RULE_3D_1, EFE_RULE_3D_2X2X2, EFE_RULE_3D_3X3X3 = 3, 4, 5

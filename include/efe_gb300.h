@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define EFE_ABI_VERSION 1
+#define EFE_ABI_VERSION 2
 
 /* element shapes (node numbering of computeNOperator, _elementcomputationmatrices.py:106-212) */
 enum { EFE_QUAD4 = 0, EFE_QUAD8 = 1, EFE_HEXA8 = 2, EFE_HEXA20 = 3 };
