@@ -803,7 +803,7 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
             acc[j][k] += pb[j] * ha[k] + qa[j] * hb[k] + c4s * ha[j] * gb[k] + (j == k ? c1s * dot : KT(0));
       } else if constexpr (FORM == TLV3) {
         const KT Lq = sc[0], Mq = sc[1], Aq = sc[2];
-        const KT FF[3][3] = {{sc[3], sc[4], sc[5]}, {sc[4], sc[6], sc[7]}, {sc[5], sc[7], sc[8]}};
+        const KT Fm[3][3] = {{sc[3], sc[4], sc[5]}, {sc[4], sc[6], sc[7]}, {sc[5], sc[7], sc[8]}};
         const KT* Ga = va;
         const KT* Gb = vb;
         const KT* ga = va + DIM;
@@ -821,7 +821,7 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
         for (int c = 0; c < DIM; ++c)
 #pragma unroll
           for (int d = 0; d < DIM; ++d)
-            acc[c][d] += Lq * ga[c] * gb[d] + Mq * (FF[c][d] * dot + gb[c] * ga[d]) - Aq * wa[c] * wb[d] +
+            acc[c][d] += Lq * ga[c] * gb[d] + Mq * (Fm[c][d] * dot + gb[c] * ga[d]) - Aq * wa[c] * wb[d] +
                          (c == d ? geo : KT(0));
       } else {  // TLV2
         const KT* C = sc;
