@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(BUILD, "libefe_gb300.so")
-SOURCES = ["efe_abi.cu", "efe_quad4.cu", "efe_quad8.cu", "efe_hexa8.cu", "efe_hexa20.cu", "efe_batch.cu", "efe_solve.cu"]
+SOURCES = ["efe_abi.cu", "efe_quad4.cu", "efe_quad8.cu", "efe_hexa8.cu", "efe_hexa20.cu", "efe_batch.cu", "efe_solve.cu", "efe_probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE]
 

@@ -34,6 +34,7 @@ EXPORTS = [
     "efe_compute_elements_persistent",
     "efe_compute_elements_persistent_noalloc",
     "efe_accept_state",
+    "efe_fma_probe",
     "efe_csr_spmv",
     "efe_pcg_start",
     "efe_pcg_iterate",
@@ -213,6 +214,8 @@ def load(build_if_missing=False):
     lib.efe_split_pairs.argtypes = [i64, P, P, P]
     lib.efe_accept_state.restype = i32
     lib.efe_accept_state.argtypes = [ctypes.POINTER(EfeGroup), i32, P]
+    lib.efe_fma_probe.restype = i32
+    lib.efe_fma_probe.argtypes = [i32, i32, i64, P, P, P]
     lib.efe_pattern_count.restype = i64
     lib.efe_pattern_count.argtypes = [i32, i32, P, i32, P, P, P, i64, P, P]
     lib.efe_pattern_fill.restype = i32

@@ -84,18 +84,36 @@ class MeshBatch:
                 slice(int(self.nnz_offsets[i]), int(self.nnz_offsets[i + 1])))  # fmt: skip
 
 
-# element types of the persistent kernel (efe_compute_elements_persistent)
-PERSISTENT_TYPES = {"C3D20TL": "heavy", "C3D20NTL": "heavy", "CPE8RTL": "light", "CPS8RTL": "light"}
+# element types of the persistent kernel (efe_compute_elements_persistent), in its hand-out order:
+# (shape, rule, kinematics, hyperelastic material) -> type index of the kernel
+PERSISTENT_TYPES = {
+    (L.EFE_HEXA20, L.EFE_RULE_3D_3X3X3, L.EFE_TOTAL_LAGRANGIAN, True): 0,  # e.g. C3D20TL Neo-Hooke
+    (L.EFE_HEXA20, L.EFE_RULE_3D_3X3X3, L.EFE_SMALL_STRAIN, False): 1,  # C3D20 von Mises / linear elastic
+    (L.EFE_HEXA8, L.EFE_RULE_3D_2X2X2, L.EFE_TOTAL_LAGRANGIAN, True): 2,  # C3D8TL Neo-Hooke
+    (L.EFE_HEXA8, L.EFE_RULE_3D_2X2X2, L.EFE_SMALL_STRAIN, False): 3,  # C3D8 von Mises / linear elastic
+    (L.EFE_QUAD8, L.EFE_RULE_2D_2X2, L.EFE_TOTAL_LAGRANGIAN, True): 4,  # CPE8RTL Neo-Hooke
+}
 PERSISTENT_MAX_GROUPS = 8
 
 
+def persistent_type(elType, material):
+    """Type index of an element type and material in the persistent kernel, or None."""
+    from .library import element_type
+
+    et = element_type(elType)
+    hyper = material.lower().startswith("neohooke")
+    if hyper and et.plane == L.EFE_PLANE_STRESS:
+        return None  # the reference has no plane-stress hyperelasticity
+    return PERSISTENT_TYPES.get((et.shape, et.rule, et.kinematics, hyper))
+
+
 def persistent_capable(batches):
-    """True if one persistent launch can run all batches: total-Lagrangian Neo-Hooke Hexa20 3x3x3 and
-    Quad8 2x2 batches, at most eight of each, one precision."""
-    kinds = [PERSISTENT_TYPES.get(b.asm.groups[0].elType.upper()) for b in batches]
-    if None in kinds or any(not b.asm.groups[0].material.lower().startswith("neohooke") for b in batches):
+    """True if one persistent launch can run all batches: every batch of a type of the persistent
+    kernel (PERSISTENT_TYPES), at most eight batches of each type, one precision."""
+    kinds = [persistent_type(b.asm.groups[0].elType, b.asm.groups[0].material) for b in batches]
+    if None in kinds or any(len(b.asm.groups) != 1 for b in batches):
         return False
-    if kinds.count("heavy") > PERSISTENT_MAX_GROUPS or kinds.count("light") > PERSISTENT_MAX_GROUPS:
+    if any(kinds.count(k) > PERSISTENT_MAX_GROUPS for k in set(kinds)):
         return False
     # one precision for all, FP64 or the FP32 tangent (the persistent kernel has no float-float form)
     precs = {b.asm.kPrecision for b in batches}

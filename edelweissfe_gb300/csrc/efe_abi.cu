@@ -1,5 +1,6 @@
 // efe_abi.cu -- extern "C" entry points of libefe_gb300 (declared in include/efe_gb300.h).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -411,11 +412,14 @@ int32_t efe_adjoint_small_strain(const EfeMesh* mesh, const EfeGroup* g, const d
 }
 
 namespace {
-// Sort the work items of a persistent pass by element type: heavy = Hexa20 3x3x3 and light = Quad8
-// 2x2, both total-Lagrangian Neo-Hooke.
+// The work items of a persistent pass, sorted by element type (efe::persistent_type_index).
+struct PersistentItems {
+  efe::GroupArgs g[efe::PERSISTENT_NTYPES][efe::MAX_PERSISTENT_GROUPS];
+  int n[efe::PERSISTENT_NTYPES] = {};
+};
+
 int32_t persistent_items(const EfeWorkItem* items, int32_t nItems, int32_t kPrecision, int32_t* status,
-                         efe::GroupArgs* heavy, int& nHeavy, efe::GroupArgs* light, int& nLight) {
-  nHeavy = nLight = 0;
+                         PersistentItems& out) {
   if (!items || nItems < 1 || !status) return fail(EFE_ERR_ARGUMENT, "work items and a status word expected");
   if (kPrecision != EFE_K_FP64 && kPrecision != EFE_K_FP32) return fail(EFE_ERR_ARGUMENT, "unknown K precision");
   for (int32_t i = 0; i < nItems; ++i) {
@@ -427,17 +431,17 @@ int32_t persistent_items(const EfeWorkItem* items, int32_t nItems, int32_t kPrec
     rc = check_item_buffers(*it.group, it.U, it.dU);
     if (rc) return rc;
     const EfeGroup& g = *it.group;
-    const int form = form_of(g);
-    const bool h = g.shape == EFE_HEXA20 && g.rule == EFE_RULE_3D_3X3X3 && form == efe::TLH;
-    const bool l = g.shape == EFE_QUAD8 && g.rule == EFE_RULE_2D_2X2 && form == efe::TLH;
-    if (!h && !l)
-      return fail(EFE_ERR_UNSUPPORTED, "no persistent kernel for this element type (implemented: Hexa20 3x3x3 and "
-                                       "Quad8 2x2, total-Lagrangian Neo-Hooke)");
-    int& n = h ? nHeavy : nLight;
+    const int type = efe::persistent_type_index(g.shape, g.rule, form_of(g));
+    if (type < 0)
+      return fail(EFE_ERR_UNSUPPORTED,
+                  "no persistent kernel for this element type (implemented: Hexa20 3x3x3 and Hexa8 2x2x2 total-"
+                  "Lagrangian Neo-Hooke and small-strain von Mises / linear elastic, Quad8 2x2 total-Lagrangian "
+                  "Neo-Hooke)");
+    int& n = out.n[type];
     if (n == efe::MAX_PERSISTENT_GROUPS)
       return fail(EFE_ERR_ARGUMENT, "at most " + std::to_string(efe::MAX_PERSISTENT_GROUPS) +
                                         " groups of each element type in one persistent pass");
-    (h ? heavy : light)[n++] = make_args(it.mesh, g, it.U, it.dU, it.Kdata, it.P, it.F, status);
+    out.g[type][n++] = make_args(it.mesh, g, it.U, it.dU, it.Kdata, it.P, it.F, status);
   }
   return EFE_OK;
 }
@@ -446,11 +450,10 @@ int32_t persistent_items(const EfeWorkItem* items, int32_t nItems, int32_t kPrec
 int32_t efe_compute_elements_persistent(const EfeWorkItem* items, int32_t nItems, int32_t kPrecision,
                                         uint64_t* workCounter, int32_t* status, void* stream) {
   if (!workCounter) return fail(EFE_ERR_ARGUMENT, "null work counter");
-  efe::GroupArgs heavy[efe::MAX_PERSISTENT_GROUPS], light[efe::MAX_PERSISTENT_GROUPS];
-  int nHeavy = 0, nLight = 0;
-  int32_t rc = persistent_items(items, nItems, kPrecision, status, heavy, nHeavy, light, nLight);
+  PersistentItems pi;
+  int32_t rc = persistent_items(items, nItems, kPrecision, status, pi);
   if (rc) return rc;
-  cudaError_t e = efe::persistent_groups(kPrecision, heavy, nHeavy, light, nLight, (unsigned long long*)workCounter,
+  cudaError_t e = efe::persistent_groups(kPrecision, pi.g, pi.n, (unsigned long long*)workCounter,
                                          (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "efe_compute_elements_persistent");
   return EFE_OK;
@@ -460,13 +463,11 @@ int32_t efe_compute_elements_persistent(const EfeWorkItem* items, int32_t nItems
 // library's static scratch array (efe_batch.cu), so nothing here allocates device memory.
 int32_t efe_compute_elements_persistent_noalloc(const EfeWorkItem* items, int32_t nItems, int32_t kPrecision,
                                                 int32_t* status, void* stream) {
-  efe::GroupArgs heavy[efe::MAX_PERSISTENT_GROUPS], light[efe::MAX_PERSISTENT_GROUPS];
-  int nHeavy = 0, nLight = 0;
-  int32_t rc = persistent_items(items, nItems, kPrecision, status, heavy, nHeavy, light, nLight);
+  PersistentItems pi;
+  int32_t rc = persistent_items(items, nItems, kPrecision, status, pi);
   if (rc) return rc;
   int64_t needed = 0;
-  cudaError_t e =
-      efe::persistent_groups_noalloc(kPrecision, heavy, nHeavy, light, nLight, &needed, (cudaStream_t)stream);
+  cudaError_t e = efe::persistent_groups_noalloc(kPrecision, pi.g, pi.n, &needed, (cudaStream_t)stream);
   if (needed > EFE_NOALLOC_MAX_TILES) {
     return fail(EFE_ERR_ARGUMENT, "efe_compute_elements_persistent_noalloc: the batch needs " + std::to_string(needed) +
                                       " tile indices, the 32-bit work counter in the static scratch allows at most " +
@@ -577,6 +578,15 @@ int32_t efe_pcg_iterate(const EfePcg* s, int64_t firstIteration, int32_t nIterat
   return EFE_OK;
 }
 
+int32_t efe_fma_probe(int32_t fp64, int32_t blocks, int64_t iterations, void* sink, void* stream,
+                      int64_t* flops) {
+  if (blocks < 1 || iterations < 0 || !sink || !flops) return fail(EFE_ERR_ARGUMENT, "efe_fma_probe: bad argument");
+  *flops = efe::fma_probe_flops(blocks, iterations);
+  cudaError_t e = efe::fma_probe(fp64, blocks, iterations, sink, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "efe_fma_probe");
+  return EFE_OK;
+}
+
 int32_t efe_accept_state(const EfeGroup* groups, int32_t nGroups, void* stream) {
   if (!groups || nGroups < 0) return fail(EFE_ERR_ARGUMENT, "null argument");
   cudaStream_t st = (cudaStream_t)stream;
@@ -650,7 +660,7 @@ int32_t efe_pattern_fill(int32_t dim, int32_t nNodes, const int32_t* nodeDof, in
     }
   });
   if (pairSlots) {
-    int32_t bad = 0;
+    std::atomic<int32_t> bad{0};  // set by any of the parallel_for threads
     for (int g = 0; g < nGroups; ++g) {
       if (!pairSlots[g]) continue;
       const int32_t* conn = conns[g];
@@ -665,7 +675,7 @@ int32_t efe_pattern_fill(int32_t dim, int32_t nNodes, const int32_t* nodeDof, in
             const int32_t* end = indices + indptr[rowDof + 1];
             const int32_t* it = std::lower_bound(beg, end, colDof);
             if (it == end || *it != colDof) {
-              bad = 1;
+              bad.store(1, std::memory_order_relaxed);
               slots[(e * m + a) * m + b] = -1;
             } else {
               slots[(e * m + a) * m + b] = (int32_t)(it - indices);
@@ -673,7 +683,7 @@ int32_t efe_pattern_fill(int32_t dim, int32_t nNodes, const int32_t* nodeDof, in
           }
       });
     }
-    if (bad) return fail(EFE_ERR_PATTERN, "element node pair missing from the pattern");
+    if (bad.load()) return fail(EFE_ERR_PATTERN, "element node pair missing from the pattern");
   }
   return EFE_OK;
 }

@@ -1,5 +1,6 @@
-// efe_batch.cu -- persistent launch over several element groups of two types (uneven batches of
-// meshes), and its variant for callers that cannot allocate device memory.
+// efe_batch.cu -- persistent launch over several element groups of mixed types (uneven batches of
+// meshes and load cases), and its variant for callers that cannot allocate device memory.
+#include <initializer_list>
 #include <mutex>
 
 #include "efe_launch.cuh"
@@ -9,8 +10,7 @@ namespace efe {
 namespace {
 
 // Fill a group table: group k owns ceil(nElements / EPB) tiles.
-template <int EPB>
-void fill_table(GroupTable& t, const GroupArgs* g, int n) {
+void fill_table(GroupTable& t, const GroupArgs* g, int n, int EPB) {
   t = GroupTable{};
   t.n = n;
   t.tileStart[0] = 0;
@@ -20,20 +20,40 @@ void fill_table(GroupTable& t, const GroupArgs* g, int n) {
   }
 }
 
-// heavy: Hexa20 3x3x3 total-Lagrangian Neo-Hooke groups, light: Quad8 2x2 total-Lagrangian
-// Neo-Hooke groups; the heavier tiles are handed out first
-template <typename KT, typename CT>
-cudaError_t run_groups(const GroupArgs* heavy, int nHeavy, const GroupArgs* light, int nLight, CT* counter,
-                       int64_t maxTiles, int64_t* needed, cudaStream_t st) {
-  constexpr int SA = EFE_HEXA20, RA = EFE_RULE_3D_3X3X3, SB = EFE_QUAD8, RB = EFE_RULE_2D_2X2;
-  using TA = Tile<SA, RA, TLH, KT>;
-  using TB = Tile<SB, RB, TLH, KT>;
-  static_assert(TA::NT == TB::NT, "both tile types must use the same CTA size");
-  constexpr int NT = TA::NT;
-  constexpr size_t bytes = TA::bytes > TB::bytes ? TA::bytes : TB::bytes;
-  if (nHeavy < 0 || nLight < 0 || nHeavy > MAX_PERSISTENT_GROUPS || nLight > MAX_PERSISTENT_GROUPS)
-    return cudaErrorInvalidValue;
-  auto kern = assemble_persistent_kernel<SA, RA, TLH, TA::EPB, SB, RB, TLH, TB::EPB, KT, NT, CT>;
+// The element types of the persistent pass by persistent_type_index, each with its variant-0 tile
+// (128 threads): the (shape, rule, form, elements per tile) and the tile's shared memory.
+template <int IDX, typename KT> struct TypeOf;
+template <int S, int R, int F, typename KT>
+struct TypeOfBase {
+  using T = PersistentType<S, R, F, Tile<S, R, F, KT>::EPB>;
+  static constexpr size_t bytes = Tile<S, R, F, KT>::bytes;
+  static constexpr int NT = Tile<S, R, F, KT>::NT;
+};
+template <typename KT> struct TypeOf<0, KT> : TypeOfBase<EFE_HEXA20, EFE_RULE_3D_3X3X3, TLH, KT> {};
+template <typename KT> struct TypeOf<1, KT> : TypeOfBase<EFE_HEXA20, EFE_RULE_3D_3X3X3, SS3, KT> {};
+template <typename KT> struct TypeOf<2, KT> : TypeOfBase<EFE_HEXA8, EFE_RULE_3D_2X2X2, TLH, KT> {};
+template <typename KT> struct TypeOf<3, KT> : TypeOfBase<EFE_HEXA8, EFE_RULE_3D_2X2X2, SS3, KT> {};
+template <typename KT> struct TypeOf<4, KT> : TypeOfBase<EFE_QUAD8, EFE_RULE_2D_2X2, TLH, KT> {};
+
+constexpr size_t max_of(std::initializer_list<size_t> v) {
+  size_t m = 0;
+  for (size_t x : v) m = x > m ? x : m;
+  return m;
+}
+
+// One persistent kernel over the types IDX... (in that order; every other type must have no groups),
+// with registers held to MINB resident CTAs per SM.
+template <typename KT, typename CT, int MINB, int... IDX>
+cudaError_t run_list(const GroupArgs (*groups)[MAX_PERSISTENT_GROUPS], const int* nGroups, CT* counter,
+                     int64_t maxTiles, int64_t* needed, cudaStream_t st) {
+  constexpr int N = sizeof...(IDX);
+  constexpr int idx[N] = {IDX...};
+  constexpr int epb[N] = {TypeOf<IDX, KT>::T::EPB...};
+  constexpr int NT = 128;
+  static_assert(((TypeOf<IDX, KT>::NT == NT) && ...), "all tiles of a persistent kernel use 128 threads");
+  constexpr size_t bytes = max_of({TypeOf<IDX, KT>::bytes...});
+  static_assert(bytes <= 200 * 1024, "persistent tile does not fit in shared memory");
+  auto kern = assemble_persistent_kernel<KT, NT, MINB, CT, typename TypeOf<IDX, KT>::T...>;
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (err != cudaSuccess) return err;
   int dev = 0, sms = 0, perSM = 0;
@@ -41,34 +61,52 @@ cudaError_t run_groups(const GroupArgs* heavy, int nHeavy, const GroupArgs* ligh
   if ((err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return err;
   if ((err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, NT, bytes)) != cudaSuccess) return err;
   if (perSM < 1) return cudaErrorInvalidConfiguration;
-  GroupTable ta, tb;
-  fill_table<TA::EPB>(ta, heavy, nHeavy);
-  fill_table<TB::EPB>(tb, light, nLight);
-  const int64_t tilesA = ta.tileStart[nHeavy], tilesB = tb.tileStart[nLight];
+  GroupTables<N> tabs;
+  int64_t tiles = 0;
+  for (int j = 0; j < N; ++j) {
+    fill_table(tabs.t[j], groups[idx[j]], nGroups[idx[j]], epb[j]);
+    tiles += tabs.t[j].tileStart[nGroups[idx[j]]];
+  }
   int64_t grid = (int64_t)sms * perSM;
-  if (grid > tilesA + tilesB) grid = tilesA + tilesB;
-  // the counter ends at tilesA + tilesB + grid (every CTA takes one tile index past the end)
-  if (needed) *needed = tilesA + tilesB + grid;
-  if (tilesA + tilesB + grid > maxTiles) return cudaErrorInvalidValue;
+  if (grid > tiles) grid = tiles;
+  // the counter ends at tiles + grid (every CTA takes one tile index past the end)
+  if (needed) *needed = tiles + grid;
+  if (tiles + grid > maxTiles) return cudaErrorInvalidValue;
   if ((err = cudaMemsetAsync(counter, 0, sizeof(CT), st)) != cudaSuccess) return err;
   if (grid == 0) return cudaSuccess;
-  kern<<<(unsigned)grid, NT, bytes, st>>>(ta, tb, counter);
+  kern<<<(unsigned)grid, NT, bytes, st>>>(tabs, counter);
   return cudaGetLastError();
 }
 
+// The smallest instantiated type list covering the types present: total-Lagrangian Neo-Hooke Hexa20
+// + Quad8 (batches of uneven 2D/3D meshes), Hexa8 small strain alone (load cases of one material,
+// four CTAs per SM as tile variant 2), or all five types.
+template <typename KT, typename CT>
+cudaError_t run_groups(const GroupArgs (*groups)[MAX_PERSISTENT_GROUPS], const int* nGroups, CT* counter,
+                       int64_t maxTiles, int64_t* needed, cudaStream_t st) {
+  unsigned present = 0;
+  for (int k = 0; k < PERSISTENT_NTYPES; ++k) {
+    if (nGroups[k] < 0 || nGroups[k] > MAX_PERSISTENT_GROUPS) return cudaErrorInvalidValue;
+    if (nGroups[k] > 0) present |= 1u << k;
+  }
+  if ((present & ~((1u << 0) | (1u << 4))) == 0)
+    return run_list<KT, CT, 1, 0, 4>(groups, nGroups, counter, maxTiles, needed, st);
+  if ((present & ~(1u << 3)) == 0) return run_list<KT, CT, 4, 3>(groups, nGroups, counter, maxTiles, needed, st);
+  return run_list<KT, CT, 2, 0, 1, 2, 3, 4>(groups, nGroups, counter, maxTiles, needed, st);
+}
+
 template <typename CT>
-cudaError_t persistent_groups_t(int kprec, const GroupArgs* heavy, int nHeavy, const GroupArgs* light, int nLight,
+cudaError_t persistent_groups_t(int kprec, const GroupArgs (*groups)[MAX_PERSISTENT_GROUPS], const int* nGroups,
                                 CT* counter, int64_t maxTiles, int64_t* needed, cudaStream_t st) {
-  if (kprec == EFE_K_FP32)
-    return run_groups<float>(heavy, nHeavy, light, nLight, counter, maxTiles, needed, st);
-  return run_groups<double>(heavy, nHeavy, light, nLight, counter, maxTiles, needed, st);
+  if (kprec == EFE_K_FP32) return run_groups<float>(groups, nGroups, counter, maxTiles, needed, st);
+  return run_groups<double>(groups, nGroups, counter, maxTiles, needed, st);
 }
 
 }  // namespace
 
-cudaError_t persistent_groups(int kprec, const GroupArgs* heavy, int nHeavy, const GroupArgs* light, int nLight,
+cudaError_t persistent_groups(int kprec, const GroupArgs (*groups)[MAX_PERSISTENT_GROUPS], const int* nGroups,
                               unsigned long long* counter, cudaStream_t st) {
-  return persistent_groups_t(kprec, heavy, nHeavy, light, nLight, counter, INT64_MAX, nullptr, st);
+  return persistent_groups_t(kprec, groups, nGroups, counter, INT64_MAX, nullptr, st);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -110,12 +148,12 @@ cudaError_t noalloc_scratch_address(unsigned int** out) {
 
 }  // namespace
 
-cudaError_t persistent_groups_noalloc(int kprec, const GroupArgs* heavy, int nHeavy, const GroupArgs* light,
-                                      int nLight, int64_t* needed, cudaStream_t st) {
+cudaError_t persistent_groups_noalloc(int kprec, const GroupArgs (*groups)[MAX_PERSISTENT_GROUPS], const int* nGroups,
+                                      int64_t* needed, cudaStream_t st) {
   unsigned int* counter = nullptr;
   cudaError_t err = noalloc_scratch_address(&counter);
   if (err != cudaSuccess) return err;
-  return persistent_groups_t(kprec, heavy, nHeavy, light, nLight, counter, (int64_t)EFE_NOALLOC_MAX_TILES, needed, st);
+  return persistent_groups_t(kprec, groups, nGroups, counter, (int64_t)EFE_NOALLOC_MAX_TILES, needed, st);
 }
 
 }  // namespace efe

@@ -227,6 +227,85 @@ __device__ __forceinline__ void ff_fma(ff& acc, ff a, ff b) {
   acc.l = __fadd_rn(acc.l, __fadd_rn(err, e));
   acc.h = s;
 }
+// ------------------------------------------------------------------ conversions off the FP64 pipe
+// On this GPU the conversions between double and float (F2F) issue on the FP64 pipe, which binds
+// the element pass; a float-float pass spends about a third of that pipe on them.  The forms below
+// give the same values (or an equally accurate split) with integer and FP32 instructions, from the
+// IEEE-754 bit layouts: float = sign | exponent (8, bias 127) | fraction (23); double = sign |
+// exponent (11, bias 1023) | fraction (52).  Arguments outside the ranges they handle (zero is
+// handled; subnormals, infinities, NaN and magnitudes beyond the float range) take the hardware
+// conversions.
+
+// float -> double, exact
+__device__ __forceinline__ double f2d_bits(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t e = (b >> 23) & 0xffu;
+  if (e - 1u < 254u) {  // normal: exponent + (1023 - 127), fraction shifted to the top of 52 bits
+    const uint64_t mag = ((uint64_t)(b & 0x7fffffffu) << 29) + (896ull << 52);
+    return __longlong_as_double((long long)(((uint64_t)(b & 0x80000000u) << 32) | mag));
+  }
+  if ((b & 0x7fffffffu) == 0u) return __longlong_as_double((long long)((uint64_t)b << 32));  // +-0
+  return (double)f;
+}
+
+// double -> float, rounded toward zero (the 23 leading fraction bits)
+__device__ __forceinline__ float d2f_trunc(double x) {
+  const uint64_t X = (uint64_t)__double_as_longlong(x);
+  const uint32_t hi = (uint32_t)(X >> 32), lo = (uint32_t)X;
+  const uint32_t E = (hi >> 20) & 0x7ffu;
+  if (E - 897u < 254u)  // the float exponent E - 896 is in [1, 254]; the exponent bits wrap mod 2^32
+    return __uint_as_float((hi & 0x80000000u) | ((((hi & 0x7fffffffu) << 3) | (lo >> 29)) - (896u << 23)));
+  if (((hi & 0x7fffffffu) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
+  return __double2float_rn(x);
+}
+
+// double -> (hi, lo): hi = x rounded toward zero to 24 bits, lo = fl32(x - hi) (x - hi is the low 29
+// fraction bits times 2^(E - 1075); fl32 of that integer from its exact 13- and 16-bit halves and
+// one rounding FMA).  hi + lo agrees with x to ~2^-47 relative, like ff_split's.
+__device__ __forceinline__ ff ff_split_bits(double x) {
+  const uint64_t X = (uint64_t)__double_as_longlong(x);
+  const uint32_t hi = (uint32_t)(X >> 32), lo = (uint32_t)X;
+  const uint32_t E = (hi >> 20) & 0x7ffu;
+  if (E - 949u < 202u) {  // E in [949, 1150]: hi normal, and 2^(E - 1075) a normal float
+    const uint32_t sign = hi & 0x80000000u;
+    const float h = __uint_as_float(sign | ((((hi & 0x7fffffffu) << 3) | (lo >> 29)) - (896u << 23)));
+    const uint32_t R = lo & 0x1fffffffu;
+    const float r1 = __fsub_rn(__uint_as_float(0x4B000000u | (R >> 16)), 8388608.0f);      // exact
+    const float r0 = __fsub_rn(__uint_as_float(0x4B000000u | (R & 0xffffu)), 8388608.0f);  // exact
+    const float l = __fmul_rn(__fmaf_rn(r1, 65536.0f, r0), __uint_as_float((E - 948u) << 23));
+    return ff{h, sign ? -l : l};
+  }
+  if (((hi & 0x7fffffffu) | lo) == 0u) return ff{__uint_as_float(hi & 0x80000000u), 0.0f};
+  return ff_split(x);
+}
+
+// hi + lo as a double: exact conversions, one rounding add
+__device__ __forceinline__ double ff_to_double_bits(ff a) { return f2d_bits(a.h) + f2d_bits(a.l); }
+
+// not infinite and not NaN, from the exponent bits
+__device__ __forceinline__ bool finite_bits(double x) {
+  return ((uint32_t)((uint64_t)__double_as_longlong(x) >> 32) & 0x7ff00000u) != 0x7ff00000u;
+}
+
+// the tangent's precision: doubles pass through, floats are truncated off the FP64 pipe
+template <typename KT>
+__device__ __forceinline__ KT to_kt(double x) {
+  if constexpr (sizeof(KT) == 4)
+    return d2f_trunc(x);
+  else
+    return x;
+}
+
+// a * b (both float-float), renormalised
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  const float s = __fadd_rn(p, e);
+  return ff{s, __fsub_rn(e, __fsub_rn(s, p))};
+}
+
 // acc += a
 __device__ __forceinline__ void ff_add(ff& acc, ff a) {
   const float s = __fadd_rn(acc.h, a.h);

@@ -215,7 +215,7 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
         // displacement relative to node 0 (sum_a dN_a/dX = 0): no cancellation in the strain sum
         const int32_t dof0 = g.nodeDof[g.conn[e * NN]];
         ff* sf = reinterpret_cast<ff*>(su);
-        for (int c = 0; c < DIM; ++c) sf[(le * NN + a) * DIM + c] = ff_split(Ux[dof + c] - Ux[dof0 + c]);
+        for (int c = 0; c < DIM; ++c) sf[(le * NN + a) * DIM + c] = ff_split_bits(Ux[dof + c] - Ux[dof0 + c]);
       } else {
         for (int c = 0; c < DIM; ++c) su[(le * NN + a) * DIM + c] = Ux[dof + c];
       }
@@ -255,7 +255,7 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
         for (int a = 0; a < NN; ++a)
           ff_fma(acc, uf[a * DIM + i],
                  ff{g.geomG32[(int64_t)(j * NN + a) * stride + pt], g.geomGlo[(int64_t)(j * NN + a) * stride + pt]});
-        f += ff_to_double(acc);
+        f += ff_to_double_bits(acc);
       } else {
         const double* u = su + le * NN * DIM;
         double h = 0.0;
@@ -312,16 +312,17 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
       }
       const double s = g.geomS[pt];
       KT* sc = ssc + (le * NQ + q) * L::SC;
-      sc[0] = (KT)(o.c1 * s);
-      sc[1] = (KT)(o.c4 * s);
+      const KT c1s = to_kt<KT>(o.c1 * s);
+      sc[0] = c1s;
+      sc[1] = to_kt<KT>(o.c4 * s);
       for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) {
           rec[i * 3 + j] = F[i][j];
           rec[9 + i * 3 + j] = iF[i][j];
           rec[18 + i * 3 + j] = o.tau[i][j];
           rec[27 + i * 3 + j] = o.Bm[i][j];
-          reck[i * 3 + j] = (KT)F[i][j];
-          reck[9 + i * 3 + j] = (KT)o.Bm[i][j];
+          reck[i * 3 + j] = to_kt<KT>(F[i][j]);
+          reck[9 + i * 3 + j] = to_kt<KT>(o.Bm[i][j]);
         }
       rec[36] = o.c1;
       rec[37] = o.c2;
@@ -332,14 +333,14 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
         ff* recf = reinterpret_cast<ff*>(rec);
         for (int i = 0; i < 3; ++i)
           for (int j = 0; j < 3; ++j) {
-            recf[9 + i * 3 + j] = ff_split(iF[i][j]);
-            recf[18 + i * 3 + j] = ff_split(o.tau[i][j]);
+            recf[9 + i * 3 + j] = ff_split_bits(iF[i][j]);
+            recf[18 + i * 3 + j] = ff_split_bits(o.tau[i][j]);
           }
-        recf[39] = ff_split(s);
+        recf[39] = ff_split_bits(s);
       }
-      reck[18] = (KT)(o.c1 * s);
-      reck[19] = (KT)(o.c2 * s);
-      reck[20] = (KT)(o.c3 * s);
+      reck[18] = c1s;
+      reck[19] = to_kt<KT>(o.c2 * s);
+      reck[20] = to_kt<KT>(o.c3 * s);
       // state write (stateTemp = updated copy of stateRef)
       for (int f = 0; f < 6; ++f) {
         g.stateTemp[(int64_t)f * stride + pt] = sig[f];
@@ -347,7 +348,7 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
       }
       g.stateTemp[(int64_t)12 * stride + pt] = o.energy;
       bool finite = true;
-      for (int f = 0; f < 6; ++f) finite = finite && isfinite(sig[f]);
+      for (int f = 0; f < 6; ++f) finite = finite && finite_bits(sig[f]);
       if (!finite) atomicOr(g.status, EFE_STATUS_NONFINITE);
     }
     __syncthreads();
@@ -376,9 +377,9 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
           for (int i = 0; i < DIM; ++i) ff_fma(th, recf[18 + j * 3 + i], h[i]);
           ff_fma(ths, th, recf[39]);
           rf[a * DIM + j] = ths;
-          Gk[j] = (KT)Gf[j].h;
-          hk[j] = (KT)h[j].h;
-          thk[j] = (KT)ths.h;
+          Gk[j] = Gf[j].h;
+          hk[j] = h[j].h;
+          thk[j] = ths.h;
         }
       } else {
         double G[3] = {0, 0, 0};
@@ -393,14 +394,14 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
           for (int i = 0; i < DIM; ++i) th += rec[18 + j * 3 + i] * h[i];
           const double ths = th * s;
           rq[a * DIM + j] = ths;
-          thk[j] = (KT)ths;
+          thk[j] = to_kt<KT>(ths);
         }
         for (int j = 0; j < DIM; ++j) {
           if constexpr (std::is_same<KT, float>::value)
-            Gk[j] = g.geomG32 ? (KT)g.geomG32[(int64_t)(j * NN + a) * stride + pt] : (KT)G[j];
+            Gk[j] = g.geomG32 ? g.geomG32[(int64_t)(j * NN + a) * stride + pt] : to_kt<KT>(G[j]);
           else
-            Gk[j] = (KT)G[j];
-          hk[j] = (KT)h[j];
+            Gk[j] = G[j];
+          hk[j] = to_kt<KT>(h[j]);
         }
       }
       for (int i = 0; i < DIM; ++i) {
@@ -471,7 +472,7 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
           ff_fma(acc[5], Gf[2 % DIM][a], uy);
           ff_fma(acc[5], Gf[1][a], uz);
         }
-        for (int f = 0; f < 6; ++f) de[f] = ff_to_double(acc[f]);
+        for (int f = 0; f < 6; ++f) de[f] = ff_to_double_bits(acc[f]);
       } else if constexpr (DIM == 3) {
         for (int a = 0; a < NN; ++a) {
           const double ux = u[a * 3 + 0], uy = u[a * 3 + 1], uz = u[a * 3 + 2];
@@ -500,11 +501,10 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
         else
           linear_elastic_3d(smc[le], sig, de, T);
         // residual r_a = s * sigma . G_a   (small-strain Voigt order 11,22,33,12,13,23)
-        double ss[6];
-        for (int f = 0; f < 6; ++f) ss[f] = sig[f] * s;
         if constexpr (FF) {
           ff sf[6];
-          for (int f = 0; f < 6; ++f) sf[f] = ff_split(ss[f]);
+          const ff s_ff = ff_split_bits(s);
+          for (int f = 0; f < 6; ++f) sf[f] = ff_mul(ff_split_bits(sig[f]), s_ff);
           ff* rf = reinterpret_cast<ff*>(rq);
           for (int a = 0; a < NN; ++a) {
             ff r0{0, 0}, r1{0, 0}, r2{0, 0};
@@ -522,6 +522,8 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
             rf[a * DIM + 2 % DIM] = r2;
           }
         } else {
+          double ss[6];
+          for (int f = 0; f < 6; ++f) ss[f] = sig[f] * s;
           for (int a = 0; a < NN; ++a) {
             const double gx = Gm[0][a], gy = Gm[1][a], gz = Gm[2 % DIM][a];
             rq[a * DIM + 0] = ss[0] * gx + ss[3] * gy + ss[4] * gz;
@@ -529,18 +531,18 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
             rq[a * DIM + 2 % DIM] = ss[4] * gx + ss[5] * gy + ss[2] * gz;
           }
         }
-        sc[0] = (KT)(T.c12 * s);
-        sc[1] = (KT)(T.c44 * s);
-        sc[2] = (KT)(T.a * s);
+        sc[0] = to_kt<KT>(T.c12 * s);
+        sc[1] = to_kt<KT>(T.c44 * s);
+        sc[2] = to_kt<KT>(T.a * s);
         // tangent vectors G_a and n.G_a in the tangent's precision (FP32 copy of G when present)
         KT n[6];
-        for (int f = 0; f < 6; ++f) n[f] = (KT)T.n[f];
+        for (int f = 0; f < 6; ++f) n[f] = to_kt<KT>(T.n[f]);
         for (int a = 0; a < NN; ++a) {
           KT gx, gy, gz;
           if constexpr (FF) {
-            gx = (KT)Gf[0][a].h;
-            gy = (KT)Gf[1][a].h;
-            gz = (KT)Gf[2 % DIM][a].h;
+            gx = Gf[0][a].h;
+            gy = Gf[1][a].h;
+            gz = Gf[2 % DIM][a].h;
           } else if (std::is_same<KT, float>::value && g.geomG32) {
             gx = (KT)g.geomG32[(int64_t)(0 * NN + a) * stride + pt];
             gy = (KT)g.geomG32[(int64_t)(1 * NN + a) * stride + pt];
@@ -712,7 +714,7 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
     }
     if (hasM) g.stateTemp[(int64_t)12 * stride + pt] = kappa;
     bool finite = true;
-    for (int f = 0; f < 6; ++f) finite = finite && isfinite(sig[f]);
+    for (int f = 0; f < 6; ++f) finite = finite && finite_bits(sig[f]);
     if (!ok) report(g.status, EFE_STATUS_CUTBACK, g.elementOffset + e, 1);
     if (!finite) atomicOr(g.status, EFE_STATUS_NONFINITE);
   }
@@ -729,7 +731,7 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
       const ff* rf = reinterpret_cast<const ff*>(sr);
       ff acc{0, 0};
       for (int q = 0; q < NQ; ++q) ff_add(acc, rf[(le * NQ + q) * L::SR + k]);
-      pe = -ff_to_double(acc);
+      pe = -ff_to_double_bits(acc);
     } else {
       for (int q = 0; q < NQ; ++q) pe -= sr[(le * NQ + q) * L::SR + k];
     }
@@ -875,39 +877,68 @@ __global__ void __launch_bounds__(NT, MINB) assemble_kernel(GroupArgs g) {
 // Groups of one element type for the persistent pass: group k owns the tiles
 // [tileStart[k], tileStart[k+1]) of its type.  Passed by value (kernel parameters).
 constexpr int MAX_PERSISTENT_GROUPS = EFE_PERSISTENT_MAX_GROUPS;
+// The element types of the persistent pass, heaviest first: index of (shape, rule, form) or -1.
+constexpr int PERSISTENT_NTYPES = 5;
+__host__ __device__ inline int persistent_type_index(int shape, int rule, int form) {
+  if (shape == EFE_HEXA20 && rule == EFE_RULE_3D_3X3X3 && form == TLH) return 0;
+  if (shape == EFE_HEXA20 && rule == EFE_RULE_3D_3X3X3 && form == SS3) return 1;
+  if (shape == EFE_HEXA8 && rule == EFE_RULE_3D_2X2X2 && form == TLH) return 2;
+  if (shape == EFE_HEXA8 && rule == EFE_RULE_3D_2X2X2 && form == SS3) return 3;
+  if (shape == EFE_QUAD8 && rule == EFE_RULE_2D_2X2 && form == TLH) return 4;
+  return -1;
+}
 struct GroupTable {
   GroupArgs g[MAX_PERSISTENT_GROUPS];
   int64_t tileStart[MAX_PERSISTENT_GROUPS + 1];
   int n;
 };
 
-// Persistent form: a grid sized to the resident CTAs pulls tiles of up to MAX_PERSISTENT_GROUPS groups
-// of each of two element types from one work counter (scratch, zeroed before the launch), the
-// heavier type first, until all are done.
-template <int SA, int RA, int FA, int EA, int SB, int RB, int FB, int EB, typename KT, int NT,
-          typename CT = unsigned long long>
-__global__ void __launch_bounds__(NT, 1)
-    assemble_persistent_kernel(GroupTable ta, GroupTable tb, CT* counter) {
+// One element type of the persistent pass: shape, quadrature rule, form and elements per tile.
+template <int SHAPE_, int RULE_, int FORM_, int EPB_>
+struct PersistentType {
+  static constexpr int SHAPE = SHAPE_, RULE = RULE_, FORM = FORM_, EPB = EPB_;
+};
+
+// The group tables of every type of one persistent launch (kernel parameters).
+template <int N>
+struct GroupTables {
+  GroupTable t[N];
+};
+
+// Run tile t of the concatenated tile ranges of types I, I+1, ... (in the order of the type list) and
+// return true, or return false when t lies past the last type's tiles.
+template <typename KT, int NT, int N, int I, typename T0, typename... Rest>
+__device__ __forceinline__ bool persistent_tile(const GroupTables<N>& tabs, long long t, unsigned char* smem) {
+  const GroupTable& tb = tabs.t[I];
+  const long long tiles = tb.tileStart[tb.n];
+  if (t < tiles) {
+    int k = 0;
+    while (t >= tb.tileStart[k + 1]) ++k;
+    assemble_tile<T0::SHAPE, T0::RULE, T0::FORM, KT, T0::EPB, NT, false>(tb.g[k],
+                                                                         (int64_t)(t - tb.tileStart[k]) * T0::EPB, smem);
+    return true;
+  }
+  if constexpr (sizeof...(Rest) > 0)
+    return persistent_tile<KT, NT, N, I + 1, Rest...>(tabs, t - tiles, smem);
+  else
+    return false;
+}
+
+// Persistent form: a grid sized to the resident CTAs pulls tiles from one work counter (scratch,
+// zeroed before the launch) over up to MAX_PERSISTENT_GROUPS groups of each element type of the
+// list, the types in list order (the heaviest first), until all are done.  MINB: resident CTAs per SM
+// the register budget is held to.
+template <typename KT, int NT, int MINB, typename CT, typename... Types>
+__global__ void __launch_bounds__(NT, MINB)
+    assemble_persistent_kernel(GroupTables<sizeof...(Types)> tabs, CT* counter) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ long long tile;
-  const long long tilesA = ta.tileStart[ta.n], tilesB = tb.tileStart[tb.n];
   while (true) {
     if (threadIdx.x == 0) tile = (long long)atomicAdd(counter, (CT)1);
     __syncthreads();
     const long long t = tile;
     __syncthreads();
-    if (t < tilesA) {
-      int k = 0;
-      while (t >= ta.tileStart[k + 1]) ++k;
-      assemble_tile<SA, RA, FA, KT, EA, NT, false>(ta.g[k], (int64_t)(t - ta.tileStart[k]) * EA, smem);
-    } else if (t < tilesA + tilesB) {
-      const long long u = t - tilesA;
-      int k = 0;
-      while (u >= tb.tileStart[k + 1]) ++k;
-      assemble_tile<SB, RB, FB, KT, EB, NT, false>(tb.g[k], (int64_t)(u - tb.tileStart[k]) * EB, smem);
-    } else {
-      break;
-    }
+    if (!persistent_tile<KT, NT, (int)sizeof...(Types), 0, Types...>(tabs, t, smem)) break;
     __syncthreads();
   }
 }

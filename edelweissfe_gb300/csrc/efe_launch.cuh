@@ -154,14 +154,17 @@ EFE_BODY_DECL(quad8)
 EFE_BODY_DECL(hexa8)
 EFE_BODY_DECL(hexa20)
 #undef EFE_BODY_DECL
-// the persistent pass over up to MAX_PERSISTENT_GROUPS groups of each of its two element types
-// (heavy: Hexa20 3x3x3 total-Lagrangian Neo-Hooke; light: Quad8 2x2 total-Lagrangian Neo-Hooke)
-cudaError_t persistent_groups(int kprec, const GroupArgs* heavy, int nHeavy, const GroupArgs* light, int nLight,
+// the persistent pass over up to MAX_PERSISTENT_GROUPS groups of each of its element types
+// (groups[k][0 .. nGroups[k]) for type k of persistent_type_index)
+cudaError_t persistent_groups(int kprec, const GroupArgs (*groups)[MAX_PERSISTENT_GROUPS], const int* nGroups,
                               unsigned long long* counter, cudaStream_t st);
 // same pass with the work counter in the library's static scratch array; *needed = tile indices
 // the counter runs through (written before the range check)
-cudaError_t persistent_groups_noalloc(int kprec, const GroupArgs* heavy, int nHeavy, const GroupArgs* light,
-                                      int nLight, int64_t* needed, cudaStream_t st);
+cudaError_t persistent_groups_noalloc(int kprec, const GroupArgs (*groups)[MAX_PERSISTENT_GROUPS], const int* nGroups,
+                                      int64_t* needed, cudaStream_t st);
+// FMA-chain probe of the FP64 / FP32 pipe (efe_probe.cu)
+cudaError_t fma_probe(int fp64, int blocks, int64_t iterations, void* sink, cudaStream_t st);
+int64_t fma_probe_flops(int blocks, int64_t iterations);
 // device linear solve (efe_solve.cu)
 cudaError_t csr_spmv(const EfePcg& s, const double* x, double* y, cudaStream_t st);
 cudaError_t csr_gemv(const EfeCsr& a, const double* x, double alpha, double beta, double* y, cudaStream_t st);

@@ -1,0 +1,106 @@
+// efe_tc.cuh -- 5th-generation tensor-core (tcgen05) building blocks for sm_103a, in inline PTX:
+// tensor-memory (TMEM) allocation, shared-memory matrix descriptors, the single-CTA MMA with FP32
+// accumulators in TMEM, completion through an mbarrier, and the TMEM-to-register load.
+//
+// Operand layout (both operands K-major, no swizzle): the tile is stored in "core matrices" of
+// 8 rows x 16 bytes (8 rows x 4 TF32 values), element (r, k) at byte
+//     (r / 8) * SBO + (k / 4) * LBO + (r % 8) * 16 + (k % 4) * 4,
+// LBO = byte distance between K-neighbouring core matrices, SBO = between 8-row groups.  One MMA
+// consumes K = 8 TF32 values per row (two core matrices along K).
+// Accumulator layout (M = 128, cta_group::1): row i of D is TMEM lane i, column j is TMEM column
+// base + j; warp w of a warpgroup reads lanes [32 (w % 4), 32 (w % 4) + 32).
+#pragma once
+#include <cstdint>
+
+namespace efe {
+namespace tc {
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start address, LBO, SBO (all >> 4), descriptor version 1 (sm_100
+// family), base offset 0, no swizzle
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// instruction descriptor of kind::tf32 with FP32 accumulation, A and B K-major: D format F32 (bits
+// 4-5 = 1), A and B format TF32 (bits 7-9, 10-12 = 2), N >> 3 at bits 17-22, M >> 4 at bits 24-28
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// TMEM allocation of ncols columns (a power of two >= 32) by one full warp; the address is written
+// to *slot (shared memory)
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(slot)), "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// make this thread's shared-memory stores visible to the tensor core (async proxy)
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// wait for the phase with parity `parity` to complete; gives up after `limit` polls (false)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int limit) {
+  uint32_t done = 0;
+  for (int it = 0; it < limit && !done; ++it)
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+  return done != 0;
+}
+
+// D (TMEM) (+)= A (smem, M x 8) * B (smem, N x 8)^T; issued by one thread
+__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         bool accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate ? 1u : 0u)
+      : "memory");
+}
+// arrive on the mbarrier when every MMA issued so far by this thread has completed
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
+               : "memory");
+}
+
+// 8 consecutive 32-bit columns of this thread's TMEM lane (shape 32x32b); waits for the load
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float v[8]) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr)
+               : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// x rounded to TF32 (10 fraction bits, ties away from zero); inf / nan unchanged
+__device__ __forceinline__ float round_tf32(float x) {
+  const uint32_t b = __float_as_uint(x);
+  return (((b >> 23) & 0xffu) == 0xffu) ? x : __uint_as_float((b + 0x1000u) & 0xFFFFE000u);
+}
+// x = hi + lo + O(2^-22 |x|) with hi = tf32(x) and lo = tf32(x - hi): the products hi*hi + hi*lo +
+// lo*hi (exact in the FP32 accumulator) leave ~2^-21 relative per product -- an FP32-grade tangent
+// from three TF32 MMAs
+__device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
+  hi = round_tf32(x);
+  lo = round_tf32(__fsub_rn(x, hi));
+}
+
+}  // namespace tc
+}  // namespace efe

@@ -241,6 +241,12 @@ def make_nist_gpu(NIST, precision="fp64", writeBackState=True, assemblerClass=No
             return self._gpuAssembler.assembleStiffnessCSR(self._gpuK, host=True)
 
         def solveStep(self, step, model, fieldOutputController, outputmanagers):
+            if getattr(model, "constraints", None):
+                # assembleConstraints (nonlinearimplicitstatic.py:851-901) adds the constraints' terms
+                # to the host VIJ matrix, which this subclass does not assemble: the returned GPU
+                # tangent would lack them
+                raise NotImplementedError("NISTGPU: models with constraints are not supported (the GPU tangent "
+                                          "carries element contributions only)")  # fmt: skip
             advance = model.advanceToTime
 
             def advanceToTime(time):

@@ -180,6 +180,8 @@ class NISTGPU:
         self._diag_pos = torch.from_numpy(np.nonzero(ix == rows)[0]).to(dev)
         self.history = []  # one record per attempted increment
         self.linearIterations = []
+        self.linearConverged = []  # per device CG solve: met pcgTolerance (False: stopped at pcgMaxIter)
+        self.linearResiduals = []  # per device CG solve: final |r| / |b| when it stopped at pcgMaxIter
         self.lastK = self.lastU = self.lastP = None
         # called as onAccept(timeStep, U_old, U_new, dU) before each accepted increment's state is
         # committed (the state of the assembler is still the one before the increment)
@@ -411,8 +413,22 @@ class NISTGPU:
                 if not rr <= tol2 and rr == rr and pAp != 0.0:  # not converged, no NaN, no breakdown
                     continue
                 break
-        self.linearIterations.append(k)
+        self._record_linear(k, bnorm, tol2, lambda: float(work[2]))
         return vec[0] + xd
+
+    def _record_linear(self, k, bnorm, tol2, final_rr):
+        """Iterations of one device CG solve, and whether it met its tolerance: a solve that ran into
+        pcgMaxIter gives Newton an inexact correction (the Newton convergence test still decides),
+        so it is recorded in linearConverged / linearResiduals (final |r| / |b|) instead of passing
+        unseen.  final_rr reads the last r.r (one device read, only for solves that hit the limit)."""
+        self.linearIterations.append(k)
+        if k >= self.pcgMaxIter and bnorm > 0.0:
+            rr = final_rr()
+            self.linearConverged.append(bool(rr <= tol2))
+            self.linearResiduals.append(float(np.sqrt(max(rr, 0.0)) / bnorm) if rr == rr else float("nan"))
+        else:
+            self.linearConverged.append(True)
+            self.linearResiduals.append(None)
 
     def _solve_pcg_amg(self, K, R, dir_idx):
         """CG on the same system as _solve_pcg, preconditioned by one aggregation-multigrid V-cycle
@@ -493,7 +509,9 @@ class NISTGPU:
                 if not rr <= tol2 and rr == rr and pApSeen != 0.0:  # not converged, no NaN, no breakdown
                     continue
                 break
-        self.linearIterations.append(k)
+            self._record_linear(k, bnorm, tol2, lambda: float(rrLast))
+        else:
+            self._record_linear(k, bnorm, tol2, lambda: 0.0)
         return x + xd
 
     def _capture_pcg_batch(self, lib, s, k, step):

@@ -225,7 +225,9 @@ int32_t efe_compute_elements_persistent(const EfeWorkItem* items, int32_t nItems
    instead of a caller-provided buffer.  The call makes no cudaMalloc/cudaFree and calls no
    allocating library routine.
    - The first call on a device looks up the array's device address on that device (with it
-     current); make that first call before any stream capture on the device.
+     current); make that first call before any stream capture on the device.  The address is
+     kept for the life of the process: after cudaDeviceReset on a device (a new primary context)
+     this entry point must not be called on that device again.
    - The counter is zeroed by every call, on `stream`, before its launch; status is NOT zeroed
      (the caller zeroes it, as for the other passes).
    - All calls on one device share the array: calls whose launches may overlap on the GPU (other
@@ -311,6 +313,13 @@ int32_t efe_csr_gemv_pairs(const EfeCsr* A, const float* xPairs, double alpha, d
 int32_t efe_chebyshev_step(int64_t n, const double* dinv, const double* r, double c1, double c2, int32_t accumulate,
                            double* d, double* z, float* dPairs, void* stream);
 int32_t efe_split_pairs(int64_t n, const double* x, float* pairs, void* stream);
+
+/* Measurement aid, no counterpart in the reference: FMA throughput of the FP64 (fp64 != 0) or FP32
+   pipe, for the roofline of the element pass, which the FP64 pipe binds on this GPU.  Launches
+   `blocks` CTAs of 256 threads, each thread running 8 independent FMA chains of `iterations`
+   steps; *flops = the FLOPs of the launch (2 per FMA).  sink: one device double (fp64) or float,
+   never written in practice.  The caller times the launch on `stream`. */
+int32_t efe_fma_probe(int32_t fp64, int32_t blocks, int64_t iterations, void* sink, void* stream, int64_t* flops);
 
 /* acceptLastState: stateTemp -> stateRef and auxTemp -> auxRef for every group. */
 int32_t efe_accept_state(const EfeGroup* groups, int32_t nGroups, void* stream);

@@ -8,6 +8,21 @@ def _mesh(nEl, nn):
     return {"conn": np.zeros((nEl, nn), np.int32)}
 
 
+def test_persistent_types():
+    """The element types the persistent kernel takes, in its hand-out order; plane-stress Neo-Hooke
+    (refused by the reference) and other rules / materials are not among them."""
+    from edelweissfe_gb300.batch import persistent_type
+
+    assert persistent_type("C3D20TL", "neohookewa") == 0
+    assert persistent_type("C3D20", "vonmises") == 1 and persistent_type("C3D20", "linearelastic") == 1
+    assert persistent_type("C3D8TL", "neohookewb") == 2
+    assert persistent_type("C3D8", "vonmises") == 3
+    assert persistent_type("CPE8RTL", "neohookewa") == 4
+    assert persistent_type("CPS8RTL", "neohookewa") is None
+    assert persistent_type("C3D8R", "vonmises") is None and persistent_type("C3D8TL", "vonmises") is None
+    assert persistent_type("CPE4", "linearelastic") is None
+
+
 def test_chunks_respect_the_entry_bound():
     from edelweissfe_gb300.batch import chunk_meshes
 

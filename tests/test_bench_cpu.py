@@ -60,6 +60,44 @@ def test_roofline_fraction_is_achieved_over_peak():
 
 
 
+def test_parity_selection_compares_like_with_like():
+    """The at-size check of the headline pass compares the full mesh's P, F and CSR rows only on
+    DOFs whose nodes lie in the oracle's block: with the oracle's own full-mesh pass standing in for
+    the GPU's, every error is exactly zero and the column pattern agrees; a planted error in one
+    state entry of a sample element and in one K entry of a checked row shows up."""
+    import numpy as np
+
+    import bench
+
+    n = 6
+    coords, conn, nodeDof, nDof, dU1, dU2 = bench.workload(n)
+    sel = bench.parity_selection(conn, nodeDof, len(coords), block=72, sample=40)
+    assert len(sel["rows"]) > 0 and len(sel["sample"]) == 40 and sel["sample"].min() >= 72
+    full = bench._oracle_model(coords, conn, nodeDof, nDof, np.arange(len(conn)))
+    st = full.accept_state(full.compute_elements(dU1, dU1, full.initial_state())["stateTemp"])
+    r = full.compute_elements(dU1 + dU2, dU2, st)
+    kpos, _ = bench.csr_row_positions(full.indptr, sel["rows"])
+    sfull = r["stateTemp"][0]["state"]
+    gpu = dict(P=r["P"][sel["rows"]], F=r["F"][sel["rows"]], K=r["Kdata"][kpos], Kcols=full.indices[kpos],
+               st_block=sfull[sel["block"]], st_sample=sfull[sel["sample"]])  # fmt: skip
+    blk = bench._oracle_model(coords, conn, nodeDof, nDof, sel["block"])
+    sb = blk.accept_state(blk.compute_elements(dU1, dU1, blk.initial_state())["stateTemp"])
+    rb = blk.compute_elements(dU1 + dU2, dU2, sb)
+    orc_block = dict(P=rb["P"], F=rb["F"], Kdata=rb["Kdata"], indptr=blk.indptr, indices=blk.indices,
+                     state=rb["stateTemp"][0]["state"])  # fmt: skip
+    # P and F of the block model differ from the full mesh's outside the checked rows
+    assert np.abs(rb["P"] - r["P"]).max() > 1e-6
+    out = bench.oracle_parity(sel, gpu, orc_block, sfull[sel["sample"]])
+    assert out["pattern_bit_exact"]
+    assert out["R"] == 0.0 and out["F"] == 0.0 and out["K"] == 0.0 and out["state"] == 0.0
+    assert set(out["state_per_field"]) == {"stress", "strain", "kappa"}
+    bad = dict(gpu, st_sample=gpu["st_sample"].copy(), K=gpu["K"].copy())
+    bad["st_sample"][3, 2, 12] *= 1 + 1e-9
+    bad["K"][5] *= 1 + 1e-6
+    out = bench.oracle_parity(sel, bad, orc_block, sfull[sel["sample"]])
+    assert out["state_per_field"]["kappa"] > 1e-11 and out["K"] > 1e-10
+
+
 def test_reference_arm_under_torchrun_prints_one_line():
     """Launched as the multi-GPU runs are (torch.distributed.run, two ranks, 127.0.0.1): rank 0
     alone runs the reference arm and prints its line; the other rank exits 0 without work."""

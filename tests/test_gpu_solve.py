@@ -36,6 +36,12 @@ def test_pcg_matches_direct_solve(elType, precision, preconditioner):
     x2 = solver._solve_pcg(K, R, dir_idx)
     assert torch.equal(x1, x2)
     assert 0 < solver.linearIterations[-1] < 2000
+    assert solver.linearConverged[-1] and solver.linearResiduals[-1] is None
+    # a solve cut off by pcgMaxIter says so, with its final relative residual
+    short = NISTGPU(asm, pcgTolerance=1e-14, pcgPreconditioner=preconditioner, pcgMaxIter=10)
+    short._solve_pcg(K, R, dir_idx)
+    assert short.linearIterations == [10] and short.linearConverged == [False]
+    assert 1e-14 < short.linearResiduals[0] < 1.0
     A = sp.csr_matrix((K.double().cpu().numpy(), asm.indices_host, asm.indptr_host), shape=(nDof, nDof))
     free = np.setdiff1d(np.arange(nDof), fixed)
     Rh = R.cpu().numpy()

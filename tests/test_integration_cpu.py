@@ -1,8 +1,8 @@
 """The adapter from reference objects to the GPU path's arrays (edelweissfe_gb300.integration).
 
-Needs the reference source tree (EDELWEISSFE_ROOT, default ../reference next to this repository's
-parent); skipped when it is not present.  No GPU: the extracted arrays are checked against the
-reference's own DofManager and, through the oracle, against the reference's computeElements.
+Needs the reference source tree, named by the EDELWEISSFE_ROOT environment variable; skipped when
+it is unset.  No GPU: the extracted arrays are checked against the reference's own DofManager and,
+through the oracle, against the reference's computeElements.
 """
 
 import os
@@ -11,8 +11,9 @@ import sys
 import numpy as np
 import pytest
 
-REF = os.environ.get("EDELWEISSFE_ROOT", "/root/reference")
-pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "edelweissfe")), reason="reference not present")
+REF = os.environ.get("EDELWEISSFE_ROOT", "")
+pytestmark = pytest.mark.skipif(not REF or not os.path.isdir(os.path.join(REF, "edelweissfe")),
+                                reason="EDELWEISSFE_ROOT (the reference source tree) is not set")  # fmt: skip
 
 
 @pytest.fixture(scope="module")

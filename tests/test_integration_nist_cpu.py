@@ -10,7 +10,8 @@ second step of the von Mises case, read-back, cutback translation -- not the CUD
 reference's own NIST run of the same input: final displacements, every increment's Newton
 iterations, and the field outputs that read the written-back state -- on inputs written here and
 on all 17 edelweiss-provider test inputs of the reference (`testfiles/`).
-Needs the reference source tree; skipped when it is not present.
+Needs the reference source tree, named by the EDELWEISSFE_ROOT environment variable; skipped when
+it is unset.
 """
 
 import os
@@ -21,9 +22,10 @@ from types import SimpleNamespace
 import numpy as np
 import pytest
 
-REF = os.environ.get("EDELWEISSFE_ROOT", "/root/reference")
+REF = os.environ.get("EDELWEISSFE_ROOT", "")
 pytestmark = [
-    pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "edelweissfe")), reason="reference not present"),
+    pytest.mark.skipif(not REF or not os.path.isdir(os.path.join(REF, "edelweissfe")),
+                       reason="EDELWEISSFE_ROOT (the reference source tree) is not set"),  # fmt: skip
     pytest.mark.filterwarnings("ignore::PendingDeprecationWarning"),  # numpy.matrix inside the reference
 ]
 torch = pytest.importorskip("torch")
@@ -311,6 +313,20 @@ def test_cutback_reaches_the_reference_as_its_own_exception(ref):
     with pytest.raises(refexc.CutbackRequest) as e:
         solver.computeElements({}, np.zeros(3), np.zeros(3), np.zeros(3), None, np.zeros(3), None)
     assert e.value.cutbackSize == 0.5 and "element 0" in str(e.value)
+
+
+def test_models_with_constraints_are_refused(ref):
+    """assembleConstraints adds to the host VIJ matrix, which the subclass does not assemble: a model
+    with constraints is refused before the step runs instead of solving with a tangent that lacks them."""
+    from edelweissfe.solvers.nonlinearimplicitstatic import NIST
+
+    from edelweissfe_gb300.integration import make_nist_gpu
+
+    cls = make_nist_gpu(NIST)
+    solver = cls.__new__(cls)
+    model = SimpleNamespace(constraints={"tie": object()}, advanceToTime=lambda t: None)
+    with pytest.raises(NotImplementedError, match="constraints"):
+        solver.solveStep(None, model, None, [])
 
 
 def test_assembler_is_kept_across_steps_and_rebuilt_with_the_state_on_changes(ref):
