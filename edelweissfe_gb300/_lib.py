@@ -19,7 +19,7 @@ EFE_SOLID, EFE_PLANE_STRAIN, EFE_PLANE_STRESS = 0, 1, 2
 EFE_MAT_LINEAR_ELASTIC, EFE_MAT_VON_MISES = 0, 1
 EFE_MAT_NEOHOOKE_WA, EFE_MAT_NEOHOOKE_WB, EFE_MAT_NEOHOOKE_WC = 2, 3, 4
 EFE_K_FP64, EFE_K_FP32, EFE_K_FP32_FF = 0, 1, 2
-EFE_STATUS_CUTBACK, EFE_STATUS_BAD_JACOBIAN, EFE_STATUS_NONFINITE = 1, 2, 4
+EFE_STATUS_CUTBACK, EFE_STATUS_BAD_JACOBIAN, EFE_STATUS_NONFINITE, EFE_STATUS_TC_TIMEOUT, EFE_STATUS_BOUNDS = 1, 2, 4, 8, 16
 EFE_OK, EFE_ERR_ARGUMENT, EFE_ERR_UNSUPPORTED, EFE_ERR_CUDA, EFE_ERR_PATTERN = 0, 1, 2, 3, 4
 
 # every symbol the header declares

@@ -250,6 +250,11 @@ class GPUAssembler:
     def check_status(self):
         """Raise CutbackRequest if a material point failed in the last pass (synchronises)."""
         st = self.status.cpu().numpy()
+        if st[0] & L.EFE_STATUS_TC_TIMEOUT:
+            raise RuntimeError("the tensor-core tangent gave up waiting for its MMAs (tile variant 3): K is incomplete")
+        if st[0] & L.EFE_STATUS_BOUNDS:
+            raise IndexError(f"device bounds check: element {0x7FFFFFFF - int(st[1])} indexes outside a node, DOF "
+                             "or CSR array (the access was skipped; P, F and K of this pass are invalid)")
         if st[0] & L.EFE_STATUS_CUTBACK:
             first = 0x7FFFFFFF - int(st[1])
             raise CutbackRequest(f"material point failed in element {first} ({int(st[2])} points)", 0.5)

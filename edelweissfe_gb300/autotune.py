@@ -9,6 +9,20 @@ import os
 import torch
 
 VARIANTS = (0, 1, 2)
+TENSOR_VARIANT = 3  # the element tangent on the tensor cores (Hexa20 total-Lagrangian Neo-Hooke, FP32 tangent)
+
+
+def variants_for(asm, gi):
+    """Tile variants to time for group gi: the CTA shapes 0-2, and the tensor-core tangent where the
+    library has it (Hexa20 3x3x3 total-Lagrangian with a hyperelastic material and an FP32 tangent)."""
+    from . import _lib as L
+    from .library import element_type
+
+    g = asm.groups[gi]
+    et = element_type(g.elType)
+    tc = (et.shape == L.EFE_HEXA20 and et.rule == L.EFE_RULE_3D_3X3X3 and et.totalLagrangian
+          and g.material.lower().startswith("neohooke") and asm.kPrecision in (L.EFE_K_FP32, L.EFE_K_FP32_FF))  # fmt: skip
+    return VARIANTS + ((TENSOR_VARIANT,) if tc else ())
 
 
 def _key(asm, gi):
@@ -59,7 +73,7 @@ class Autotuner:
                 asm._groups_c[gi].tileVariant = int(self.cache[key]["variant"])
                 continue
             times = {}
-            for v in VARIANTS:
+            for v in variants_for(asm, gi):
                 asm._groups_c[gi].tileVariant = v
 
                 def run():

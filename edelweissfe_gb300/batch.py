@@ -186,6 +186,10 @@ class BatchedPass:
 
     def check_status(self):
         st = self.status.cpu().numpy()
+        if st[0] & L.EFE_STATUS_TC_TIMEOUT:
+            raise RuntimeError("the tensor-core tangent gave up waiting for its MMAs: K is incomplete")
+        if st[0] & L.EFE_STATUS_BOUNDS:
+            raise IndexError("device bounds check: an element indexes outside a node, DOF or CSR array")
         if st[0] & L.EFE_STATUS_CUTBACK:
             from .exceptions import CutbackRequest
 

@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -139,6 +140,16 @@ int32_t check_group(const EfeMesh* mesh, const EfeGroup& g) {
   return EFE_OK;
 }
 
+// Device-side bounds checks of the element pass (EFE_STATUS_BOUNDS): on when the environment has
+// EFE_DEVICE_CHECKS set to a non-zero integer, read once per process.
+int32_t device_checks() {
+  static const int32_t on = [] {
+    const char* v = std::getenv("EFE_DEVICE_CHECKS");
+    return (v && std::atoi(v) != 0) ? 1 : 0;
+  }();
+  return on;
+}
+
 efe::GroupArgs make_args(const EfeMesh* mesh, const EfeGroup& gr, const double* U, const double* dU, void* Kdata,
                          double* P, double* F, int32_t* status) {
   efe::GroupArgs a;
@@ -168,6 +179,10 @@ efe::GroupArgs make_args(const EfeMesh* mesh, const EfeGroup& gr, const double* 
   a.P = P;
   a.F = F;
   a.status = status;
+  a.nnz = mesh->nnz;
+  a.nDof = mesh->nDof;
+  a.nNodes = mesh->nNodes;
+  a.checks = device_checks();
   return a;
 }
 

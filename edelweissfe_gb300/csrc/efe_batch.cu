@@ -1,6 +1,7 @@
 // efe_batch.cu -- persistent launch over several element groups of mixed types (uneven batches of
 // meshes and load cases), and its variant for callers that cannot allocate device memory.
 #include <initializer_list>
+#include <type_traits>
 #include <mutex>
 
 #include "efe_launch.cuh"
@@ -22,18 +23,25 @@ void fill_table(GroupTable& t, const GroupArgs* g, int n, int EPB) {
 
 // The element types of the persistent pass by persistent_type_index, each with its variant-0 tile
 // (128 threads): the (shape, rule, form, elements per tile) and the tile's shared memory.
+// SRC: the persistent_type_index whose groups the type runs.
 template <int IDX, typename KT> struct TypeOf;
-template <int S, int R, int F, typename KT>
+template <int S, int R, int F, typename KT, int SRC_>
 struct TypeOfBase {
   using T = PersistentType<S, R, F, Tile<S, R, F, KT>::EPB>;
   static constexpr size_t bytes = Tile<S, R, F, KT>::bytes;
-  static constexpr int NT = Tile<S, R, F, KT>::NT;
+  static constexpr int NT = Tile<S, R, F, KT>::NT, SRC = SRC_;
 };
-template <typename KT> struct TypeOf<0, KT> : TypeOfBase<EFE_HEXA20, EFE_RULE_3D_3X3X3, TLH, KT> {};
-template <typename KT> struct TypeOf<1, KT> : TypeOfBase<EFE_HEXA20, EFE_RULE_3D_3X3X3, SS3, KT> {};
-template <typename KT> struct TypeOf<2, KT> : TypeOfBase<EFE_HEXA8, EFE_RULE_3D_2X2X2, TLH, KT> {};
-template <typename KT> struct TypeOf<3, KT> : TypeOfBase<EFE_HEXA8, EFE_RULE_3D_2X2X2, SS3, KT> {};
-template <typename KT> struct TypeOf<4, KT> : TypeOfBase<EFE_QUAD8, EFE_RULE_2D_2X2, TLH, KT> {};
+template <typename KT> struct TypeOf<0, KT> : TypeOfBase<EFE_HEXA20, EFE_RULE_3D_3X3X3, TLH, KT, 0> {};
+template <typename KT> struct TypeOf<1, KT> : TypeOfBase<EFE_HEXA20, EFE_RULE_3D_3X3X3, SS3, KT, 1> {};
+template <typename KT> struct TypeOf<2, KT> : TypeOfBase<EFE_HEXA8, EFE_RULE_3D_2X2X2, TLH, KT, 2> {};
+template <typename KT> struct TypeOf<3, KT> : TypeOfBase<EFE_HEXA8, EFE_RULE_3D_2X2X2, SS3, KT, 3> {};
+template <typename KT> struct TypeOf<4, KT> : TypeOfBase<EFE_QUAD8, EFE_RULE_2D_2X2, TLH, KT, 4> {};
+// type 0 with its tangent on the tensor cores (tile variant 3; FP32 tangent only)
+template <> struct TypeOf<5, float> {
+  using T = PersistentType<EFE_HEXA20, EFE_RULE_3D_3X3X3, TLH, 1, true>;
+  static constexpr size_t bytes = Layout<EFE_HEXA20, EFE_RULE_3D_3X3X3, TLH, float, 1, true>::bytes;
+  static constexpr int NT = 128, SRC = 0;
+};
 
 constexpr size_t max_of(std::initializer_list<size_t> v) {
   size_t m = 0;
@@ -47,7 +55,7 @@ template <typename KT, typename CT, int MINB, int... IDX>
 cudaError_t run_list(const GroupArgs (*groups)[MAX_PERSISTENT_GROUPS], const int* nGroups, CT* counter,
                      int64_t maxTiles, int64_t* needed, cudaStream_t st) {
   constexpr int N = sizeof...(IDX);
-  constexpr int idx[N] = {IDX...};
+  constexpr int idx[N] = {TypeOf<IDX, KT>::SRC...};
   constexpr int epb[N] = {TypeOf<IDX, KT>::T::EPB...};
   constexpr int NT = 128;
   static_assert(((TypeOf<IDX, KT>::NT == NT) && ...), "all tiles of a persistent kernel use 128 threads");
@@ -79,8 +87,9 @@ cudaError_t run_list(const GroupArgs (*groups)[MAX_PERSISTENT_GROUPS], const int
 }
 
 // The smallest instantiated type list covering the types present: total-Lagrangian Neo-Hooke Hexa20
-// + Quad8 (batches of uneven 2D/3D meshes), Hexa8 small strain alone (load cases of one material,
-// four CTAs per SM as tile variant 2), or all five types.
+// + Quad8 (batches of uneven 2D/3D meshes; with the FP32 tangent and every Hexa20 group on tile
+// variant 3, the Hexa20 tangent on the tensor cores), Hexa8 small strain alone (load cases of one
+// material, four CTAs per SM as tile variant 2), or all five types.
 template <typename KT, typename CT>
 cudaError_t run_groups(const GroupArgs (*groups)[MAX_PERSISTENT_GROUPS], const int* nGroups, CT* counter,
                        int64_t maxTiles, int64_t* needed, cudaStream_t st) {
@@ -89,8 +98,15 @@ cudaError_t run_groups(const GroupArgs (*groups)[MAX_PERSISTENT_GROUPS], const i
     if (nGroups[k] < 0 || nGroups[k] > MAX_PERSISTENT_GROUPS) return cudaErrorInvalidValue;
     if (nGroups[k] > 0) present |= 1u << k;
   }
-  if ((present & ~((1u << 0) | (1u << 4))) == 0)
+  if ((present & ~((1u << 0) | (1u << 4))) == 0) {
+    if constexpr (std::is_same<KT, float>::value) {
+      // the Hexa20 groups' tangent on the tensor cores when the tile choice says so for all of them
+      bool tc = nGroups[0] > 0;
+      for (int k = 0; k < nGroups[0]; ++k) tc = tc && groups[0][k].tileVariant == 3;
+      if (tc) return run_list<KT, CT, 2, 5, 4>(groups, nGroups, counter, maxTiles, needed, st);
+    }
     return run_list<KT, CT, 1, 0, 4>(groups, nGroups, counter, maxTiles, needed, st);
+  }
   if ((present & ~(1u << 3)) == 0) return run_list<KT, CT, 4, 3>(groups, nGroups, counter, maxTiles, needed, st);
   return run_list<KT, CT, 2, 0, 1, 2, 3, 4>(groups, nGroups, counter, maxTiles, needed, st);
 }

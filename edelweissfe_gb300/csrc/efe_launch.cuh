@@ -41,8 +41,38 @@ cudaError_t launch_assemble_variant(const GroupArgs& g, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// the tensor-core tangent (tile variant 3) exists for the Hexa20 3x3x3 total-Lagrangian Neo-Hooke form
+// with an FP32 tangent
+template <int SHAPE, int RULE, int FORM, typename KT>
+constexpr bool has_tc_variant() {
+  return SHAPE == EFE_HEXA20 && RULE == EFE_RULE_3D_3X3X3 && FORM == TLH && std::is_same<KT, float>::value;
+}
+
+template <int SHAPE, int RULE, int FORM, bool FF>
+cudaError_t launch_assemble_tc(const GroupArgs& g, cudaStream_t st) {
+  constexpr int NT = 128;
+  constexpr size_t bytes = Layout<SHAPE, RULE, FORM, float, 1, true>::bytes;
+  static_assert(bytes <= 110 * 1024, "two tensor-core tiles must fit in one SM");
+  auto kern = assemble_kernel_tc<SHAPE, RULE, FORM, NT, FF>;
+  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (err != cudaSuccess) return err;
+  int dev = 0, sms = 0, perSM = 0;
+  if ((err = cudaGetDevice(&dev)) != cudaSuccess) return err;
+  if ((err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return err;
+  if ((err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, NT, bytes)) != cudaSuccess) return err;
+  if (perSM < 1) return cudaErrorInvalidConfiguration;
+  int64_t grid = (int64_t)sms * perSM;
+  if (grid > g.nElements) grid = g.nElements;
+  if (grid == 0) return cudaSuccess;
+  kern<<<(unsigned)grid, NT, bytes, st>>>(g);
+  return cudaGetLastError();
+}
+
 template <int SHAPE, int RULE, int FORM, typename KT, bool FF = false>
 cudaError_t launch_assemble(const GroupArgs& g, cudaStream_t st) {
+  if constexpr (has_tc_variant<SHAPE, RULE, FORM, KT>()) {
+    if (g.tileVariant == 3) return launch_assemble_tc<SHAPE, RULE, FORM, FF>(g, st);
+  }
   if (g.tileVariant == 1) return launch_assemble_variant<SHAPE, RULE, FORM, KT, FF, 1>(g, st);
   if constexpr (Tile<SHAPE, RULE, FORM, KT, 2>::MINB != Tile<SHAPE, RULE, FORM, KT, 0>::MINB) {
     if (g.tileVariant == 2) return launch_assemble_variant<SHAPE, RULE, FORM, KT, FF, 2>(g, st);

@@ -85,7 +85,14 @@ enum {
 enum {
   EFE_STATUS_CUTBACK = 1,      /* a material point asked for a cutback (CutbackRequest(.., 0.5)) */
   EFE_STATUS_BAD_JACOBIAN = 2, /* det J <= 0 or not finite at set-up                               */
-  EFE_STATUS_NONFINITE = 4     /* a non-finite stress was produced                                 */
+  EFE_STATUS_NONFINITE = 4,    /* a non-finite stress was produced                                 */
+  EFE_STATUS_TC_TIMEOUT = 8,   /* the tensor-core tangent (tile variant 3) gave up waiting for its
+                                  MMAs; K of the pass is incomplete (an internal error)           */
+  EFE_STATUS_BOUNDS = 16       /* debug checks (environment EFE_DEVICE_CHECKS=1, read once per
+                                  process): a connectivity node outside [0, nNodes), a node DOF
+                                  outside the DOF vector, or a pair slot + block offset outside
+                                  [0, nnz) in the element pass; the access was skipped, the
+                                  pass's outputs are invalid                                     */
 };
 /* error codes */
 enum {
@@ -130,7 +137,11 @@ typedef struct EfeGroup {
   double* auxTemp;           /* TL only: Green-Lagrange strain of this call                  */
   int32_t tileVariant;       /* CTA shape of the element pass: 0 = 128 threads, 3 CTAs/SM;
                                 1 = 256 threads, larger tiles; 2 = as 0 with 4 CTAs/SM where
-                                shared memory allows (chosen by the autotuner)                */
+                                shared memory allows; 3 = the element tangent on the tensor
+                                cores (tcgen05, TF32 hi/lo split, FP32 accumulation in TMEM) for
+                                Hexa20 3x3x3 total-Lagrangian Neo-Hooke with an FP32 tangent
+                                (EFE_K_FP32 / EFE_K_FP32_FF), otherwise as 0 (chosen by the
+                                autotuner)                                                     */
 } EfeGroup;
 
 /* One (mesh, group) pair of a persistent launch, with its own DOF vectors and CSR data. */
