@@ -436,7 +436,8 @@ struct PersistentItems {
 int32_t persistent_items(const EfeWorkItem* items, int32_t nItems, int32_t kPrecision, int32_t* status,
                          PersistentItems& out) {
   if (!items || nItems < 1 || !status) return fail(EFE_ERR_ARGUMENT, "work items and a status word expected");
-  if (kPrecision != EFE_K_FP64 && kPrecision != EFE_K_FP32) return fail(EFE_ERR_ARGUMENT, "unknown K precision");
+  if (kPrecision != EFE_K_FP64 && kPrecision != EFE_K_FP32 && kPrecision != EFE_K_FP32_FF)
+    return fail(EFE_ERR_ARGUMENT, "unknown K precision");
   for (int32_t i = 0; i < nItems; ++i) {
     const EfeWorkItem& it = items[i];
     if (!it.mesh || !it.group || !it.P || !it.F || (!it.Kdata && it.mesh->nnz > 0))
@@ -446,6 +447,9 @@ int32_t persistent_items(const EfeWorkItem* items, int32_t nItems, int32_t kPrec
     rc = check_item_buffers(*it.group, it.U, it.dU);
     if (rc) return rc;
     const EfeGroup& g = *it.group;
+    // every type of the persistent kernels has a float-float form (small strain 3D, TL Neo-Hooke)
+    if (kPrecision == EFE_K_FP32_FF && g.nElements > 0 && (!g.geomG32 || !g.geomGlo))
+      return fail(EFE_ERR_ARGUMENT, "EFE_K_FP32_FF needs geomG32 and geomGlo");
     const int type = efe::persistent_type_index(g.shape, g.rule, form_of(g));
     if (type < 0)
       return fail(EFE_ERR_UNSUPPORTED,

@@ -130,7 +130,7 @@ template <int SHAPE, int RULE, bool FF>
 __global__ void __launch_bounds__(SSAdjointTile<SHAPE, RULE>::NT) adjoint_ss_kernel(SSAdjointArgs a) {
   using T = SSAdjointTile<SHAPE, RULE>;
   constexpr int DIM = T::DIM, NN = T::NN, NQ = T::NQ, NDOF = T::NDOF, EPB = T::EPB, NT = T::NT;
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(128) unsigned char smem[];
   double* su = reinterpret_cast<double*>(smem + T::u_off);
   double* sp = reinterpret_cast<double*>(smem + T::p_off);
   double* sr = reinterpret_cast<double*>(smem + T::r_off);

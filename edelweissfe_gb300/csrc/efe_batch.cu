@@ -36,10 +36,11 @@ template <typename KT> struct TypeOf<1, KT> : TypeOfBase<EFE_HEXA20, EFE_RULE_3D
 template <typename KT> struct TypeOf<2, KT> : TypeOfBase<EFE_HEXA8, EFE_RULE_3D_2X2X2, TLH, KT, 2> {};
 template <typename KT> struct TypeOf<3, KT> : TypeOfBase<EFE_HEXA8, EFE_RULE_3D_2X2X2, SS3, KT, 3> {};
 template <typename KT> struct TypeOf<4, KT> : TypeOfBase<EFE_QUAD8, EFE_RULE_2D_2X2, TLH, KT, 4> {};
-// type 0 with its tangent on the tensor cores (tile variant 3; FP32 tangent only)
+// type 0 with its tangent on the tensor cores (tile variant 3, efe_tl20_tc.cuh; FP32 tangent only)
 template <> struct TypeOf<5, float> {
   using T = PersistentType<EFE_HEXA20, EFE_RULE_3D_3X3X3, TLH, 1, true>;
-  static constexpr size_t bytes = Layout<EFE_HEXA20, EFE_RULE_3D_3X3X3, TLH, float, 1, true>::bytes;
+  static constexpr size_t bytes = TL20Layout<false>::bytes;
+  static_assert(TL20Layout<false>::bytes == TL20Layout<true>::bytes, "one tile size for both forms");
   static constexpr int NT = 128, SRC = 0;
 };
 
@@ -51,7 +52,7 @@ constexpr size_t max_of(std::initializer_list<size_t> v) {
 
 // One persistent kernel over the types IDX... (in that order; every other type must have no groups),
 // with registers held to MINB resident CTAs per SM.
-template <typename KT, typename CT, int MINB, int... IDX>
+template <typename KT, bool FF, typename CT, int MINB, int... IDX>
 cudaError_t run_list(const GroupArgs (*groups)[MAX_PERSISTENT_GROUPS], const int* nGroups, CT* counter,
                      int64_t maxTiles, int64_t* needed, cudaStream_t st) {
   constexpr int N = sizeof...(IDX);
@@ -61,13 +62,21 @@ cudaError_t run_list(const GroupArgs (*groups)[MAX_PERSISTENT_GROUPS], const int
   static_assert(((TypeOf<IDX, KT>::NT == NT) && ...), "all tiles of a persistent kernel use 128 threads");
   constexpr size_t bytes = max_of({TypeOf<IDX, KT>::bytes...});
   static_assert(bytes <= 200 * 1024, "persistent tile does not fit in shared memory");
-  auto kern = assemble_persistent_kernel<KT, NT, MINB, CT, typename TypeOf<IDX, KT>::T...>;
+  auto kern = assemble_persistent_kernel<KT, NT, MINB, FF, CT, typename TypeOf<IDX, KT>::T...>;
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (err != cudaSuccess) return err;
+  // the largest shared-memory partition, so that the grid is sized to every CTA that fits an SM
+  err = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
   if (err != cudaSuccess) return err;
   int dev = 0, sms = 0, perSM = 0;
   if ((err = cudaGetDevice(&dev)) != cudaSuccess) return err;
   if ((err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return err;
-  if ((err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, NT, bytes)) != cudaSuccess) return err;
+  // a list with a tensor-core type allocates TMEM (the runtime's occupancy query then answers 1)
+  if constexpr ((TypeOf<IDX, KT>::T::TC || ...)) {
+    if ((err = resident_ctas_tmem(kern, NT, bytes, (int)TL20::TMEM_COLS, &perSM)) != cudaSuccess) return err;
+  } else {
+    if ((err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, NT, bytes)) != cudaSuccess) return err;
+  }
   if (perSM < 1) return cudaErrorInvalidConfiguration;
   GroupTables<N> tabs;
   int64_t tiles = 0;
@@ -82,7 +91,7 @@ cudaError_t run_list(const GroupArgs (*groups)[MAX_PERSISTENT_GROUPS], const int
   if (tiles + grid > maxTiles) return cudaErrorInvalidValue;
   if ((err = cudaMemsetAsync(counter, 0, sizeof(CT), st)) != cudaSuccess) return err;
   if (grid == 0) return cudaSuccess;
-  kern<<<(unsigned)grid, NT, bytes, st>>>(tabs, counter);
+  kern<<<(unsigned)grid, NT, bytes, st>>>(tabs, counter, sms);
   return cudaGetLastError();
 }
 
@@ -90,7 +99,7 @@ cudaError_t run_list(const GroupArgs (*groups)[MAX_PERSISTENT_GROUPS], const int
 // + Quad8 (batches of uneven 2D/3D meshes; with the FP32 tangent and every Hexa20 group on tile
 // variant 3, the Hexa20 tangent on the tensor cores), Hexa8 small strain alone (load cases of one
 // material, four CTAs per SM as tile variant 2), or all five types.
-template <typename KT, typename CT>
+template <typename KT, bool FF, typename CT>
 cudaError_t run_groups(const GroupArgs (*groups)[MAX_PERSISTENT_GROUPS], const int* nGroups, CT* counter,
                        int64_t maxTiles, int64_t* needed, cudaStream_t st) {
   unsigned present = 0;
@@ -103,19 +112,20 @@ cudaError_t run_groups(const GroupArgs (*groups)[MAX_PERSISTENT_GROUPS], const i
       // the Hexa20 groups' tangent on the tensor cores when the tile choice says so for all of them
       bool tc = nGroups[0] > 0;
       for (int k = 0; k < nGroups[0]; ++k) tc = tc && groups[0][k].tileVariant == 3;
-      if (tc) return run_list<KT, CT, 2, 5, 4>(groups, nGroups, counter, maxTiles, needed, st);
+      if (tc) return run_list<KT, FF, CT, 3, 5, 4>(groups, nGroups, counter, maxTiles, needed, st);
     }
-    return run_list<KT, CT, 1, 0, 4>(groups, nGroups, counter, maxTiles, needed, st);
+    return run_list<KT, FF, CT, 1, 0, 4>(groups, nGroups, counter, maxTiles, needed, st);
   }
-  if ((present & ~(1u << 3)) == 0) return run_list<KT, CT, 4, 3>(groups, nGroups, counter, maxTiles, needed, st);
-  return run_list<KT, CT, 2, 0, 1, 2, 3, 4>(groups, nGroups, counter, maxTiles, needed, st);
+  if ((present & ~(1u << 3)) == 0) return run_list<KT, FF, CT, 4, 3>(groups, nGroups, counter, maxTiles, needed, st);
+  return run_list<KT, FF, CT, 2, 0, 1, 2, 3, 4>(groups, nGroups, counter, maxTiles, needed, st);
 }
 
 template <typename CT>
 cudaError_t persistent_groups_t(int kprec, const GroupArgs (*groups)[MAX_PERSISTENT_GROUPS], const int* nGroups,
                                 CT* counter, int64_t maxTiles, int64_t* needed, cudaStream_t st) {
-  if (kprec == EFE_K_FP32) return run_groups<float>(groups, nGroups, counter, maxTiles, needed, st);
-  return run_groups<double>(groups, nGroups, counter, maxTiles, needed, st);
+  if (kprec == EFE_K_FP32) return run_groups<float, false>(groups, nGroups, counter, maxTiles, needed, st);
+  if (kprec == EFE_K_FP32_FF) return run_groups<float, true>(groups, nGroups, counter, maxTiles, needed, st);
+  return run_groups<double, false>(groups, nGroups, counter, maxTiles, needed, st);
 }
 
 }  // namespace

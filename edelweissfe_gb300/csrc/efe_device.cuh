@@ -558,51 +558,70 @@ struct NeoHookeOut {
   double Bm[3][3];
   double c1, c2, c3, c4, energy;
 };
-__device__ inline void neo_hooke(int material, double mu, double K, const double F[3][3], NeoHookeOut& o) {
-  double B[3][3];
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) B[i][j] = F[i][0] * F[j][0] + F[i][1] * F[j][1] + F[i][2] * F[j][2];
-  const double J = det3(F);
-  double I1 = B[0][0] + B[1][1] + B[2][2];
-  double sB, sI;  // tau = sB * B + sI * I
+// The scalar part of the three variants: tau = sB B + sI I, the tangent coefficients c1-c4 and the
+// energy, from J = det F, I1 = tr B and tr F (the energy of c uses tr F as I1, c.py:141).  The
+// first Piola-Kirchhoff stress follows without a 3x3 product: tau F^-T = sB F + sI F^-T, since
+// B F^-T = F.  Variant b forms J^(-2/3) as rcbrt(J)^2 and 1/J^2 once (one reciprocal instead of
+// pow and four divisions).
+struct NeoHookeScalars {
+  double sB, sI, c1, c2, c3, c4, energy;
+};
+__device__ inline NeoHookeScalars neo_hooke_scalars(int material, double mu, double K, double J, double I1,
+                                                    double trF) {
+  NeoHookeScalars o;
   if (material == EFE_MAT_NEOHOOKE_WA) {
     const double lambdaBar = (K - 2.0 / 3.0 * mu) * (J * J - J) - mu;
     const double muBar = (K - 2.0 / 3.0 * mu) * (2.0 * J * J - J);
-    sB = mu;
-    sI = lambdaBar;
+    o.sB = mu;
+    o.sI = lambdaBar;
     o.c1 = mu;
     o.c2 = muBar;
     o.c3 = 0.0;
     o.c4 = 0.0;
     o.energy = mu / 2.0 * (I1 - 3.0) + (K / 2.0 - mu / 3.0) * (J - 1.0) * (J - 1.0) - mu * log(J);
   } else if (material == EFE_MAT_NEOHOOKE_WB) {
-    const double J23 = pow(J, 2.0 / 3.0);
-    const double lambdaHat = K / 2.0 * (J * J + 1.0 / (J * J));
-    const double muBar = mu / (3.0 * J23);
-    const double lambdaBar = K / 4.0 * (J * J - 1.0 / (J * J)) - muBar * I1;
-    sB = mu / J23;
-    sI = lambdaBar;
+    const double r = rcbrt(J);
+    // J^(-2/3); NaN for an inverted point, like pow(J, 2/3) of a negative J
+    const double rJ23 = J < 0.0 ? __longlong_as_double(0x7ff8000000000000ll) : r * r;
+    const double J2 = J * J, rJ2 = 1.0 / J2;  // J^2, J^-2
+    const double lambdaHat = K / 2.0 * (J2 + rJ2);
+    const double muBar = mu * rJ23 / 3.0;
+    const double lambdaBar = K / 4.0 * (J2 - rJ2) - muBar * I1;
+    o.sB = mu * rJ23;
+    o.sI = lambdaBar;
     o.c1 = 3.0 * muBar;
     o.c2 = lambdaHat + 2.0 / 3.0 * I1 * muBar;
     o.c3 = -2.0 * muBar;
     o.c4 = -2.0 * muBar;
-    o.energy = mu / 2.0 * (I1 / J23 - 3.0) + K / 8.0 * (J * J + 1.0 / (J * J) - 2.0);
-  } else {  // EFE_MAT_NEOHOOKE_WC; its energy uses trace(F) as I1 (c.py:141)
+    o.energy = mu / 2.0 * (I1 * rJ23 - 3.0) + K / 8.0 * (J2 + rJ2 - 2.0);
+  } else {  // EFE_MAT_NEOHOOKE_WC
     const double p = pow(J, 2.0 / 3.0 - K / mu);
     const double muBar = mu * p;
     const double lambdaBar = (K / mu - 2.0 / 3.0) * muBar;
-    sB = mu;
-    sI = -muBar;
+    o.sB = mu;
+    o.sI = -muBar;
     o.c1 = mu;
     o.c2 = lambdaBar;
     o.c3 = 0.0;
     o.c4 = 0.0;
-    const double trF = F[0][0] + F[1][1] + F[2][2];
     o.energy = mu / 2.0 * (trF - 3.0) + 3.0 * mu * mu / (3.0 * K - 2.0 * mu) * (p - 1.0);
   }
+  return o;
+}
+__device__ inline void neo_hooke(int material, double mu, double K, const double F[3][3], NeoHookeOut& o) {
+  double B[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = i; j < 3; ++j) B[i][j] = B[j][i] = F[i][0] * F[j][0] + F[i][1] * F[j][1] + F[i][2] * F[j][2];
+  const NeoHookeScalars n =
+      neo_hooke_scalars(material, mu, K, det3(F), B[0][0] + B[1][1] + B[2][2], F[0][0] + F[1][1] + F[2][2]);
+  o.c1 = n.c1;
+  o.c2 = n.c2;
+  o.c3 = n.c3;
+  o.c4 = n.c4;
+  o.energy = n.energy;
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) {
-      o.tau[i][j] = sB * B[i][j] + (i == j ? sI : 0.0);
+      o.tau[i][j] = n.sB * B[i][j] + (i == j ? n.sI : 0.0);
       o.Bm[i][j] = B[i][j];
     }
 }

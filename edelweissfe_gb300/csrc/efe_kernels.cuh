@@ -167,34 +167,16 @@ template <int DIM> struct FormInfo<TLH, DIM> { static constexpr int NVEC = 5, NS
 template <int DIM> struct FormInfo<TLV3, DIM> { static constexpr int NVEC = 4, NSCAL = 9; };
 template <int DIM> struct FormInfo<TLV2, DIM> { static constexpr int NVEC = 2, NSCAL = 10; };
 
-// Operand tiles of the tensor-core tangent (TC: Hexa20 total-Lagrangian Neo-Hooke, efe_tlh_tc.cuh):
-// per chunk of 8 quadrature points (24 K-values), A = W with 184 stored rows (23 groups of 8) and
-// B = dN/dX with 32 rows, each as TF32 hi and lo parts; 8-row groups of 24 values = 768 bytes.
-// The second M-half MMA reads A rows 128-255: rows 184-255 lie past the stored rows (in A_lo, the
-// B tiles and the slack behind them), inside the allocation; their results are never read.
-struct TCTiles {
-  static constexpr int KC = 24, SBO = KC * 4 * 8, LBO = 128;
-  static constexpr int A_GROUPS = 23, B_GROUPS = 4;
-  static constexpr size_t a_bytes = (size_t)A_GROUPS * SBO, b_bytes = (size_t)B_GROUPS * SBO;
-  static constexpr size_t a_hi = 0, a_lo = a_hi + a_bytes, b_hi = a_lo + a_bytes, b_lo = b_hi + b_bytes;
-  static constexpr size_t slack = (32 - A_GROUPS) * (size_t)SBO - 2 * b_bytes;  // read past b_lo by the A_lo M-half
-  static constexpr size_t bytes = b_lo + b_bytes + slack;
-};
-
-template <int SHAPE, int RULE, int FORM, typename KT, int EPB, bool TC = false>
+template <int SHAPE, int RULE, int FORM, typename KT, int EPB>
 struct Layout {
   static constexpr int DIM = ShapeInfo<SHAPE>::DIM, NN = ShapeInfo<SHAPE>::NN, NQ = RuleInfo<RULE>::NQ;
-  static constexpr bool TCT = TC && FORM == TLH;
-  // per-node tangent vectors of a point; the tensor-core tangent of the TL Neo-Hooke form needs
-  // G, h, g, p (not q)
-  static constexpr int NVEC = TCT ? 4 : FormInfo<FORM, DIM>::NVEC, NSCAL = FormInfo<FORM, DIM>::NSCAL;
+  static constexpr int NVEC = FormInfo<FORM, DIM>::NVEC, NSCAL = FormInfo<FORM, DIM>::NSCAL;
   static constexpr int NDOF = NN * DIM;
   // total-Lagrangian Neo-Hooke: per-point record between its sub-phases (F, F^-1, tau, B, c1-c3, s)
-  // in FP64 and a copy of F, B, c1 s, c2 s, c3 s (+ F^-1, M = (c2 s I + c3 s B) F^-T, c4 s for the
-  // tensor-core tangent) in the tangent's precision
+  // in FP64 and a copy of F, B, c1 s, c2 s, c3 s in the tangent's precision
   // Per-point strides of the shared arrays are odd (in their element size): consecutive threads
   // handle consecutive points, so an even stride would put several of them on one memory bank.
-  static constexpr int NX = FORM == TLH ? 41 : 0, NXK = FORM == TLH ? (TCT ? 41 : 25) : 0;
+  static constexpr int NX = FORM == TLH ? 41 : 0, NXK = FORM == TLH ? 25 : 0;
   static constexpr int SR = (NN * DIM) | 1;                                           // doubles per point of r
   static constexpr int SC = FormInfo<FORM, DIM>::NSCAL | 1;                           // KT per point of sc
   static constexpr int SV = (NN * NVEC * DIM) | 1;                                    // KT per point of v
@@ -207,8 +189,7 @@ struct Layout {
   static constexpr size_t xk_off = v_off + sizeof(KT) * EPB * NQ * SV;            // KT [EPB][NQ][NXK]
   static constexpr size_t mc_off = (xk_off + sizeof(KT) * EPB * NQ * NXK + 15) / 16 * 16;  // VMConst [EPB]
   static constexpr size_t rl_off = mc_off + sizeof(VMConst) * EPB;                                     // int [EPB][NN]
-  static constexpr size_t tc_off = (rl_off + sizeof(int) * EPB * NN + 127) / 128 * 128;  // TCTiles (TC only)
-  static constexpr size_t bytes = TCT ? tc_off + TCTiles::bytes : rl_off + sizeof(int) * EPB * NN;
+  static constexpr size_t bytes = rl_off + sizeof(int) * EPB * NN;
 };
 
 template <typename KT>
@@ -216,8 +197,8 @@ __device__ __forceinline__ void kadd(KT* p, KT v) {
   atomicAdd(p, v);
 }
 
-// State of the tensor-core tangent across the tiles of one CTA: the TMEM accumulators (two of 128
-// lanes x 32 FP32 columns: M-halves 0 and 1) and the parity of the mbarrier's next phase.
+// State of the tensor-core tangent across the tiles of one CTA: the base of its TMEM columns and
+// the parity of the MMA-completion mbarrier's next phase.
 struct TCState {
   uint32_t tmem;
   uint32_t phase;
@@ -229,142 +210,14 @@ struct TCState {
 // MMA chunk takes.  On expiry the CTA records EFE_STATUS_TC_TIMEOUT and stops issuing MMAs.
 constexpr int TC_WAIT_LIMIT = 1 << 22;
 
-// K_e of one Hexa20 element in total-Lagrangian Neo-Hooke form on the tensor cores (tcgen05, TF32
-// with a hi/lo split, FP32 accumulation in TMEM), scattered into the CSR data.  With the per-point
-// factors of phase A (F^-1, M = (c2 s I + c3 s B) F^-T, c1 s, c4 s) and per-node vectors G = dN/dX,
-// h = F^-T G, g = F G, p = c1 s g - s tau h, the structured tangent of the SIMT form
-//   K[(a,j),(b,k)] = sum_q p_b,j h_a,k + q_a,j h_b,k + c4 s h_a,j g_b,k + c1 s delta_jk G_a.G_b
-// (displacementtlelement/element.py:408-412 in closed form for Neo-Hooke) is the product
-//   K[(a,j),(b,k)] = sum_{q,l} G_q[a][l] W_q[(j,l),(b,k)],
-//   W_q[(j,l),(b,k)] = F^-1[l][k] p_b,j + M[j][l] h_b,k + c4 s F^-1[l][j] g_b,k + c1 s delta_jk G_b,l,
-// i.e. D[(j,b,k)][a] = sum_kappa A[(j,b,k)][kappa] B[a][kappa] with kappa = (q, l): M = 180 rows in
-// two MMA halves of 128, N = 32 (20 nodes), K = 81 in chunks of 8 points.  Every thread of the CTA
-// calls it (it synchronises the CTA); thread 0 issues the MMAs.
-template <int NT, bool FF, typename L>
-__device__ __forceinline__ void tangent_tc(const GroupArgs& g, int64_t e, unsigned char* smem, TCState& tcs) {
-  constexpr int NN = 20, NQ = 27, DIM = 3;
-  const float* sv = reinterpret_cast<const float*>(smem + L::v_off);
-  const float* sxk = reinterpret_cast<const float*>(smem + L::xk_off);
-  const float* ssc = reinterpret_cast<const float*>(smem + L::sc_off);
-  const int* srl = reinterpret_cast<const int*>(smem + L::rl_off);
-  unsigned char* tb = smem + L::tc_off;
-  uint64_t* mbar = tcs.mbar;
-  constexpr uint32_t idesc = tc::idesc_tf32(128, 32);
-  // byte offset of element (row, kappa) in a TCTiles operand
-  auto off = [](int r, int k) {
-    return (r >> 3) * TCTiles::SBO + (k >> 2) * TCTiles::LBO + (r & 7) * 16 + (k & 3) * 4;
-  };
-  auto put = [&](size_t hiBase, size_t loBase, int r, int k, float x) {
-    float hi, lo;
-    tc::split_tf32(x, hi, lo);
-    *reinterpret_cast<float*>(tb + hiBase + off(r, k)) = hi;
-    *reinterpret_cast<float*>(tb + loBase + off(r, k)) = lo;
-  };
-  for (int q0 = 0; q0 < NQ; q0 += 8) {
-    const int P = NQ - q0 < 8 ? NQ - q0 : 8;  // points of this chunk
-    const int nks = (3 * P + 7) / 8;          // K-steps of 8
-    // A = W: one thread per (point, node b, component k), the 3 x 3 values (j, l)
-    for (int t = threadIdx.x; t < P * NN * DIM; t += NT) {
-      const int pl = t / (NN * DIM), bk = t % (NN * DIM), b = bk / DIM, k = bk % DIM;
-      const int q = q0 + pl;
-      const float* rk = sxk + q * L::NXK;
-      const float* Fi = rk + 21;  // F^-1[l][m] at 3 l + m
-      const float* Mm = rk + 30;  // M[j][l] at 3 j + l
-      const float c1s = ssc[q * L::SC + 0], c4s = rk[39];
-      const float* v = sv + (size_t)q * L::SV + b * L::NVEC * DIM;  // G, h, g, p of node b
-#pragma unroll
-      for (int j = 0; j < 3; ++j)
-#pragma unroll
-        for (int l = 0; l < 3; ++l) {
-          float w = Fi[3 * l + k] * v[9 + j] + Mm[3 * j + l] * v[3 + k] + c4s * Fi[3 * l + j] * v[6 + k];
-          if (j == k) w += c1s * v[l];
-          put(TCTiles::a_hi, TCTiles::a_lo, j * 60 + bk, pl * 3 + l, w);
-        }
-    }
-    // B = G: one thread per (point, node a, component l)
-    for (int t = threadIdx.x; t < P * NN * DIM; t += NT) {
-      const int pl = t / (NN * DIM), al = t % (NN * DIM), a = al / DIM, l = al % DIM;
-      put(TCTiles::b_hi, TCTiles::b_lo, a, pl * 3 + l, sv[(size_t)(q0 + pl) * L::SV + a * L::NVEC * DIM + l]);
-    }
-    // zero the K padding of the last chunk in both operands
-    for (int t = threadIdx.x; t < (8 * nks - 3 * P) * 184; t += NT) {
-      const int k = 3 * P + t / 184, r = t % 184;
-      put(TCTiles::a_hi, TCTiles::a_lo, r, k, 0.0f);
-      if (r < NN) put(TCTiles::b_hi, TCTiles::b_lo, r, k, 0.0f);
-    }
-    tc::fence_proxy_async();
-    __syncthreads();
-    if (threadIdx.x == 0 && !tcs.failed) {
-      tc::fence_after_sync();
-      const uint32_t base = tc::smem_addr(tb);
-      for (int s = 0; s < nks; ++s) {
-        const uint64_t bh = tc::smem_desc(base + TCTiles::b_hi + s * 256, TCTiles::LBO, TCTiles::SBO);
-        const uint64_t bl = tc::smem_desc(base + TCTiles::b_lo + s * 256, TCTiles::LBO, TCTiles::SBO);
-        for (int half = 0; half < 2; ++half) {
-          const uint32_t rowOff = half * 16 * TCTiles::SBO + s * 256;
-          const uint64_t ah = tc::smem_desc(base + TCTiles::a_hi + rowOff, TCTiles::LBO, TCTiles::SBO);
-          const uint64_t al = tc::smem_desc(base + TCTiles::a_lo + rowOff, TCTiles::LBO, TCTiles::SBO);
-          const uint32_t d = tcs.tmem + half * 32;
-          tc::mma_tf32(d, ah, bh, idesc, q0 > 0 || s > 0);
-          tc::mma_tf32(d, ah, bl, idesc, true);
-          tc::mma_tf32(d, al, bh, idesc, true);
-        }
-      }
-      tc::mma_commit(mbar);
-    }
-    // the operand tiles are reused by the next chunk: wait for the MMAs that read them (the phase
-    // parity advances only with a completed phase, so after a time-out tcs.phase is the one still
-    // outstanding)
-    if (!tcs.failed) {
-      if (tc::mbar_wait(mbar, tcs.phase, TC_WAIT_LIMIT)) {
-        tcs.phase ^= 1u;
-      } else {
-        tcs.failed = true;
-        atomicOr(g.status, EFE_STATUS_TC_TIMEOUT);
-      }
-    }
-    tcs.failed = __syncthreads_or(tcs.failed);
-  }
-  tc::fence_after_sync();
-  // read back: thread t holds rows t (half 0) and 128 + t (half 1) of D, columns a = 0 .. 19
-  const int w = threadIdx.x >> 5;
-  for (int half = 0; half < 2; ++half) {
-    const int m = half * 128 + (int)threadIdx.x;
-    float d[24];
-    const uint32_t ta = tcs.tmem + ((uint32_t)(w * 32) << 16) + half * 32;
-    tc::tmem_ld8(ta, d);
-    tc::tmem_ld8(ta + 8, d + 8);
-    tc::tmem_ld8(ta + 16, d + 16);
-    if (m < 180 && !tcs.failed) {
-      const int j = m / 60, b = (m % 60) / 3, k = m % 3;
-      float* K = reinterpret_cast<float*>(g.Kdata);
-      const int rl = srl[b];
-      // K[(a,j),(b,k)] -> CSR (row = dof(b,k), col = dof(a,j)) = slot(a,b) + k * rowLen(b) + j
-      for (int a = 0; a < NN; ++a) {
-        const int32_t slot = g.pairSlot[(e * NN + a) * NN + b];
-        if (!in_bounds(g, slot + (int64_t)k * rl + j, g.nnz, e)) continue;
-        kadd(K + slot + (int64_t)k * rl + j, d[a]);
-      }
-    }
-  }
-  tc::fence_before_sync();
-  __syncthreads();
-}
-
 // FF: the strain increment and the residual of the small-strain 3D form are formed in float-float
 // arithmetic from the float-float geometry (geomG32 + geomGlo); the return map stays FP64.
 // One tile: the EPB elements starting at e0, processed by the NT threads of the calling CTA
 // (every thread of the CTA must call it: it synchronises the CTA).
-// TC: the tangent of the Hexa20 total-Lagrangian Neo-Hooke form on the tensor cores (tangent_tc;
-// EPB = 1, FP32 tangent, TMEM and mbarrier state in tcs).
-template <int SHAPE, int RULE, int FORM, typename KT, int EPB, int NT, bool FF, bool TC = false>
-__device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t e0, unsigned char* smem,
-                                              TCState* tcs = nullptr) {
-  using L = Layout<SHAPE, RULE, FORM, KT, EPB, TC>;
-  static_assert(!L::TCT || (SHAPE == EFE_HEXA20 && RULE == EFE_RULE_3D_3X3X3 && EPB == 1 &&
-                            std::is_same<KT, float>::value && NT == 128),
-                "the tensor-core tangent covers one Hexa20 3x3x3 element per 128-thread tile, FP32 tangent");
-  constexpr int DIM = L::DIM, NN = L::NN, NQ = L::NQ, NVEC = L::NVEC, NSCAL = L::NSCAL, NDOF = L::NDOF;
+template <int SHAPE, int RULE, int FORM, typename KT, int EPB, int NT, bool FF>
+__device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t e0, unsigned char* smem) {
+  using L = Layout<SHAPE, RULE, FORM, KT, EPB>;
+  constexpr int DIM = L::DIM, NN = L::NN, NQ = L::NQ, NVEC = L::NVEC, NDOF = L::NDOF;
   // the faster return-map arithmetic goes with the FP32 tangent (mixed modes)
   constexpr bool FASTRM = std::is_same<KT, float>::value;
   double* su = reinterpret_cast<double*>(smem + L::u_off);
@@ -520,16 +373,6 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
       reck[18] = c1s;
       reck[19] = to_kt<KT>(o.c2 * s);
       reck[20] = to_kt<KT>(o.c3 * s);
-      if constexpr (L::TCT) {
-        // F^-1, M[j][l] = c2 s F^-1[l][j] + c3 s sum_n B[j][n] F^-1[l][n], c4 s for the tensor-core W
-        for (int i = 0; i < 3; ++i)
-          for (int j = 0; j < 3; ++j) {
-            reck[21 + i * 3 + j] = to_kt<KT>(iF[i][j]);
-            const double bf = o.Bm[i][0] * iF[j][0] + o.Bm[i][1] * iF[j][1] + o.Bm[i][2] * iF[j][2];
-            reck[30 + i * 3 + j] = to_kt<KT>((o.c2 * iF[j][i] + o.c3 * bf) * s);
-          }
-        reck[39] = to_kt<KT>(o.c4 * s);
-      }
       // state write (stateTemp = updated copy of stateRef)
       for (int f = 0; f < 6; ++f) {
         g.stateTemp[(int64_t)f * stride + pt] = sig[f];
@@ -609,7 +452,7 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
         v[1 * DIM + j] = hk[j];
         v[2 * DIM + j] = gg[j];
         v[3 * DIM + j] = c1s * gg[j] - thk[j];
-        if constexpr (!L::TCT) v[4 * DIM + j] = c2s * hk[j] + c3s * bh[j];
+        v[4 * DIM + j] = c2s * hk[j] + c3s * bh[j];
       }
     }
   } else {
@@ -934,11 +777,6 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
   }
 
   // ---- phase B: tangent blocks
-  if constexpr (L::TCT) {
-    // on the tensor cores (phase A's records are complete: the CTA synchronised after phase A)
-    tangent_tc<NT, FF, L>(g, e0, smem, *tcs);
-    return;
-  }
   KT* K = reinterpret_cast<KT*>(g.Kdata);
   // the element tangents are symmetric (K_ab[j][k] = K_ba[k][j]): evaluate the pairs a <= b and
   // scatter each block twice
@@ -1070,16 +908,25 @@ __device__ __forceinline__ void assemble_tile(const GroupArgs& g, const int64_t 
 
 template <int SHAPE, int RULE, int FORM, typename KT, int EPB, int NT, int MINB, bool FF = false>
 __global__ void __launch_bounds__(NT, MINB) assemble_kernel(GroupArgs g) {
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(128) unsigned char smem[];
   assemble_tile<SHAPE, RULE, FORM, KT, EPB, NT, FF>(g, (int64_t)blockIdx.x * EPB, smem);
 }
 
 // Set-up and tear-down of the tensor-core state of a CTA (every thread calls both): the mbarrier
 // of MMA completion, 64 TMEM columns (two 128 x 32 FP32 accumulators) allocated by warp 0; at the
 // end, after a bounded wait for MMAs still in flight if a wait expired, warp 0 frees the columns.
+}  // namespace efe
+
+#include "efe_tl20_tc.cuh"
+
+namespace efe {
+
+// Set-up and tear-down of the tensor-core state of a CTA (every thread calls both): the mbarrier
+// of MMA completion and TL20::TMEM_COLS TMEM columns allocated by warp 0; at the end, after a
+// bounded wait for MMAs still in flight if a wait expired, warp 0 frees the columns.
 __device__ __forceinline__ TCState tc_begin(uint64_t* mbar, uint32_t* slot) {
   if (threadIdx.x == 0) tc::mbar_init(mbar, 1);
-  if (threadIdx.x < 32) tc::tmem_alloc(slot, 64);
+  if (threadIdx.x < 32) tc::tmem_alloc(slot, TL20::TMEM_COLS);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -1089,21 +936,32 @@ __device__ __forceinline__ void tc_end(TCState& tcs) {
   if (tcs.failed) tc::mbar_wait(tcs.mbar, tcs.phase, TC_WAIT_LIMIT);
   tc::fence_before_sync();
   __syncthreads();
-  if (threadIdx.x < 32) tc::tmem_dealloc(tcs.tmem, 64);
+  if (threadIdx.x < 32) tc::tmem_dealloc(tcs.tmem, TL20::TMEM_COLS);
 }
 
-// Tile variant 3, the tensor-core tangent: a grid of resident CTAs (two per SM), one Hexa20 element
-// per tile, tiles strided by the grid; each CTA allocates its 64 TMEM columns once and frees them
-// at the end, after a bounded wait for MMAs still in flight if a wait expired.
-template <int SHAPE, int RULE, int FORM, int NT, bool FF>
-__global__ void __launch_bounds__(NT, 2) assemble_kernel_tc(GroupArgs g) {
-  extern __shared__ __align__(16) unsigned char smem[];
+// Tile variant 3, the Hexa20 total-Lagrangian Neo-Hooke pass with the tensor-core tangent
+// (efe_tl20_tc.cuh): a grid of resident CTAs (sms per wave), one element per tile, tiles strided by
+// the grid; each CTA allocates its TMEM columns once and frees them at the end.  The CTAs of one
+// wave share no SM, so the wave index picks the warp of the per-point update.  Each element's
+// K_e scatter runs during the next element's material update (the last one after the loop).
+template <bool FF>
+__global__ void __launch_bounds__(128, 3) assemble_kernel_tc(GroupArgs g, int sms) {
+  extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t mbar;
   __shared__ uint32_t slot;
   TCState tcs = tc_begin(&mbar, &slot);
-  for (int64_t e = blockIdx.x; e < g.nElements; e += gridDim.x) {
-    assemble_tile<SHAPE, RULE, FORM, float, 1, NT, FF, true>(g, e, smem, &tcs);
+  int rot = (int)(blockIdx.x / (unsigned)sms), par = 0;
+  int64_t prev = TL20_DEFER_NONE;  // the element whose K_e is pending in shared memory
+  for (int64_t e = blockIdx.x; e < g.nElements; e += gridDim.x, ++rot, par ^= 1) {
+    const int64_t next = e + gridDim.x < g.nElements ? e + gridDim.x : -1;
+    assemble_tile_tl20_tc<FF>(g, e, smem, tcs, rot, prev, next, prev >= 0, par);
+    prev = e;
     __syncthreads();
+  }
+  if (prev >= 0 && !tcs.failed) {
+    using L = TL20Layout<FF>;
+    tl20_scatter(g, prev, smem + L::tc_off, reinterpret_cast<const int*>(smem + L::ps_off) + (par ^ 1) * TL20::NN * TL20::NN,
+                 reinterpret_cast<const int*>(smem + L::rl_off) + (par ^ 1) * TL20::NN, threadIdx.x, 128);
   }
   tc_end(tcs);
 }
@@ -1143,20 +1001,23 @@ struct GroupTables {
 
 // Run tile t of the concatenated tile ranges of types I, I+1, ... (in the order of the type list) and
 // return true, or return false when t lies past the last type's tiles.
-template <typename KT, int NT, int N, int I, typename T0, typename... Rest>
+template <typename KT, int NT, bool FF, int N, int I, typename T0, typename... Rest>
 __device__ __forceinline__ bool persistent_tile(const GroupTables<N>& tabs, long long t, unsigned char* smem,
-                                                TCState* tcs) {
+                                                TCState* tcs, int rot) {
   const GroupTable& tb = tabs.t[I];
   const long long tiles = tb.tileStart[tb.n];
   if (t < tiles) {
     int k = 0;
     while (t >= tb.tileStart[k + 1]) ++k;
-    assemble_tile<T0::SHAPE, T0::RULE, T0::FORM, KT, T0::EPB, NT, false, T0::TC>(
-        tb.g[k], (int64_t)(t - tb.tileStart[k]) * T0::EPB, smem, tcs);
+    if constexpr (T0::TC)
+      assemble_tile_tl20_tc<FF>(tb.g[k], (int64_t)(t - tb.tileStart[k]), smem, *tcs, rot, TL20_NOW, -1, false, 0);
+    else
+      assemble_tile<T0::SHAPE, T0::RULE, T0::FORM, KT, T0::EPB, NT, FF>(tb.g[k], (int64_t)(t - tb.tileStart[k]) * T0::EPB,
+                                                                        smem);
     return true;
   }
   if constexpr (sizeof...(Rest) > 0)
-    return persistent_tile<KT, NT, N, I + 1, Rest...>(tabs, t - tiles, smem, tcs);
+    return persistent_tile<KT, NT, FF, N, I + 1, Rest...>(tabs, t - tiles, smem, tcs, rot);
   else
     return false;
 }
@@ -1164,11 +1025,11 @@ __device__ __forceinline__ bool persistent_tile(const GroupTables<N>& tabs, long
 // Persistent form: a grid sized to the resident CTAs pulls tiles from one work counter (scratch,
 // zeroed before the launch) over up to MAX_PERSISTENT_GROUPS groups of each element type of the
 // list, the types in list order (the heaviest first), until all are done.  MINB: resident CTAs per SM
-// the register budget is held to.
-template <typename KT, int NT, int MINB, typename CT, typename... Types>
+// the register budget is held to.  FF: the float-float forms (mixed-ff) of the types that have one.
+template <typename KT, int NT, int MINB, bool FF, typename CT, typename... Types>
 __global__ void __launch_bounds__(NT, MINB)
-    assemble_persistent_kernel(GroupTables<sizeof...(Types)> tabs, CT* counter) {
-  extern __shared__ __align__(16) unsigned char smem[];
+    assemble_persistent_kernel(GroupTables<sizeof...(Types)> tabs, CT* counter, int sms) {
+  extern __shared__ __align__(128) unsigned char smem[];
   __shared__ long long tile;
   constexpr bool anyTC = (Types::TC || ...);
   __shared__ uint64_t mbar;
@@ -1180,7 +1041,9 @@ __global__ void __launch_bounds__(NT, MINB)
     __syncthreads();
     const long long t = tile;
     __syncthreads();
-    if (!persistent_tile<KT, NT, (int)sizeof...(Types), 0, Types...>(tabs, t, smem, &tcs)) break;
+    if (!persistent_tile<KT, NT, FF, (int)sizeof...(Types), 0, Types...>(tabs, t, smem, &tcs,
+                                                                         (int)(blockIdx.x / (unsigned)sms + t)))
+      break;
     __syncthreads();
   }
   if constexpr (anyTC) tc_end(tcs);

@@ -1,5 +1,7 @@
 // efe_launch.cuh -- tile sizing and launch of the kernels of one element shape.
 #pragma once
+#include <algorithm>
+
 #include "efe_kernels.cuh"
 
 namespace efe {
@@ -48,30 +50,59 @@ constexpr bool has_tc_variant() {
   return SHAPE == EFE_HEXA20 && RULE == EFE_RULE_3D_3X3X3 && FORM == TLH && std::is_same<KT, float>::value;
 }
 
-template <int SHAPE, int RULE, int FORM, bool FF>
+// Resident CTAs per SM of a kernel that allocates tmemCols TMEM columns per CTA, from its registers
+// (allocated per thread in units of 8), its shared memory (plus the per-CTA reservation), its threads
+// and the SM's 512 TMEM columns.  The runtime's occupancy query answers 1 for kernels that allocate
+// TMEM whatever their size; the CTAs beyond what actually fits only wait for an SM (none waits on
+// another, and tcgen05.alloc waits for free columns), so an estimate that is too high costs nothing.
+template <typename K>
+cudaError_t resident_ctas_tmem(K kern, int nt, size_t dynBytes, int tmemCols, int* perSM) {
+  cudaFuncAttributes fa;
+  cudaError_t err = cudaFuncGetAttributes(&fa, kern);
+  if (err != cudaSuccess) return err;
+  int dev = 0, regsSM = 0, smemSM = 0, reserved = 0, threadsSM = 0;
+  if ((err = cudaGetDevice(&dev)) != cudaSuccess) return err;
+  if ((err = cudaDeviceGetAttribute(&regsSM, cudaDevAttrMaxRegistersPerMultiprocessor, dev)) != cudaSuccess) return err;
+  if ((err = cudaDeviceGetAttribute(&smemSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess) return err;
+  if ((err = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev)) != cudaSuccess) return err;
+  if ((err = cudaDeviceGetAttribute(&threadsSM, cudaDevAttrMaxThreadsPerMultiProcessor, dev)) != cudaSuccess) return err;
+  const int regs = (fa.numRegs + 7) / 8 * 8;
+  int n = regsSM / (regs * nt);
+  const long long perCta = (long long)dynBytes + (long long)fa.sharedSizeBytes + reserved;
+  n = std::min<long long>(n, smemSM / perCta);
+  n = std::min(n, threadsSM / nt);
+  n = std::min(n, 512 / tmemCols);
+  *perSM = n;
+  return n >= 1 ? cudaSuccess : cudaErrorInvalidConfiguration;
+}
+
+template <bool FF>
 cudaError_t launch_assemble_tc(const GroupArgs& g, cudaStream_t st) {
   constexpr int NT = 128;
-  constexpr size_t bytes = Layout<SHAPE, RULE, FORM, float, 1, true>::bytes;
-  static_assert(bytes <= 110 * 1024, "two tensor-core tiles must fit in one SM");
-  auto kern = assemble_kernel_tc<SHAPE, RULE, FORM, NT, FF>;
+  constexpr size_t bytes = TL20Layout<FF>::bytes;
+  static_assert(bytes <= 74 * 1024, "three tensor-core tiles must fit in one SM");
+  auto kern = assemble_kernel_tc<FF>;
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (err != cudaSuccess) return err;
+  // the largest shared-memory partition: without it the occupancy query (and the launch) assume the
+  // default split and fit one CTA per SM
+  err = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
   if (err != cudaSuccess) return err;
   int dev = 0, sms = 0, perSM = 0;
   if ((err = cudaGetDevice(&dev)) != cudaSuccess) return err;
   if ((err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return err;
-  if ((err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, NT, bytes)) != cudaSuccess) return err;
-  if (perSM < 1) return cudaErrorInvalidConfiguration;
+  if ((err = resident_ctas_tmem(kern, NT, bytes, (int)TL20::TMEM_COLS, &perSM)) != cudaSuccess) return err;
   int64_t grid = (int64_t)sms * perSM;
   if (grid > g.nElements) grid = g.nElements;
   if (grid == 0) return cudaSuccess;
-  kern<<<(unsigned)grid, NT, bytes, st>>>(g);
+  kern<<<(unsigned)grid, NT, bytes, st>>>(g, sms);
   return cudaGetLastError();
 }
 
 template <int SHAPE, int RULE, int FORM, typename KT, bool FF = false>
 cudaError_t launch_assemble(const GroupArgs& g, cudaStream_t st) {
   if constexpr (has_tc_variant<SHAPE, RULE, FORM, KT>()) {
-    if (g.tileVariant == 3) return launch_assemble_tc<SHAPE, RULE, FORM, FF>(g, st);
+    if (g.tileVariant == 3 || g.tileVariant == 4) return launch_assemble_tc<FF>(g, st);
   }
   if (g.tileVariant == 1) return launch_assemble_variant<SHAPE, RULE, FORM, KT, FF, 1>(g, st);
   if constexpr (Tile<SHAPE, RULE, FORM, KT, 2>::MINB != Tile<SHAPE, RULE, FORM, KT, 0>::MINB) {

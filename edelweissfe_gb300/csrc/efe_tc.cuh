@@ -77,29 +77,30 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
                : "memory");
 }
 
-// 8 consecutive 32-bit columns of this thread's TMEM lane (shape 32x32b); waits for the load
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float v[8]) {
-  uint32_t r[8];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr)
-               : "memory");
+// 16 consecutive 32-bit columns of this thread's TMEM lane (shape 32x32b); waits for the load
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
-// x rounded to TF32 (10 fraction bits, ties away from zero); inf / nan unchanged
-__device__ __forceinline__ float round_tf32(float x) {
-  const uint32_t b = __float_as_uint(x);
-  return (((b >> 23) & 0xffu) == 0xffu) ? x : __uint_as_float((b + 0x1000u) & 0xFFFFE000u);
+// asynchronous global -> shared copies of 4 or 8 bytes (cp.async, L1-cached), and the wait for all
+// copies this thread issued
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
 }
-// x = hi + lo + O(2^-22 |x|) with hi = tf32(x) and lo = tf32(x - hi): the products hi*hi + hi*lo +
-// lo*hi (exact in the FP32 accumulator) leave ~2^-21 relative per product -- an FP32-grade tangent
-// from three TF32 MMAs
-__device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
-  hi = round_tf32(x);
-  lo = round_tf32(__fsub_rn(x, hi));
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n cp.async.wait_group 0;" ::: "memory");
 }
 
 }  // namespace tc

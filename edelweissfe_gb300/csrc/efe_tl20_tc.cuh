@@ -1,0 +1,462 @@
+// efe_tl20_tc.cuh -- the Hexa20 3x3x3 total-Lagrangian Neo-Hooke element pass with its element
+// tangent on the tensor cores (tile variant 3): one element per 128-thread CTA tile.
+//
+// The tangent of the TL Neo-Hooke form (displacementtlelement/element.py:408-412 in closed form) is,
+// with per-point scalars c1s..c4s and per-node vectors G = dN/dX, h = F^-T G, g = F G,
+// p = c1s g - s tau h, q = c2s h + c3s B h,
+//   K[(a,j),(b,k)] = sum_q  q_a[j] h_b[k] + c4s h_a[j] g_b[k]        (plain: j with a, k with b)
+//                         + p_b[j] h_a[k]                            (swapped: j with b, k with a)
+//                         + delta_jk c1s G_a . G_b                   (node-pair diagonal)
+// Each of the three kinds is a plain matrix product over K = (point, factor) of per-node vectors:
+//   P[(a,j),(b,k)] = sum_q [q_a[j], c4s h_a[j]] . [h_b[k], g_b[k]]       (60 x 60, K = 2 per point)
+//   X[(b,j),(a,k)] = sum_q p_b[j] h_a[k]                                 (60 x 60, K = 1 per point)
+//   D[a,b]         = sum_q sum_l (c1s G_a[l]) G_b[l]                     (20 x 20, K = 3 per point)
+// and K[(a,j),(b,k)] = P[(a,j),(b,k)] + X[(b,j),(a,k)] + delta_jk D[a,b].
+// P and X share their B operand [h | g] and run as ONE M = 128 MMA (rows 0-59 plain, rows 64-123
+// swapped; the swapped rows' g-slots are zero), D as a second one.  The per-node vectors are the
+// operands themselves: phase A2 writes them (TF32 hi/lo split, ~2^-22 per product with the
+// hi*hi + hi*lo + lo*hi MMAs, FP32 accumulation in TMEM) straight into the operand tiles, in three
+// chunks of 9 points; no element stiffness block is formed on the SIMT pipes.
+//
+// The element residual uses the first Piola-Kirchhoff form P_e[a][j] = -sum_q (s tau F^-T)_q[j] . G_qa
+// (:402, :414), one thread per (node, component), in FP64 (mixed) or float-float (mixed-ff); F is
+// formed as in the SIMT pass.  The element's dN/dX is staged in shared memory once per element.
+#pragma once
+
+namespace efe {
+
+struct TL20 {
+  static constexpr int NN = 20, NQ = 27, NDOF = 60, QC = 9, NCH = 3;
+  static constexpr int RK = 44;  // floats per point of the FP32 record (16-byte rows)
+  // FP32 record offsets: F, F^-1 (row-major, F^-1[l][m] at 3l+m), B = F F^T, Pq = s tau F^-T,
+  // c1 s .. c4 s
+  static constexpr int R_F = 0, R_FI = 9, R_B = 18, R_PQ = 27, R_C = 36;
+  // operand tiles (K-major, no swizzle; element (r, k) at (r/8) SBO + (k/4) 128 + (r%8) 16 + (k%4) 4)
+  static constexpr int KPS = 24;  // P/X operands: K = 2 per point, 18 used per chunk
+  static constexpr int KD = 32;   // D operands: K = 3 per point, 27 used per chunk
+  static constexpr int SBO_PS = KPS / 4 * 128, SBO_D = KD / 4 * 128;
+  // tile byte offsets inside the tensor-core region: the M = 128 read of the D operand covers
+  // 16 row groups (rows 24-127: the following tiles, results never read), its N = 32 read 4
+  static constexpr size_t dA_hi = 0, dA_lo = dA_hi + 3 * SBO_D, dB_hi = dA_lo + 3 * SBO_D,
+                          dB_lo = dB_hi + 3 * SBO_D, a_hi = dB_lo + 3 * SBO_D, a_lo = a_hi + 16 * SBO_PS,
+                          b_hi = a_lo + 16 * SBO_PS, b_lo = b_hi + 8 * SBO_PS, tc_bytes = b_lo + 8 * SBO_PS;
+  static_assert(dA_lo + 16 * SBO_D <= tc_bytes && dB_lo + 4 * SBO_D <= tc_bytes, "D reads stay in the region");
+  // epilogue: the accumulators copied to shared memory over the (then idle) operand tiles
+  static constexpr int SS = NDOF + 1;  // odd row stride
+  static constexpr size_t sP = 0, sX = sP + sizeof(float) * NDOF * SS, sD = sX + sizeof(float) * NDOF * SS;
+  static_assert(sD + sizeof(float) * NN * (NN + 1) <= tc_bytes, "epilogue copy fits the operand tiles");
+  // TMEM columns: P/X accumulator at 0 (64 columns), D at 64 (32 columns)
+  static constexpr uint32_t TMEM_COLS = 128, D_COL = 64;
+};
+
+template <bool FF>
+struct TL20Layout {
+  using T = TL20;
+  static constexpr size_t u_off = 0;                                          // ff or double [NN][3]
+  static constexpr size_t f_off = u_off + 8 * T::NN * 3;                      // double [NQ][9]: F
+  static constexpr size_t pq_off = f_off + 8 * T::NQ * 9;                     // ff or double [NQ][9]: s tau F^-T
+  static constexpr size_t rk_off = pq_off + 8 * T::NQ * 9;                    // float [NQ][RK]
+  static_assert(rk_off % 16 == 0 && T::RK % 4 == 0, "16-byte record rows");
+  // the element's dN/dX, [(l NN + a) NQ + q]: float-float hi and lo arrays (mixed-ff) or double
+  // (mixed), staged by cp.async
+  static constexpr size_t g_off = rk_off + sizeof(float) * T::NQ * T::RK;
+  static constexpr size_t glo_off = g_off + sizeof(float) * T::NQ * T::NDOF;
+  // pair slots and row lengths of two consecutive elements (the pending K_e and the current one)
+  static constexpr size_t ps_off = g_off + 8 * T::NQ * T::NDOF;         // int [2][NN][NN]
+  static constexpr size_t rl_off = ps_off + sizeof(int) * 2 * T::NN * T::NN;  // int [2][NN]
+  static constexpr size_t tc_off = (rl_off + sizeof(int) * 2 * T::NN + 127) / 128 * 128;
+  static constexpr size_t bytes = tc_off + T::tc_bytes;
+};
+
+// round to TF32 (10 fraction bits, to nearest with ties away from zero) for a finite FP32 value
+__device__ __forceinline__ float tf32_rna(float x) { return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u); }
+
+// byte offset of element (r, k) in an operand tile with row-group stride SBO
+template <int SBO>
+__device__ __forceinline__ uint32_t tc_off(int r, int k) {
+  return (uint32_t)((r >> 3) * SBO + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4);
+}
+// x at (r, k) of the hi and lo tiles (lo = the TF32 rounding of x - hi)
+template <int SBO>
+__device__ __forceinline__ void tc_put(unsigned char* hi, unsigned char* lo, int r, int k, float x) {
+  const float h = tf32_rna(x);
+  const uint32_t o = tc_off<SBO>(r, k);
+  *reinterpret_cast<float*>(hi + o) = h;
+  *reinterpret_cast<float*>(lo + o) = tf32_rna(__fsub_rn(x, h));
+}
+// x at (r, k) and y at (r, k + 1), k even (one 8-byte store per tile)
+template <int SBO>
+__device__ __forceinline__ void tc_put2(unsigned char* hi, unsigned char* lo, int r, int k, float x, float y) {
+  const float hx = tf32_rna(x), hy = tf32_rna(y);
+  const uint32_t o = tc_off<SBO>(r, k);
+  *reinterpret_cast<float2*>(hi + o) = make_float2(hx, hy);
+  *reinterpret_cast<float2*>(lo + o) = make_float2(tf32_rna(__fsub_rn(x, hx)), tf32_rna(__fsub_rn(y, hy)));
+}
+
+// K_e of element e (the accumulators copied to the tile's shared memory by its epilogue) into the
+// CSR data: Ke[(a,j),(b,k)] at row dof(b,k), column dof(a,j) = slot(a,b) + k rowLen(b) + j, with the
+// element's staged pair slots sps and row lengths srl.  Threads ti = 0 .. nth - 1 take the entries
+// in (b, k)-row order, consecutive threads consecutive columns (a, j) of one CSR row.
+__device__ __forceinline__ void tl20_scatter(const GroupArgs& g, int64_t e, const unsigned char* tb, const int* sps,
+                                             const int* srl, int ti, int nth) {
+  using T = TL20;
+  constexpr int NN = T::NN;
+  const float* sP = reinterpret_cast<const float*>(tb + T::sP);
+  const float* sX = reinterpret_cast<const float*>(tb + T::sX);
+  const float* sD = reinterpret_cast<const float*>(tb + T::sD);
+  float* K = reinterpret_cast<float*>(g.Kdata);
+  for (int t = ti; t < T::NDOF * T::NDOF; t += nth) {
+    const int bk = t / T::NDOF, aj = t - bk * T::NDOF;
+    const int b = bk / 3, k = bk - 3 * b, a = aj / 3, j = aj - 3 * a;
+    float val = sP[aj * T::SS + bk] + sX[(3 * b + j) * T::SS + 3 * a + k];
+    if (j == k) val += sD[a * (NN + 1) + b];
+    const int64_t pos = (int64_t)sps[a * NN + b] + (int64_t)k * srl[b] + j;
+    if (!in_bounds(g, pos, g.nnz, e)) continue;
+    atomicAdd(K + pos, val);
+  }
+}
+
+// Stage element e into shared memory (every thread calls it): dN/dX and the pair slots by
+// cp.async (complete after tc::cp_async_wait_all), U and the row lengths by plain loads (threads
+// with rt < NN).  par: which pair-slot / row-length buffer.
+template <bool FF>
+__device__ __forceinline__ void tl20_stage(const GroupArgs& g, int64_t e, unsigned char* smem, int par, int rt) {
+  using T = TL20;
+  using L = TL20Layout<FF>;
+  constexpr int NT = 128, NN = T::NN, NQ = T::NQ, DIM = 3;
+  const int tid = threadIdx.x;
+  const int64_t stride = g.nElements * NQ;
+  for (int t = tid; t < T::NDOF * NQ; t += NT) {
+    const int la = t / NQ, q = t - la * NQ;
+    const int64_t gi = (int64_t)la * stride + e * NQ + q;
+    if constexpr (FF) {
+      tc::cp_async4(reinterpret_cast<float*>(smem + L::g_off) + t, g.geomG32 + gi);
+      tc::cp_async4(reinterpret_cast<float*>(smem + L::glo_off) + t, g.geomGlo + gi);
+    } else {
+      tc::cp_async8(reinterpret_cast<double*>(smem + L::g_off) + t, g.geomG + gi);
+    }
+  }
+  int* sps = reinterpret_cast<int*>(smem + L::ps_off) + par * NN * NN;
+  for (int t = tid; t < NN * NN; t += NT) tc::cp_async4(sps + t, g.pairSlot + e * NN * NN + t);
+  if (rt < NN) {
+    const int a = rt;
+    const int32_t node = g.conn[e * NN + a];
+    if (in_bounds(g, node, g.nNodes, e)) {
+      reinterpret_cast<int*>(smem + L::rl_off)[par * NN + a] = g.nodeRowLen[node];
+      const int32_t dof = g.nodeDof[node];
+      if (in_bounds(g, dof, g.nDof - DIM + 1, e)) {
+        if constexpr (FF) {
+          // displacement relative to node 0 (sum_a dN_a/dX = 0): no cancellation in F
+          const int32_t node0 = g.conn[e * NN];
+          const int32_t dof0 = in_bounds(g, node0, g.nNodes, e) ? g.nodeDof[node0] : dof;
+          const int32_t d0 = in_bounds(g, dof0, g.nDof - DIM + 1, e) ? dof0 : dof;
+          ff* su = reinterpret_cast<ff*>(smem + L::u_off);
+          for (int c = 0; c < DIM; ++c) su[a * DIM + c] = ff_split_bits(g.U[dof + c] - g.U[d0 + c]);
+        } else {
+          double* su = reinterpret_cast<double*>(smem + L::u_off);
+          for (int c = 0; c < DIM; ++c) su[a * DIM + c] = g.U[dof + c];
+        }
+      }
+    }
+  }
+}
+
+// how a tile call scatters K_e (the prev argument of assemble_tile_tl20_tc)
+constexpr int64_t TL20_DEFER_NONE = -1;  // defer this element's K_e; nothing pending from before
+constexpr int64_t TL20_NOW = -2;         // scatter this element's K_e at the end of the call
+
+// One element e of group g; every thread of the CTA (NT = 128) calls it.  tcs: the CTA's TMEM
+// columns (TL20::TMEM_COLS) and MMA-completion mbarrier.  rot (0-3): the warp that runs the
+// per-point material update; warp w of every CTA sits on the same SM sub-partition, so the caller
+// varies rot between the CTAs that share an SM.  par: the pair-slot buffer of this element
+// (alternate between consecutive calls).
+// prev == TL20_NOW: K_e is scattered at the end of the call.  Otherwise K_e stays pending in shared
+// memory, and prev >= 0 is the previous call's pending element (same group), scattered by the
+// three other warps while one warp runs this element's material update; after the last call the
+// caller scatters the pending one (tl20_scatter).  next >= 0: the element of the next call, staged
+// while this element's last MMAs run; staged: this element was staged that way by the previous call.
+template <bool FF>
+__device__ __forceinline__ void assemble_tile_tl20_tc(const GroupArgs& g, const int64_t e, unsigned char* smem,
+                                                      TCState& tcs, int rot, int64_t prev, int64_t next, bool staged,
+                                                      int par) {
+  using T = TL20;
+  using L = TL20Layout<FF>;
+  constexpr int NT = 128, NN = T::NN, NQ = T::NQ, DIM = 3;
+  const int tid = threadIdx.x;
+  const int rt = (tid - 32 * (rot & 3)) & (NT - 1);  // thread index with warp rot first
+  double* sF = reinterpret_cast<double*>(smem + L::f_off);
+  float* rk = reinterpret_cast<float*>(smem + L::rk_off);
+  // staged dN/dX: FF hi / lo floats, else doubles
+  float* sGh = reinterpret_cast<float*>(smem + L::g_off);
+  float* sGl = reinterpret_cast<float*>(smem + L::glo_off);
+  double* sGd = reinterpret_cast<double*>(smem + L::g_off);
+  int* sps = reinterpret_cast<int*>(smem + L::ps_off);
+  int* srl = reinterpret_cast<int*>(smem + L::rl_off);
+  unsigned char* tb = smem + L::tc_off;
+  const int64_t stride = g.nElements * NQ;
+
+  // ---- phase 0: this element's dN/dX, pair slots, U and row lengths in shared memory
+  if (!staged) tl20_stage<FF>(g, e, smem, par, rt);
+  tc::cp_async_wait_all();
+  __syncthreads();
+
+  // ---- A0: F = I + sum_a U_a (x) dN_a/dX, one thread per (point, component)
+  for (int t = tid; t < NQ * 9; t += NT) {
+    const int c = t / NQ, q = t - c * NQ, i = c / 3, j = c - 3 * i;
+    const int g0 = j * NN * NQ + q;
+    double f = (i == j) ? 1.0 : 0.0;
+    if constexpr (FF) {
+      const ff* uf = reinterpret_cast<const ff*>(smem + L::u_off);
+      ff acc{0, 0};
+      for (int a = 0; a < NN; ++a) ff_fma(acc, uf[a * DIM + i], ff{sGh[g0 + a * NQ], sGl[g0 + a * NQ]});
+      f += ff_to_double_bits(acc);
+    } else {
+      const double* u = reinterpret_cast<const double*>(smem + L::u_off);
+      double h = 0.0;
+      for (int a = 0; a < NN; ++a) h += u[a * DIM + i] * sGd[g0 + a * NQ];
+      f += h;
+    }
+    sF[q * 9 + i * 3 + j] = f;
+  }
+  __syncthreads();
+
+  // ---- A1: one thread per point of warp rot: E, F^-1, Kirchhoff stress and tangent scalars
+  // (FP64), state, the FP32 record of the tangent and s tau F^-T for the residual; meanwhile the
+  // other warps scatter the pending K_e of the previous element
+  if (rt < 32) {
+    if (rt < NQ) {
+      const int q = rt;
+      const int64_t pt = e * NQ + q;
+      const double* props = g.props + e * g.nProps;
+      double F[3][3];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) F[i][j] = sF[q * 9 + i * 3 + j];
+      // Green-Lagrange E = 1/2 (H + H^T + H^T H), H = F - I  (:386), symmetric
+      const double H[3][3] = {{F[0][0] - 1.0, F[0][1], F[0][2]}, {F[1][0], F[1][1] - 1.0, F[1][2]},
+                              {F[2][0], F[2][1], F[2][2] - 1.0}};
+      double Eg[3][3];
+      for (int i = 0; i < 3; ++i)
+        for (int j = i; j < 3; ++j)
+          Eg[i][j] = Eg[j][i] = 0.5 * ((H[i][j] + H[j][i]) + (H[0][i] * H[0][j] + H[1][i] * H[1][j] + H[2][i] * H[2][j]));
+      const double Ev[6] = {Eg[0][0], Eg[1][1], Eg[2][2], Eg[0][1], Eg[1][2], Eg[0][2]};
+      for (int f = 0; f < 6; ++f) g.auxTemp[(int64_t)f * stride + pt] = Ev[f];
+      // F^-1 from the cofactors, det F from the same cofactors
+      double iF[3][3];
+      iF[0][0] = F[1][1] * F[2][2] - F[1][2] * F[2][1];
+      iF[1][0] = F[1][2] * F[2][0] - F[1][0] * F[2][2];
+      iF[2][0] = F[1][0] * F[2][1] - F[1][1] * F[2][0];
+      const double J = F[0][0] * iF[0][0] + F[0][1] * iF[1][0] + F[0][2] * iF[2][0];
+      iF[0][1] = F[0][2] * F[2][1] - F[0][1] * F[2][2];
+      iF[0][2] = F[0][1] * F[1][2] - F[0][2] * F[1][1];
+      iF[1][1] = F[0][0] * F[2][2] - F[0][2] * F[2][0];
+      iF[1][2] = F[0][2] * F[1][0] - F[0][0] * F[1][2];
+      iF[2][1] = F[0][1] * F[2][0] - F[0][0] * F[2][1];
+      iF[2][2] = F[0][0] * F[1][1] - F[0][1] * F[1][0];
+      const double rJ = 1.0 / J;
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) iF[i][j] *= rJ;
+      double B[3][3];
+      for (int i = 0; i < 3; ++i)
+        for (int j = i; j < 3; ++j) B[i][j] = B[j][i] = F[i][0] * F[j][0] + F[i][1] * F[j][1] + F[i][2] * F[j][2];
+      const NeoHookeScalars o = neo_hooke_scalars(g.material, props[0], props[1], J, B[0][0] + B[1][1] + B[2][2],
+                                                  F[0][0] + F[1][1] + F[2][2]);
+      // Kirchhoff stress tau = sB B + sI I (Voigt 11, 22, 33, 12, 23, 13)
+      const double sig[6] = {o.sB * B[0][0] + o.sI, o.sB * B[1][1] + o.sI, o.sB * B[2][2] + o.sI,
+                             o.sB * B[0][1],        o.sB * B[1][2],        o.sB * B[0][2]};
+      const double eps[6] = {Eg[0][0], Eg[1][1], Eg[2][2], 2.0 * Eg[0][1], 2.0 * Eg[1][2], 2.0 * Eg[0][2]};
+      const double s = g.geomS[pt];
+      // s tau F^-T = (s sB) F + (s sI) F^-T
+      const double aF = s * o.sB, aI = s * o.sI;
+      float* r = rk + q * T::RK;
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          r[T::R_F + i * 3 + j] = d2f_trunc(F[i][j]);
+          r[T::R_FI + i * 3 + j] = d2f_trunc(iF[i][j]);
+          r[T::R_B + i * 3 + j] = d2f_trunc(B[i][j]);
+          const double pq = aF * F[i][j] + aI * iF[j][i];
+          r[T::R_PQ + i * 3 + j] = d2f_trunc(pq);
+          if constexpr (FF)
+            reinterpret_cast<ff*>(smem + L::pq_off)[q * 9 + i * 3 + j] = ff_split_bits(pq);
+          else
+            reinterpret_cast<double*>(smem + L::pq_off)[q * 9 + i * 3 + j] = pq;
+        }
+      r[T::R_C + 0] = d2f_trunc(o.c1 * s);
+      r[T::R_C + 1] = d2f_trunc(o.c2 * s);
+      r[T::R_C + 2] = d2f_trunc(o.c3 * s);
+      r[T::R_C + 3] = d2f_trunc(o.c4 * s);
+      // state write (stateTemp = updated copy of stateRef)
+      for (int f = 0; f < 6; ++f) {
+        g.stateTemp[(int64_t)f * stride + pt] = sig[f];
+        g.stateTemp[(int64_t)(6 + f) * stride + pt] = eps[f];
+      }
+      g.stateTemp[(int64_t)12 * stride + pt] = o.energy;
+      bool finite = true;
+      for (int f = 0; f < 6; ++f) finite = finite && finite_bits(sig[f]);
+      if (!finite) atomicOr(g.status, EFE_STATUS_NONFINITE);
+    }
+  } else if (prev >= 0 && !tcs.failed) {
+    tl20_scatter(g, prev, tb, sps + (par ^ 1) * NN * NN, srl + (par ^ 1) * NN, rt - 32, NT - 32);
+  }
+  __syncthreads();
+  // zero the operand tiles (padding rows and slots must read as zero)
+  for (int i = tid; i < (int)(T::tc_bytes / 16); i += NT) reinterpret_cast<float4*>(tb)[i] = make_float4(0, 0, 0, 0);
+  __syncthreads();
+
+  // ---- per chunk of 9 points: operands (A2) and the residual of the chunk's points, MMAs
+  // residual threads: warps 2 and 3 (they have one A2 task each, warps 0 and 1 two); node ra,
+  // component rj, one accumulator per component of dN/dX
+  const int ri = tid - 64, ra = ri / 3, rj = ri - 3 * ra;
+  double pe[3] = {0.0, 0.0, 0.0};
+  ff pef[3] = {{0, 0}, {0, 0}, {0, 0}};
+  const uint32_t base = tc::smem_addr(tb);
+  for (int ch = 0; ch < T::NCH; ++ch) {
+    // A2: one thread per (point, node)
+    for (int t = tid; t < T::QC * NN; t += NT) {
+      const int ql = t / NN, a = t - ql * NN, q = ch * T::QC + ql;
+      // the point's record, 40 floats in ten 16-byte loads (the rows are 16-byte aligned)
+      float r[40];
+#pragma unroll
+      for (int i = 0; i < 10; ++i) {
+        const float4 v = reinterpret_cast<const float4*>(rk + q * T::RK)[i];
+        r[4 * i] = v.x;
+        r[4 * i + 1] = v.y;
+        r[4 * i + 2] = v.z;
+        r[4 * i + 3] = v.w;
+      }
+      float G[3];
+      for (int l = 0; l < 3; ++l) {
+        if constexpr (FF)
+          G[l] = sGh[(l * NN + a) * NQ + q];
+        else
+          G[l] = d2f_trunc(sGd[(l * NN + a) * NQ + q]);
+      }
+      float h[3], gg[3], th[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        h[i] = r[T::R_FI + 0 * 3 + i] * G[0] + r[T::R_FI + 1 * 3 + i] * G[1] + r[T::R_FI + 2 * 3 + i] * G[2];
+        gg[i] = r[T::R_F + i * 3 + 0] * G[0] + r[T::R_F + i * 3 + 1] * G[1] + r[T::R_F + i * 3 + 2] * G[2];
+        th[i] = r[T::R_PQ + i * 3 + 0] * G[0] + r[T::R_PQ + i * 3 + 1] * G[1] + r[T::R_PQ + i * 3 + 2] * G[2];
+      }
+      const float c1s = r[T::R_C + 0], c2s = r[T::R_C + 1], c3s = r[T::R_C + 2], c4s = r[T::R_C + 3];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const float bh = r[T::R_B + j * 3 + 0] * h[0] + r[T::R_B + j * 3 + 1] * h[1] + r[T::R_B + j * 3 + 2] * h[2];
+        const int row = 3 * a + j;
+        tc_put2<T::SBO_PS>(tb + T::a_hi, tb + T::a_lo, row, 2 * ql, c2s * h[j] + c3s * bh, c4s * h[j]);
+        tc_put<T::SBO_PS>(tb + T::a_hi, tb + T::a_lo, 64 + row, 2 * ql, c1s * gg[j] - th[j]);
+        tc_put2<T::SBO_PS>(tb + T::b_hi, tb + T::b_lo, row, 2 * ql, h[j], gg[j]);
+        tc_put<T::SBO_D>(tb + T::dA_hi, tb + T::dA_lo, a, 3 * ql + j, c1s * G[j]);
+        tc_put<T::SBO_D>(tb + T::dB_hi, tb + T::dB_lo, a, 3 * ql + j, G[j]);
+      }
+    }
+    // residual of the chunk's points: P_e[a][j] -= sum_q sum_l Pq[j][l] G_qa[l]
+    if (ri >= 0 && ri < T::NDOF) {
+      for (int ql = 0; ql < T::QC; ++ql) {
+        const int q = ch * T::QC + ql;
+#pragma unroll
+        for (int l = 0; l < 3; ++l) {
+          const int gi = (l * NN + ra) * NQ + q;
+          if constexpr (FF)
+            ff_fma(pef[l], reinterpret_cast<const ff*>(smem + L::pq_off)[q * 9 + rj * 3 + l], ff{sGh[gi], sGl[gi]});
+          else
+            pe[l] -= reinterpret_cast<const double*>(smem + L::pq_off)[q * 9 + rj * 3 + l] * sGd[gi];
+        }
+      }
+    }
+    tc::fence_proxy_async();
+    __syncthreads();
+    // after the last chunk's operands the staged dN/dX, U and the other pair-slot buffer are dead:
+    // stage the next element while the MMAs run
+    if (ch == T::NCH - 1 && next >= 0) tl20_stage<FF>(g, next, smem, par ^ 1, rt);
+    if (tid == 0 && !tcs.failed) {
+      tc::fence_after_sync();
+      constexpr uint32_t idPS = tc::idesc_tf32(128, 64), idD = tc::idesc_tf32(128, 32);
+      for (int s = 0; s < T::KPS / 8; ++s) {
+        const uint64_t ah = tc::smem_desc(base + T::a_hi + s * 256, 128, T::SBO_PS);
+        const uint64_t al = tc::smem_desc(base + T::a_lo + s * 256, 128, T::SBO_PS);
+        const uint64_t bh = tc::smem_desc(base + T::b_hi + s * 256, 128, T::SBO_PS);
+        const uint64_t bl = tc::smem_desc(base + T::b_lo + s * 256, 128, T::SBO_PS);
+        tc::mma_tf32(tcs.tmem, ah, bh, idPS, ch > 0 || s > 0);
+        tc::mma_tf32(tcs.tmem, ah, bl, idPS, true);
+        tc::mma_tf32(tcs.tmem, al, bh, idPS, true);
+      }
+      for (int s = 0; s < T::KD / 8; ++s) {
+        const uint64_t ah = tc::smem_desc(base + T::dA_hi + s * 256, 128, T::SBO_D);
+        const uint64_t al = tc::smem_desc(base + T::dA_lo + s * 256, 128, T::SBO_D);
+        const uint64_t bh = tc::smem_desc(base + T::dB_hi + s * 256, 128, T::SBO_D);
+        const uint64_t bl = tc::smem_desc(base + T::dB_lo + s * 256, 128, T::SBO_D);
+        tc::mma_tf32(tcs.tmem + T::D_COL, ah, bh, idD, ch > 0 || s > 0);
+        tc::mma_tf32(tcs.tmem + T::D_COL, ah, bl, idD, true);
+        tc::mma_tf32(tcs.tmem + T::D_COL, al, bh, idD, true);
+      }
+      tc::mma_commit(tcs.mbar);
+    }
+    // the operand tiles are rewritten by the next chunk: wait for the MMAs that read them (the
+    // phase parity advances only with a completed phase, so after a time-out tcs.phase is the one
+    // still outstanding)
+    if (!tcs.failed) {
+      if (tc::mbar_wait(tcs.mbar, tcs.phase, TC_WAIT_LIMIT)) {
+        tcs.phase ^= 1u;
+      } else {
+        tcs.failed = true;
+        atomicOr(g.status, EFE_STATUS_TC_TIMEOUT);
+      }
+    }
+    tcs.failed = __syncthreads_or(tcs.failed);
+  }
+  tc::fence_after_sync();
+
+  // ---- epilogue: accumulators -> shared memory (over the operand tiles)
+  {
+    float* sP = reinterpret_cast<float*>(tb + T::sP);
+    float* sX = reinterpret_cast<float*>(tb + T::sX);
+    float* sD = reinterpret_cast<float*>(tb + T::sD);
+    const int w = tid >> 5, lane = tid & 31, row = tid;  // warp w reads TMEM lanes 32w .. 32w+31
+    const uint32_t ta = tcs.tmem + ((uint32_t)(w * 32) << 16);
+    float v[16];
+    for (int c0 = 0; c0 < 64; c0 += 16) {
+      tc::tmem_ld16(ta + c0, v);
+      if (row < T::NDOF) {
+        for (int c = 0; c < 16; ++c)
+          if (c0 + c < T::NDOF) sP[row * T::SS + c0 + c] = v[c];
+      } else if (row >= 64 && row < 64 + T::NDOF) {
+        for (int c = 0; c < 16; ++c)
+          if (c0 + c < T::NDOF) sX[(row - 64) * T::SS + c0 + c] = v[c];
+      }
+    }
+    if (w == 0) {
+      for (int c0 = 0; c0 < 32; c0 += 16) {
+        tc::tmem_ld16(ta + T::D_COL + c0, v);
+        if (lane < NN)
+          for (int c = 0; c < 16; ++c)
+            if (c0 + c < NN) sD[lane * (NN + 1) + c0 + c] = v[c];
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+
+  // ---- residual and flux (NIST.computeElements, nonlinearimplicitstatic.py:837-844)
+  if (ri >= 0 && ri < T::NDOF) {
+    double p;
+    if constexpr (FF) {
+      ff acc = pef[0];
+      ff_add(acc, pef[1]);
+      ff_add(acc, pef[2]);
+      p = -ff_to_double_bits(acc);
+    } else {
+      p = (pe[0] + pe[1]) + pe[2];
+    }
+    const int32_t node = g.conn[e * NN + ra];
+    if (in_bounds(g, node, g.nNodes, e)) {
+      const int32_t dof = g.nodeDof[node] + rj;
+      if (in_bounds(g, dof, g.nDof, e)) {
+        atomicAdd(g.P + dof, p);
+        atomicAdd(g.F + dof, fabs(p));
+      }
+    }
+  }
+  if (prev == TL20_NOW && !tcs.failed) tl20_scatter(g, e, tb, sps + par * NN * NN, srl + par * NN, tid, NT);
+}
+
+}  // namespace efe

@@ -219,9 +219,11 @@ int32_t efe_adjoint_small_strain(const EfeMesh* mesh, const EfeGroup* group, con
    2D meshes and batches of 3D meshes), in ONE persistent launch: the resident CTAs take tiles of all
    groups from the work counter until all are done (same results as efe_compute_elements on each
    item).  workCounter: one device uint64 of scratch, zeroed by this call.  Implemented for up to
-   EFE_PERSISTENT_MAX_GROUPS groups of each of the types Hexa20 3x3x3 and Quad8 2x2, total-Lagrangian
-   Neo-Hooke, in any order, precision EFE_K_FP64 / EFE_K_FP32; other types return
-   EFE_ERR_UNSUPPORTED. */
+   EFE_PERSISTENT_MAX_GROUPS groups of each of the types Hexa20 3x3x3 and Hexa8 2x2x2 total-
+   Lagrangian Neo-Hooke and small-strain von Mises / linear elastic, and Quad8 2x2 total-Lagrangian
+   Neo-Hooke, in any order, precision EFE_K_FP64 / EFE_K_FP32 / EFE_K_FP32_FF (the last needs
+   geomG32 and geomGlo); with an FP32 tangent and tileVariant 3 on every Hexa20 total-Lagrangian
+   group, their tangents run on the tensor cores.  Other types return EFE_ERR_UNSUPPORTED. */
 #define EFE_PERSISTENT_MAX_GROUPS 8
 int32_t efe_compute_elements_persistent(const EfeWorkItem* items, int32_t nItems, int32_t kPrecision,
                                         uint64_t* workCounter, int32_t* status, void* stream);
