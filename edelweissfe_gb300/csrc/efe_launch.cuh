@@ -102,7 +102,7 @@ cudaError_t launch_assemble_tc(const GroupArgs& g, cudaStream_t st) {
 template <int SHAPE, int RULE, int FORM, typename KT, bool FF = false>
 cudaError_t launch_assemble(const GroupArgs& g, cudaStream_t st) {
   if constexpr (has_tc_variant<SHAPE, RULE, FORM, KT>()) {
-    if (g.tileVariant == 3 || g.tileVariant == 4) return launch_assemble_tc<FF>(g, st);
+    if (g.tileVariant == 3) return launch_assemble_tc<FF>(g, st);
   }
   if (g.tileVariant == 1) return launch_assemble_variant<SHAPE, RULE, FORM, KT, FF, 1>(g, st);
   if constexpr (Tile<SHAPE, RULE, FORM, KT, 2>::MINB != Tile<SHAPE, RULE, FORM, KT, 0>::MINB) {

@@ -20,7 +20,14 @@
 //
 // The element residual uses the first Piola-Kirchhoff form P_e[a][j] = -sum_q (s tau F^-T)_q[j] . G_qa
 // (:402, :414), one thread per (node, component), in FP64 (mixed) or float-float (mixed-ff); F is
-// formed as in the SIMT pass.  The element's dN/dX is staged in shared memory once per element.
+// formed as in the SIMT pass.  In the mixed-ff pass the kinematics of a point (E, F^-1, B, tau,
+// s tau F^-T) are float-float on the FP32 pipe, spread over all threads, and only the Neo-Hooke
+// scalars (logarithms, powers) stay FP64 on one warp: on this GPU the FP64 pipe costs the same per
+// warp instruction whatever the number of active lanes, so that warp's instruction count sets the
+// phase's length.
+// Across the elements of a CTA: an element's dN/dX, pair slots and U are staged (cp.async and
+// register loads) while the previous element's last MMAs and material update run, and its K_e
+// scatter runs during the next element's material update.
 #pragma once
 
 namespace efe {
@@ -45,6 +52,18 @@ struct TL20 {
   static constexpr int SS = NDOF + 1;  // odd row stride
   static constexpr size_t sP = 0, sX = sP + sizeof(float) * NDOF * SS, sD = sX + sizeof(float) * NDOF * SS;
   static_assert(sD + sizeof(float) * NN * (NN + 1) <= tc_bytes, "epilogue copy fits the operand tiles");
+  // float-float material phase (mixed-ff): per point E (6), cofactors (9) and B (6) as float-float
+  // (A1a), then the point's scalars (A1b), in the operand region behind the epilogue copy (free
+  // until the operand tiles are zeroed; the pending epilogue copy stays intact)
+  static constexpr int NA1 = 21;
+  struct A1Scalars {
+    ff sB, sI, aF, aI, rJ;
+    double energy;
+    float c[4];
+  };
+  static constexpr size_t a1_off = 32768, a1s_off = a1_off + 8 * NQ * NA1;
+  static_assert(a1_off >= sD + sizeof(float) * NN * (NN + 1) && a1s_off + sizeof(A1Scalars) * NQ <= tc_bytes,
+                "material scratch between the epilogue copy and the end of the operand region");
   // TMEM columns: P/X accumulator at 0 (64 columns), D at 64 (32 columns)
   static constexpr uint32_t TMEM_COLS = 128, D_COL = 64;
 };
@@ -95,8 +114,7 @@ __device__ __forceinline__ void tc_put2(unsigned char* hi, unsigned char* lo, in
 
 // K_e of element e (the accumulators copied to the tile's shared memory by its epilogue) into the
 // CSR data: Ke[(a,j),(b,k)] at row dof(b,k), column dof(a,j) = slot(a,b) + k rowLen(b) + j, with the
-// element's staged pair slots sps and row lengths srl.  Threads ti = 0 .. nth - 1 take the entries
-// in (b, k)-row order, consecutive threads consecutive columns (a, j) of one CSR row.
+// element's staged pair slots sps and row lengths srl, by threads ti = 0 .. nth - 1.
 __device__ __forceinline__ void tl20_scatter(const GroupArgs& g, int64_t e, const unsigned char* tb, const int* sps,
                                              const int* srl, int ti, int nth) {
   using T = TL20;
@@ -105,28 +123,30 @@ __device__ __forceinline__ void tl20_scatter(const GroupArgs& g, int64_t e, cons
   const float* sX = reinterpret_cast<const float*>(tb + T::sX);
   const float* sD = reinterpret_cast<const float*>(tb + T::sD);
   float* K = reinterpret_cast<float*>(g.Kdata);
-  for (int t = ti; t < T::NDOF * T::NDOF; t += nth) {
-    const int bk = t / T::NDOF, aj = t - bk * T::NDOF;
-    const int b = bk / 3, k = bk - 3 * b, a = aj / 3, j = aj - 3 * a;
-    float val = sP[aj * T::SS + bk] + sX[(3 * b + j) * T::SS + 3 * a + k];
-    if (j == k) val += sD[a * (NN + 1) + b];
-    const int64_t pos = (int64_t)sps[a * NN + b] + (int64_t)k * srl[b] + j;
-    if (!in_bounds(g, pos, g.nnz, e)) continue;
-    atomicAdd(K + pos, val);
+  // one thread per (b, k, a): the three contiguous columns j = 0, 1, 2 of node a in CSR row (b, k)
+  for (int t = ti; t < T::NDOF * NN; t += nth) {
+    const int bk = t / NN, a = t - bk * NN, b = bk / 3, k = bk - 3 * b;
+    const int64_t pos = (int64_t)sps[a * NN + b] + (int64_t)k * srl[b];
+    if (!in_bounds(g, pos, g.nnz - 2, e)) continue;
+    const float d = sD[a * (NN + 1) + b];  // on the column j = k
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const float v = sP[(3 * a + j) * T::SS + 3 * b + k] + sX[(3 * b + j) * T::SS + 3 * a + k];
+      atomicAdd(K + pos + j, j == k ? v + d : v);
+    }
   }
 }
 
-// Stage element e into shared memory (every thread calls it): dN/dX and the pair slots by
-// cp.async (complete after tc::cp_async_wait_all), U and the row lengths by plain loads (threads
-// with rt < NN).  par: which pair-slot / row-length buffer.
+// Stage element e into shared memory, in two parts that complete after tc::cp_async_wait_all:
+// tl20_stage_g (every thread): dN/dX by cp.async; tl20_stage_small (threads li = 0 .. nth - 1,
+// nth >= NN): the pair slots by cp.async into buffer par, U and the row lengths by plain loads.
 template <bool FF>
-__device__ __forceinline__ void tl20_stage(const GroupArgs& g, int64_t e, unsigned char* smem, int par, int rt) {
+__device__ __forceinline__ void tl20_stage_g(const GroupArgs& g, int64_t e, unsigned char* smem) {
   using T = TL20;
   using L = TL20Layout<FF>;
-  constexpr int NT = 128, NN = T::NN, NQ = T::NQ, DIM = 3;
-  const int tid = threadIdx.x;
+  constexpr int NT = 128, NQ = T::NQ;
   const int64_t stride = g.nElements * NQ;
-  for (int t = tid; t < T::NDOF * NQ; t += NT) {
+  for (int t = threadIdx.x; t < T::NDOF * NQ; t += NT) {
     const int la = t / NQ, q = t - la * NQ;
     const int64_t gi = (int64_t)la * stride + e * NQ + q;
     if constexpr (FF) {
@@ -136,28 +156,90 @@ __device__ __forceinline__ void tl20_stage(const GroupArgs& g, int64_t e, unsign
       tc::cp_async8(reinterpret_cast<double*>(smem + L::g_off) + t, g.geomG + gi);
     }
   }
+}
+// The small per-element data of tl20_stage_small, loaded into registers first (so that the
+// latency of the dependent loads can overlap other work) and stored later.
+struct TL20Small {
+  int32_t rowLen;
+  double u[3];
+  bool valid;
+};
+template <bool FF>
+__device__ __forceinline__ TL20Small tl20_load_small(const GroupArgs& g, int64_t e, int a) {
+  constexpr int NN = TL20::NN, DIM = 3;
+  TL20Small r{0, {0.0, 0.0, 0.0}, false};
+  const int32_t node = g.conn[e * NN + a];
+  if (!in_bounds(g, node, g.nNodes, e)) return r;
+  r.rowLen = g.nodeRowLen[node];
+  const int32_t dof = g.nodeDof[node];
+  if (!in_bounds(g, dof, g.nDof - DIM + 1, e)) return r;
+  r.valid = true;
+  if constexpr (FF) {
+    // displacement relative to node 0 (sum_a dN_a/dX = 0): no cancellation in F
+    const int32_t node0 = g.conn[e * NN];
+    const int32_t dof0 = in_bounds(g, node0, g.nNodes, e) ? g.nodeDof[node0] : dof;
+    const int32_t d0 = in_bounds(g, dof0, g.nDof - DIM + 1, e) ? dof0 : dof;
+    for (int c = 0; c < DIM; ++c) r.u[c] = g.U[dof + c] - g.U[d0 + c];
+  } else {
+    for (int c = 0; c < DIM; ++c) r.u[c] = g.U[dof + c];
+  }
+  return r;
+}
+template <bool FF>
+__device__ __forceinline__ void tl20_store_small(const TL20Small& r, unsigned char* smem, int par, int a) {
+  using L = TL20Layout<FF>;
+  constexpr int NN = TL20::NN, DIM = 3;
+  reinterpret_cast<int*>(smem + L::rl_off)[par * NN + a] = r.rowLen;
+  if (!r.valid) return;
+  for (int c = 0; c < DIM; ++c) {
+    if constexpr (FF)
+      reinterpret_cast<ff*>(smem + L::u_off)[a * DIM + c] = ff_split_bits(r.u[c]);
+    else
+      reinterpret_cast<double*>(smem + L::u_off)[a * DIM + c] = r.u[c];
+  }
+}
+template <bool FF>
+__device__ __forceinline__ void tl20_stage_small(const GroupArgs& g, int64_t e, unsigned char* smem, int par, int li,
+                                                 int nth) {
+  using L = TL20Layout<FF>;
+  constexpr int NN = TL20::NN;
   int* sps = reinterpret_cast<int*>(smem + L::ps_off) + par * NN * NN;
-  for (int t = tid; t < NN * NN; t += NT) tc::cp_async4(sps + t, g.pairSlot + e * NN * NN + t);
-  if (rt < NN) {
-    const int a = rt;
-    const int32_t node = g.conn[e * NN + a];
-    if (in_bounds(g, node, g.nNodes, e)) {
-      reinterpret_cast<int*>(smem + L::rl_off)[par * NN + a] = g.nodeRowLen[node];
-      const int32_t dof = g.nodeDof[node];
-      if (in_bounds(g, dof, g.nDof - DIM + 1, e)) {
-        if constexpr (FF) {
-          // displacement relative to node 0 (sum_a dN_a/dX = 0): no cancellation in F
-          const int32_t node0 = g.conn[e * NN];
-          const int32_t dof0 = in_bounds(g, node0, g.nNodes, e) ? g.nodeDof[node0] : dof;
-          const int32_t d0 = in_bounds(g, dof0, g.nDof - DIM + 1, e) ? dof0 : dof;
-          ff* su = reinterpret_cast<ff*>(smem + L::u_off);
-          for (int c = 0; c < DIM; ++c) su[a * DIM + c] = ff_split_bits(g.U[dof + c] - g.U[d0 + c]);
-        } else {
-          double* su = reinterpret_cast<double*>(smem + L::u_off);
-          for (int c = 0; c < DIM; ++c) su[a * DIM + c] = g.U[dof + c];
-        }
-      }
-    }
+  for (int t = li; t < NN * NN; t += nth) tc::cp_async4(sps + t, g.pairSlot + e * NN * NN + t);
+  if (li < NN) tl20_store_small<FF>(tl20_load_small<FF>(g, e, li), smem, par, li);
+}
+
+// the float-float forms used by the per-point update of the mixed-ff pass
+__device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.h, -a.l}; }
+__device__ __forceinline__ ff ff_sum(ff a, ff b) {
+  ff r = a;
+  ff_add(r, b);
+  return r;
+}
+// a * b - c * d
+__device__ __forceinline__ ff ff_det2(ff a, ff b, ff c, ff d) {
+  ff r = ff_mul(a, b);
+  ff_fma(r, ff_neg(c), d);
+  return r;
+}
+
+// The three warps beside the material warp in phase A1 (li = 0 .. 95): load the next element's
+// U and row lengths into registers, scatter the pending K_e of element prev (its pair slots and
+// row lengths in buffer par ^ 1, U of this element already consumed), then -- once all three
+// warps are past the scatter -- store the next element's small data into buffer par ^ 1.
+template <bool FF>
+__device__ __forceinline__ void tl20_pending_and_next(const GroupArgs& g, int64_t prev, int64_t next, unsigned char* smem,
+                                                      const unsigned char* tb, const int* sps, const int* srl, int par,
+                                                      int li, bool failed) {
+  using L = TL20Layout<FF>;
+  constexpr int NN = TL20::NN, NTH = 96;
+  TL20Small nx{0, {0.0, 0.0, 0.0}, false};
+  if (next >= 0 && li < NN) nx = tl20_load_small<FF>(g, next, li);
+  if (prev >= 0 && !failed) tl20_scatter(g, prev, tb, sps + (par ^ 1) * NN * NN, srl + (par ^ 1) * NN, li, NTH);
+  if (next >= 0) {
+    asm volatile("bar.sync 1, %0;" ::"n"(NTH) : "memory");
+    int* nps = reinterpret_cast<int*>(smem + L::ps_off) + (par ^ 1) * NN * NN;
+    for (int t = li; t < NN * NN; t += NTH) tc::cp_async4(nps + t, g.pairSlot + next * NN * NN + t);
+    if (li < NN) tl20_store_small<FF>(nx, smem, par ^ 1, li);
   }
 }
 
@@ -196,106 +278,214 @@ __device__ __forceinline__ void assemble_tile_tl20_tc(const GroupArgs& g, const 
   const int64_t stride = g.nElements * NQ;
 
   // ---- phase 0: this element's dN/dX, pair slots, U and row lengths in shared memory
-  if (!staged) tl20_stage<FF>(g, e, smem, par, rt);
+  if (!staged) {
+    tl20_stage_g<FF>(g, e, smem);
+    tl20_stage_small<FF>(g, e, smem, par, rt, NT);
+  }
   tc::cp_async_wait_all();
   __syncthreads();
 
-  // ---- A0: F = I + sum_a U_a (x) dN_a/dX, one thread per (point, component)
+  // ---- A0: F = I + sum_a U_a (x) dN_a/dX, one thread per (point, component); the float-float
+  // pass keeps H = F - I in float-float
   for (int t = tid; t < NQ * 9; t += NT) {
     const int c = t / NQ, q = t - c * NQ, i = c / 3, j = c - 3 * i;
     const int g0 = j * NN * NQ + q;
-    double f = (i == j) ? 1.0 : 0.0;
     if constexpr (FF) {
       const ff* uf = reinterpret_cast<const ff*>(smem + L::u_off);
       ff acc{0, 0};
       for (int a = 0; a < NN; ++a) ff_fma(acc, uf[a * DIM + i], ff{sGh[g0 + a * NQ], sGl[g0 + a * NQ]});
-      f += ff_to_double_bits(acc);
+      reinterpret_cast<ff*>(sF)[q * 9 + i * 3 + j] = acc;
     } else {
       const double* u = reinterpret_cast<const double*>(smem + L::u_off);
       double h = 0.0;
       for (int a = 0; a < NN; ++a) h += u[a * DIM + i] * sGd[g0 + a * NQ];
-      f += h;
+      sF[q * 9 + i * 3 + j] = ((i == j) ? 1.0 : 0.0) + h;
     }
-    sF[q * 9 + i * 3 + j] = f;
   }
   __syncthreads();
 
-  // ---- A1: one thread per point of warp rot: E, F^-1, Kirchhoff stress and tangent scalars
-  // (FP64), state, the FP32 record of the tangent and s tau F^-T for the residual; meanwhile the
-  // other warps scatter the pending K_e of the previous element
-  if (rt < 32) {
-    if (rt < NQ) {
-      const int q = rt;
-      const int64_t pt = e * NQ + q;
-      const double* props = g.props + e * g.nProps;
-      double F[3][3];
-      for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) F[i][j] = sF[q * 9 + i * 3 + j];
-      // Green-Lagrange E = 1/2 (H + H^T + H^T H), H = F - I  (:386), symmetric
-      const double H[3][3] = {{F[0][0] - 1.0, F[0][1], F[0][2]}, {F[1][0], F[1][1] - 1.0, F[1][2]},
-                              {F[2][0], F[2][1], F[2][2] - 1.0}};
-      double Eg[3][3];
-      for (int i = 0; i < 3; ++i)
-        for (int j = i; j < 3; ++j)
-          Eg[i][j] = Eg[j][i] = 0.5 * ((H[i][j] + H[j][i]) + (H[0][i] * H[0][j] + H[1][i] * H[1][j] + H[2][i] * H[2][j]));
-      const double Ev[6] = {Eg[0][0], Eg[1][1], Eg[2][2], Eg[0][1], Eg[1][2], Eg[0][2]};
-      for (int f = 0; f < 6; ++f) g.auxTemp[(int64_t)f * stride + pt] = Ev[f];
-      // F^-1 from the cofactors, det F from the same cofactors
-      double iF[3][3];
-      iF[0][0] = F[1][1] * F[2][2] - F[1][2] * F[2][1];
-      iF[1][0] = F[1][2] * F[2][0] - F[1][0] * F[2][2];
-      iF[2][0] = F[1][0] * F[2][1] - F[1][1] * F[2][0];
-      const double J = F[0][0] * iF[0][0] + F[0][1] * iF[1][0] + F[0][2] * iF[2][0];
-      iF[0][1] = F[0][2] * F[2][1] - F[0][1] * F[2][2];
-      iF[0][2] = F[0][1] * F[1][2] - F[0][2] * F[1][1];
-      iF[1][1] = F[0][0] * F[2][2] - F[0][2] * F[2][0];
-      iF[1][2] = F[0][2] * F[1][0] - F[0][0] * F[1][2];
-      iF[2][1] = F[0][1] * F[2][0] - F[0][0] * F[2][1];
-      iF[2][2] = F[0][0] * F[1][1] - F[0][1] * F[1][0];
-      const double rJ = 1.0 / J;
-      for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) iF[i][j] *= rJ;
-      double B[3][3];
-      for (int i = 0; i < 3; ++i)
-        for (int j = i; j < 3; ++j) B[i][j] = B[j][i] = F[i][0] * F[j][0] + F[i][1] * F[j][1] + F[i][2] * F[j][2];
-      const NeoHookeScalars o = neo_hooke_scalars(g.material, props[0], props[1], J, B[0][0] + B[1][1] + B[2][2],
-                                                  F[0][0] + F[1][1] + F[2][2]);
-      // Kirchhoff stress tau = sB B + sI I (Voigt 11, 22, 33, 12, 23, 13)
-      const double sig[6] = {o.sB * B[0][0] + o.sI, o.sB * B[1][1] + o.sI, o.sB * B[2][2] + o.sI,
-                             o.sB * B[0][1],        o.sB * B[1][2],        o.sB * B[0][2]};
-      const double eps[6] = {Eg[0][0], Eg[1][1], Eg[2][2], 2.0 * Eg[0][1], 2.0 * Eg[1][2], 2.0 * Eg[0][2]};
-      const double s = g.geomS[pt];
-      // s tau F^-T = (s sB) F + (s sI) F^-T
-      const double aF = s * o.sB, aI = s * o.sI;
-      float* r = rk + q * T::RK;
-      for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
-          r[T::R_F + i * 3 + j] = d2f_trunc(F[i][j]);
-          r[T::R_FI + i * 3 + j] = d2f_trunc(iF[i][j]);
-          r[T::R_B + i * 3 + j] = d2f_trunc(B[i][j]);
-          const double pq = aF * F[i][j] + aI * iF[j][i];
-          r[T::R_PQ + i * 3 + j] = d2f_trunc(pq);
-          if constexpr (FF)
-            reinterpret_cast<ff*>(smem + L::pq_off)[q * 9 + i * 3 + j] = ff_split_bits(pq);
-          else
-            reinterpret_cast<double*>(smem + L::pq_off)[q * 9 + i * 3 + j] = pq;
-        }
-      r[T::R_C + 0] = d2f_trunc(o.c1 * s);
-      r[T::R_C + 1] = d2f_trunc(o.c2 * s);
-      r[T::R_C + 2] = d2f_trunc(o.c3 * s);
-      r[T::R_C + 3] = d2f_trunc(o.c4 * s);
-      // state write (stateTemp = updated copy of stateRef)
-      for (int f = 0; f < 6; ++f) {
-        g.stateTemp[(int64_t)f * stride + pt] = sig[f];
-        g.stateTemp[(int64_t)(6 + f) * stride + pt] = eps[f];
+  // ---- A1: the material points.  Warp rot runs the per-point FP64 part (all of it in the mixed
+  // pass; in the mixed-ff pass only the Neo-Hooke scalars, between two float-float sub-phases that
+  // use every thread); meanwhile the other warps scatter the pending K_e of the previous element.
+  if constexpr (FF) {
+    const ff* sH = reinterpret_cast<const ff*>(sF);
+    ff* sA1 = reinterpret_cast<ff*>(tb + T::a1_off);  // [q][E 0-5 | C 6-14 | B 15-20]
+    T::A1Scalars* sSc = reinterpret_cast<T::A1Scalars*>(tb + T::a1s_off);
+    // Voigt entry v (11, 22, 33, 12, 23, 13) -> (i, j)
+    auto vi = [](int v) { return v < 3 ? v : (v == 4 ? 1 : 0); };
+    auto vj = [](int v) { return v < 3 ? v : (v == 3 ? 1 : 2); };
+    // A1a: one thread per (point, entry): E = 1/2 (H + H^T + H^T H) (:386), the cofactors of F
+    // (C = adj F: F^-1 = C / J) and B = F F^T, in float-float from H = F - I
+    for (int t = tid; t < NQ * T::NA1; t += NT) {
+      const int k = t / NQ, q = t - k * NQ;
+      const ff* H = sH + q * 9;
+      auto Fv = [&](int i, int j) { return i == j ? ff_sum(H[i * 3 + j], ff{1.0f, 0.0f}) : H[i * 3 + j]; };
+      ff r;
+      if (k < 6) {
+        const int i = vi(k), j = vj(k);
+        r = ff_sum(H[i * 3 + j], H[j * 3 + i]);
+        ff_fma(r, H[0 * 3 + i], H[0 * 3 + j]);
+        ff_fma(r, H[1 * 3 + i], H[1 * 3 + j]);
+        ff_fma(r, H[2 * 3 + i], H[2 * 3 + j]);
+        r = ff{0.5f * r.h, 0.5f * r.l};
+      } else if (k < 15) {
+        // C[i][j] = F[i1][j1] F[i2][j2] - F[i1][j2] F[i2][j1] with the rows of the transposed minor
+        const int i = (k - 6) / 3, j = (k - 6) - 3 * i;
+        const int r1 = (j + 1) % 3, r2 = (j + 2) % 3, c1 = (i + 1) % 3, c2 = (i + 2) % 3;
+        r = ff_det2(Fv(r1, c1), Fv(r2, c2), Fv(r1, c2), Fv(r2, c1));
+      } else {
+        const int i = vi(k - 15), j = vj(k - 15);
+        r = ff_mul(Fv(i, 0), Fv(j, 0));
+        ff_fma(r, Fv(i, 1), Fv(j, 1));
+        ff_fma(r, Fv(i, 2), Fv(j, 2));
       }
-      g.stateTemp[(int64_t)12 * stride + pt] = o.energy;
-      bool finite = true;
-      for (int f = 0; f < 6; ++f) finite = finite && finite_bits(sig[f]);
-      if (!finite) atomicOr(g.status, EFE_STATUS_NONFINITE);
+      sA1[q * T::NA1 + k] = r;
     }
-  } else if (prev >= 0 && !tcs.failed) {
-    tl20_scatter(g, prev, tb, sps + (par ^ 1) * NN * NN, srl + (par ^ 1) * NN, rt - 32, NT - 32);
+    __syncthreads();
+    // A1b: one thread per point of warp rot: J, I1, tr F, 1/J, the Neo-Hooke scalars (FP64)
+    if (rt < 32) {
+      if (rt < NQ) {
+        const int q = rt;
+        const int64_t pt = e * NQ + q;
+        const double* props = g.props + e * g.nProps;
+        const ff* H = sH + q * 9;
+        const ff* A = sA1 + q * T::NA1;
+        ff Jf = ff_mul(ff_sum(H[0], ff{1.0f, 0.0f}), A[6 + 0]);  // F00 C00 + F01 C10 + F02 C20
+        ff_fma(Jf, H[1], A[6 + 3]);
+        ff_fma(Jf, H[2], A[6 + 6]);
+        const ff I1 = ff_sum(ff_sum(A[15], A[16]), A[17]);
+        const ff trF = ff_sum(ff_sum(ff_sum(H[0], H[4]), H[8]), ff{3.0f, 0.0f});
+        const NeoHookeScalars o = neo_hooke_scalars(g.material, props[0], props[1], ff_to_double_bits(Jf),
+                                                    ff_to_double_bits(I1), ff_to_double_bits(trF));
+        // 1/J: FP32 reciprocal and one Newton step in float-float
+        const float r0 = __frcp_rn(Jf.h);
+        ff rJ = ff_mul(Jf, ff{-r0, 0.0f});
+        ff_add(rJ, ff{1.0f, 0.0f});
+        rJ = ff_mul(rJ, ff{r0, 0.0f});
+        ff_add(rJ, ff{r0, 0.0f});
+        const double s = g.geomS[pt];
+        T::A1Scalars sc;
+        sc.sB = ff_split_bits(o.sB);
+        sc.sI = ff_split_bits(o.sI);
+        sc.aF = ff_split_bits(s * o.sB);  // s tau F^-T = (s sB) F + (s sI) F^-T
+        sc.aI = ff_split_bits(s * o.sI);
+        sc.rJ = rJ;
+        sc.energy = o.energy;
+        sc.c[0] = d2f_trunc(o.c1 * s);
+        sc.c[1] = d2f_trunc(o.c2 * s);
+        sc.c[2] = d2f_trunc(o.c3 * s);
+        sc.c[3] = d2f_trunc(o.c4 * s);
+        sSc[q] = sc;
+      }
+    } else {
+      tl20_pending_and_next<FF>(g, prev, next, smem, tb, sps, srl, par, rt - 32, tcs.failed);
+    }
+    __syncthreads();
+    // A1c: one thread per (point, entry (i, j)): F^-1, s tau F^-T, the FP32 record, state
+    for (int t = tid; t < NQ * 9; t += NT) {
+      const int c = t / NQ, q = t - c * NQ, i = c / 3, j = c - 3 * i;
+      const int64_t pt = e * NQ + q;
+      const ff* H = sH + q * 9;
+      const ff* A = sA1 + q * T::NA1;
+      const T::A1Scalars& sc = sSc[q];
+      const ff Fij = i == j ? ff_sum(H[c], ff{1.0f, 0.0f}) : H[c];
+      const ff iFij = ff_mul(A[6 + c], sc.rJ), iFji = ff_mul(A[6 + j * 3 + i], sc.rJ);
+      // B is stored in Voigt order 11, 22, 33, 12, 23, 13
+      const ff Bij = A[15 + (i == j ? i : (i + j == 1 ? 3 : (i + j == 3 ? 4 : 5)))];
+      ff pq = ff_mul(sc.aF, Fij);
+      ff_fma(pq, sc.aI, iFji);
+      float* r = rk + q * T::RK;
+      r[T::R_F + c] = Fij.h;
+      r[T::R_FI + c] = iFij.h;
+      r[T::R_B + c] = Bij.h;
+      r[T::R_PQ + c] = pq.h;
+      reinterpret_cast<ff*>(smem + L::pq_off)[q * 9 + c] = pq;
+      if (c < 4) r[T::R_C + c] = sc.c[c];
+      if (c < 6) {
+        // Voigt entry c: Kirchhoff stress tau = sB B + sI I, strain (E with doubled shears), E
+        ff tv = ff_mul(sc.sB, A[15 + c]);
+        if (c < 3) ff_add(tv, sc.sI);
+        const double sig = ff_to_double_bits(tv), Ev = ff_to_double_bits(A[c]);
+        g.stateTemp[(int64_t)c * stride + pt] = sig;
+        g.stateTemp[(int64_t)(6 + c) * stride + pt] = c < 3 ? Ev : 2.0 * Ev;
+        g.auxTemp[(int64_t)c * stride + pt] = Ev;
+        if (!finite_bits(sig)) atomicOr(g.status, EFE_STATUS_NONFINITE);
+      } else if (c == 6) {
+        g.stateTemp[(int64_t)12 * stride + pt] = sc.energy;
+      }
+    }
+  } else {
+    if (rt < 32) {
+      if (rt < NQ) {
+        const int q = rt;
+        const int64_t pt = e * NQ + q;
+        const double* props = g.props + e * g.nProps;
+        double F[3][3];
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) F[i][j] = sF[q * 9 + i * 3 + j];
+        // Green-Lagrange E = 1/2 (H + H^T + H^T H), H = F - I  (:386), symmetric
+        const double H[3][3] = {{F[0][0] - 1.0, F[0][1], F[0][2]}, {F[1][0], F[1][1] - 1.0, F[1][2]},
+                                {F[2][0], F[2][1], F[2][2] - 1.0}};
+        double Eg[3][3];
+        for (int i = 0; i < 3; ++i)
+          for (int j = i; j < 3; ++j)
+            Eg[i][j] = Eg[j][i] = 0.5 * ((H[i][j] + H[j][i]) + (H[0][i] * H[0][j] + H[1][i] * H[1][j] + H[2][i] * H[2][j]));
+        const double Ev[6] = {Eg[0][0], Eg[1][1], Eg[2][2], Eg[0][1], Eg[1][2], Eg[0][2]};
+        for (int f = 0; f < 6; ++f) g.auxTemp[(int64_t)f * stride + pt] = Ev[f];
+        // F^-1 from the cofactors, det F from the same cofactors
+        double iF[3][3];
+        iF[0][0] = F[1][1] * F[2][2] - F[1][2] * F[2][1];
+        iF[1][0] = F[1][2] * F[2][0] - F[1][0] * F[2][2];
+        iF[2][0] = F[1][0] * F[2][1] - F[1][1] * F[2][0];
+        const double J = F[0][0] * iF[0][0] + F[0][1] * iF[1][0] + F[0][2] * iF[2][0];
+        iF[0][1] = F[0][2] * F[2][1] - F[0][1] * F[2][2];
+        iF[0][2] = F[0][1] * F[1][2] - F[0][2] * F[1][1];
+        iF[1][1] = F[0][0] * F[2][2] - F[0][2] * F[2][0];
+        iF[1][2] = F[0][2] * F[1][0] - F[0][0] * F[1][2];
+        iF[2][1] = F[0][1] * F[2][0] - F[0][0] * F[2][1];
+        iF[2][2] = F[0][0] * F[1][1] - F[0][1] * F[1][0];
+        const double rJ = 1.0 / J;
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) iF[i][j] *= rJ;
+        double B[3][3];
+        for (int i = 0; i < 3; ++i)
+          for (int j = i; j < 3; ++j) B[i][j] = B[j][i] = F[i][0] * F[j][0] + F[i][1] * F[j][1] + F[i][2] * F[j][2];
+        const NeoHookeScalars o = neo_hooke_scalars(g.material, props[0], props[1], J, B[0][0] + B[1][1] + B[2][2],
+                                                    F[0][0] + F[1][1] + F[2][2]);
+        // Kirchhoff stress tau = sB B + sI I (Voigt 11, 22, 33, 12, 23, 13)
+        const double sig[6] = {o.sB * B[0][0] + o.sI, o.sB * B[1][1] + o.sI, o.sB * B[2][2] + o.sI,
+                               o.sB * B[0][1],        o.sB * B[1][2],        o.sB * B[0][2]};
+        const double eps[6] = {Eg[0][0], Eg[1][1], Eg[2][2], 2.0 * Eg[0][1], 2.0 * Eg[1][2], 2.0 * Eg[0][2]};
+        const double s = g.geomS[pt];
+        // s tau F^-T = (s sB) F + (s sI) F^-T
+        const double aF = s * o.sB, aI = s * o.sI;
+        float* r = rk + q * T::RK;
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) {
+            r[T::R_F + i * 3 + j] = d2f_trunc(F[i][j]);
+            r[T::R_FI + i * 3 + j] = d2f_trunc(iF[i][j]);
+            r[T::R_B + i * 3 + j] = d2f_trunc(B[i][j]);
+            const double pq = aF * F[i][j] + aI * iF[j][i];
+            r[T::R_PQ + i * 3 + j] = d2f_trunc(pq);
+            reinterpret_cast<double*>(smem + L::pq_off)[q * 9 + i * 3 + j] = pq;
+          }
+        r[T::R_C + 0] = d2f_trunc(o.c1 * s);
+        r[T::R_C + 1] = d2f_trunc(o.c2 * s);
+        r[T::R_C + 2] = d2f_trunc(o.c3 * s);
+        r[T::R_C + 3] = d2f_trunc(o.c4 * s);
+        // state write (stateTemp = updated copy of stateRef)
+        for (int f = 0; f < 6; ++f) {
+          g.stateTemp[(int64_t)f * stride + pt] = sig[f];
+          g.stateTemp[(int64_t)(6 + f) * stride + pt] = eps[f];
+        }
+        g.stateTemp[(int64_t)12 * stride + pt] = o.energy;
+        bool finite = true;
+        for (int f = 0; f < 6; ++f) finite = finite && finite_bits(sig[f]);
+        if (!finite) atomicOr(g.status, EFE_STATUS_NONFINITE);
+      }
+    } else {
+      tl20_pending_and_next<FF>(g, prev, next, smem, tb, sps, srl, par, rt - 32, tcs.failed);
+    }
   }
   __syncthreads();
   // zero the operand tiles (padding rows and slots must read as zero)
@@ -365,9 +555,9 @@ __device__ __forceinline__ void assemble_tile_tl20_tc(const GroupArgs& g, const 
     }
     tc::fence_proxy_async();
     __syncthreads();
-    // after the last chunk's operands the staged dN/dX, U and the other pair-slot buffer are dead:
-    // stage the next element while the MMAs run
-    if (ch == T::NCH - 1 && next >= 0) tl20_stage<FF>(g, next, smem, par ^ 1, rt);
+    // after the last chunk's operands and residual the staged dN/dX is dead: stage the next
+    // element's while the MMAs run
+    if (ch == T::NCH - 1 && next >= 0) tl20_stage_g<FF>(g, next, smem);
     if (tid == 0 && !tcs.failed) {
       tc::fence_after_sync();
       constexpr uint32_t idPS = tc::idesc_tf32(128, 64), idD = tc::idesc_tf32(128, 32);
