@@ -732,6 +732,58 @@ def run_batched(args):
     }  # fmt: skip
 
 
+# ------------------------------------------------------------------ the Hexa20 TL pass alone
+def run_hexa20tl(args):
+    """The C3D20TL Neo-Hooke (a) element pass on an n x n x n/2 box (default n = 32: 16,384 elements)
+    under F = I + 0.05 N(0,1): CUDA-event time per pass for each precision with an FP32 tangent and
+    tile variants 0 (SIMT tangent), 2 and 3 (tangent on the tensor cores), and the difference of each
+    variant's K and P from variant 0's."""
+    import torch
+
+    from edelweissfe_gb300 import ElementGroup, GPUAssembler, meshes
+
+    n = args.n if args.n != N_CUBE else 32
+    coords, conn, nodeDof, nDof = meshes.box(n, n, max(1, n // 2), nNodes=20)
+    rng = np.random.default_rng(1)
+    Fbar = np.eye(3) + 0.05 * rng.normal(size=(3, 3))
+    disp = coords @ (Fbar - np.eye(3)).T
+    U = np.zeros(nDof)
+    for c in range(3):
+        U[nodeDof + c] = disp[:, c]
+    out = {"metric": "assembled elem/s (K+R), C3D20TL Neo-Hooke (a) element pass", "unit": "elem/s",
+           "config": {"workload": f"C3D20TL {n}x{n}x{max(1, n // 2)} box, F = I + 0.05 N(0,1)", "elements": len(conn)},
+           "steps": args.steps, "warmup": args.warmup, "precisions": {}}  # fmt: skip
+    for prec in ("mixed", "mixed-ff"):
+        asm = GPUAssembler(coords, nodeDof, nDof, [ElementGroup("C3D20TL", "neohookewa", [300.0, 3000.0], conn)],
+                           precision=prec)  # fmt: skip
+        Ud = torch.tensor(U, device=asm.device)
+        P, F, K = asm.constructDofVector(), asm.constructDofVector(), asm.constructSystemMatrix()
+        ref, res = None, {}
+        for v in (0, 2, 3):
+            asm._groups_c[0].tileVariant = v
+            for _ in range(max(1, args.warmup)):
+                P.zero_(), K.zero_(), F.zero_()
+                asm.launch(Ud, Ud, P, K, F)
+            torch.cuda.synchronize()
+            asm.check_status()
+            Kc, Pc = K.double().cpu().numpy(), P.cpu().numpy()
+            ref = ref or (Kc, Pc)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            for _ in range(args.steps):
+                asm.launch(Ud, Ud, P, K, F)
+            b.record()
+            torch.cuda.synchronize()
+            ms = a.elapsed_time(b) / args.steps
+            res[str(v)] = {"ms": ms, "elem_per_s": len(conn) / (ms * 1e-3),
+                           "K_rel_vs_variant0": float(np.abs(Kc - ref[0]).max() / np.abs(ref[0]).max()),
+                           "P_rel_vs_variant0": float(np.abs(Pc - ref[1]).max() / np.abs(ref[1]).max())}  # fmt: skip
+        out["precisions"][prec] = res
+        del asm, P, F, K
+        torch.cuda.empty_cache()
+    return out
+
+
 # ------------------------------------------------------------------ Newton iteration counts (64^3 J2)
 def run_newton(args):
     """The 64^3 von Mises cube under uniaxial displacement: bottom u_y = 0, left u_x = 0, back u_z = 0,
@@ -1131,11 +1183,13 @@ def main():
     ap.add_argument("--n", type=int, default=N_CUBE, help="elements per cube edge")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tile variant (0)")
-    ap.add_argument("--workload", default="all", choices=["all", "cube", "batched", "newton", "adjoint", "plastic"],
+    ap.add_argument("--workload", default="all",
+                    choices=["all", "cube", "batched", "newton", "adjoint", "plastic", "hexa20tl"],
                     help="all (default): the 64^3 von Mises headline line, with the batched, adjoint and plastic "
                          "workloads under its 'configs' key (one GPU); cube: the headline only; batched: the "
                          "uneven-mesh batch; newton: Newton iterations FP64 vs mixed on the 64^3 cube; adjoint: "
-                         "32^3 Neo-Hooke gradients; plastic: Hexa20 J2 96x96x48 path adjoint")
+                         "32^3 Neo-Hooke gradients; plastic: Hexa20 J2 96x96x48 path adjoint; hexa20tl: the "
+                         "C3D20TL Neo-Hooke pass alone (n x n x n/2) per precision and tile variant")
     ap.add_argument("--plastic-fd", type=int, default=0, help="FD directions for the plastic workload")
     ap.add_argument("--plastic-n", type=int, default=0,
                     help="plastic workload mesh (n x n x n/2); 0: 96, or 48 inside the default 'all' run")
@@ -1149,7 +1203,7 @@ def main():
     ap.add_argument("--batch-meshes", type=int, default=512)
     ap.add_argument("--batch-scale", type=float, default=1.0)
     ap.add_argument("--batch-precision", default="mixed", choices=["mixed", "mixed-ff", "fp64"],
-                    help="batched workload: tangent/residual precision (mixed-ff: per-batch launches)")
+                    help="batched workload: tangent/residual precision")
     ap.add_argument("--batch-launch", default="persistent", choices=["persistent", "auto"],
                     help="batched workload: one persistent launch over all batches, or the autotuner's choice")
     ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64", "mixed-ff"],
@@ -1161,9 +1215,10 @@ def main():
         if rank == 0:
             run_reference(args)
         return
-    if args.workload in ("batched", "adjoint", "plastic"):
+    if args.workload in ("batched", "adjoint", "plastic", "hexa20tl"):
         if rank == 0:
-            fn = {"batched": run_batched, "adjoint": run_adjoint, "plastic": run_plastic}[args.workload]
+            fn = {"batched": run_batched, "adjoint": run_adjoint, "plastic": run_plastic,
+                  "hexa20tl": run_hexa20tl}[args.workload]  # fmt: skip
             print(json.dumps(fn(args), default=str))
         return
     if args.workload == "newton":
@@ -1279,7 +1334,8 @@ def main():
 
 def run_other_configs(args):
     """The other workloads of the benchmark set, each timed on its own with its own roofline, CPU
-    baseline, end-to-end figure and clock record: the 512-mesh batched pass (full size), the 32^3
+    baseline, end-to-end figure and clock record: the 512-mesh batched pass (full size; FP64 residual
+    and, without a second CPU baseline, float-float residual), the 32^3
     Neo-Hooke adjoint (with args.all_fd_directions finite-difference checks) and the plastic path
     adjoint at 48 x 48 x 24 (the full 96 x 96 x 48 run takes ~11 minutes: --workload plastic)."""
     import gc
@@ -1288,6 +1344,7 @@ def run_other_configs(args):
 
     out = {}
     jobs = (("batched_512_meshes", run_batched, {}),
+            ("batched_512_meshes_mixed_ff", run_batched, {"batch_precision": "mixed-ff", "no_cpu_baseline": True}),
             ("adjoint_32cube", run_adjoint, {"fd_directions": args.all_fd_directions}),
             ("plastic_adjoint_48x48x24", run_plastic, {"plastic_n": args.plastic_n or 48}))  # fmt: skip
     for name, fn, over in jobs:

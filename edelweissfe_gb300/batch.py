@@ -115,9 +115,9 @@ def persistent_capable(batches):
         return False
     if any(kinds.count(k) > PERSISTENT_MAX_GROUPS for k in set(kinds)):
         return False
-    # one precision for all, FP64 or the FP32 tangent (the persistent kernel has no float-float form)
+    # one precision for all (each type of the persistent kernel has its float-float form too)
     precs = {b.asm.kPrecision for b in batches}
-    return len(precs) == 1 and precs <= {L.EFE_K_FP64, L.EFE_K_FP32}
+    return len(precs) == 1
 
 
 class BatchedPass:

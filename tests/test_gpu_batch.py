@@ -90,7 +90,7 @@ def test_batched_pass_matches_single_meshes(precision):
         assert _rel(b.K.double().cpu().numpy(), results["persistent"][k][2]) <= ktol
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed-ff"])
 def test_persistent_pass_over_many_batches(precision):
     """Five batches (three Hexa20, two Quad8) in ONE persistent launch give the per-batch results; a
     CUDA-graph replay of it too; a batch of another element type is refused."""
@@ -207,7 +207,7 @@ def _small_strain_meshes(seed, nNodes, sizes):
     return out
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed-ff"])
 def test_mixed_type_persistent_launch(precision):
     """ONE persistent launch over Hexa20 total-Lagrangian Neo-Hooke, Hexa20 and Hexa8 small-strain von
     Mises (plastic increment), Hexa8 total-Lagrangian Neo-Hooke and Quad8 total-Lagrangian Neo-Hooke

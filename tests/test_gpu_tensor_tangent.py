@@ -66,7 +66,8 @@ def _block():
     return coords, conn, nodeDof, nDof, U
 
 
-def test_persistent_launch_with_tensor_core_hexa20():
+@pytest.mark.parametrize("precision", ["mixed", "mixed-ff"])
+def test_persistent_launch_with_tensor_core_hexa20(precision):
     """Uneven Hexa20 total-Lagrangian meshes (two batches, every group on tile variant 3) and a Quad8
     batch in ONE persistent launch: the Hexa20 tangents come from the tensor cores; results equal
     the per-batch launches with the SIMT tangent (K 2e-6) and the oracle mesh by mesh."""
@@ -95,7 +96,7 @@ def test_persistent_launch_with_tensor_core_hexa20():
     spec = [(ms3[:2], "C3D20TL"), (ms3[2:], "C3D20TL"), (ms2, "CPE8RTL")]
     batches = []
     for ms, et in spec:
-        b = MeshBatch(ms, et, "neohookewa", "mixed")
+        b = MeshBatch(ms, et, "neohookewa", precision)
         b.U.copy_(torch.tensor(np.concatenate([m["U"] for m in ms])))
         batches.append(b)
     out = {}
