@@ -9,19 +9,22 @@ import os
 import torch
 
 VARIANTS = (0, 1, 2)
-TENSOR_VARIANT = 3  # the element tangent on the tensor cores (Hexa20 total-Lagrangian Neo-Hooke, FP32 tangent)
+TENSOR_VARIANT = 3  # the element tangent on the tensor cores (Hexa20 3x3x3 TL Neo-Hooke or small strain, FP32 tangent)
 
 
 def variants_for(asm, gi):
     """Tile variants to time for group gi: the CTA shapes 0-2, and the tensor-core tangent where the
-    library has it (Hexa20 3x3x3 total-Lagrangian with a hyperelastic material and an FP32 tangent)."""
+    library has it (Hexa20 3x3x3, total-Lagrangian with a hyperelastic material or small strain,
+    with an FP32 tangent)."""
     from . import _lib as L
     from .library import element_type
 
     g = asm.groups[gi]
     et = element_type(g.elType)
-    tc = (et.shape == L.EFE_HEXA20 and et.rule == L.EFE_RULE_3D_3X3X3 and et.totalLagrangian
-          and g.material.lower().startswith("neohooke") and asm.kPrecision in (L.EFE_K_FP32, L.EFE_K_FP32_FF))  # fmt: skip
+    hyper = g.material.lower().startswith("neohooke")
+    form_ok = (et.totalLagrangian and hyper) or (not et.totalLagrangian and not hyper)
+    tc = (et.shape == L.EFE_HEXA20 and et.rule == L.EFE_RULE_3D_3X3X3 and form_ok
+          and asm.kPrecision in (L.EFE_K_FP32, L.EFE_K_FP32_FF))  # fmt: skip
     return VARIANTS + ((TENSOR_VARIANT,) if tc else ())
 
 

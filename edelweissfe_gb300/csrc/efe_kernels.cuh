@@ -939,12 +939,12 @@ __device__ __forceinline__ void tc_end(TCState& tcs) {
   if (threadIdx.x < 32) tc::tmem_dealloc(tcs.tmem, TL20::TMEM_COLS);
 }
 
-// Tile variant 3, the Hexa20 total-Lagrangian Neo-Hooke pass with the tensor-core tangent
-// (efe_tl20_tc.cuh): a grid of resident CTAs (sms per wave), one element per tile, tiles strided by
+// Tile variant 3, the Hexa20 3x3x3 pass (total-Lagrangian Neo-Hooke or small strain) with the
+// tensor-core tangent (efe_tl20_tc.cuh): a grid of resident CTAs (sms per wave), one element per tile, tiles strided by
 // the grid; each CTA allocates its TMEM columns once and frees them at the end.  The CTAs of one
 // wave share no SM, so the wave index picks the warp of the per-point update.  Each element's
 // K_e scatter runs during the next element's material update (the last one after the loop).
-template <bool FF>
+template <bool FF, int FORM>
 __global__ void __launch_bounds__(128, 3) assemble_kernel_tc(GroupArgs g, int sms) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t mbar;
@@ -954,7 +954,7 @@ __global__ void __launch_bounds__(128, 3) assemble_kernel_tc(GroupArgs g, int sm
   int64_t prev = TL20_DEFER_NONE;  // the element whose K_e is pending in shared memory
   for (int64_t e = blockIdx.x; e < g.nElements; e += gridDim.x, ++rot, par ^= 1) {
     const int64_t next = e + gridDim.x < g.nElements ? e + gridDim.x : -1;
-    assemble_tile_tl20_tc<FF>(g, e, smem, tcs, rot, prev, next, prev >= 0, par);
+    assemble_tile_tl20_tc<FF, FORM>(g, e, smem, tcs, rot, prev, next, prev >= 0, par);
     prev = e;
     __syncthreads();
   }
@@ -1010,7 +1010,8 @@ __device__ __forceinline__ bool persistent_tile(const GroupTables<N>& tabs, long
     int k = 0;
     while (t >= tb.tileStart[k + 1]) ++k;
     if constexpr (T0::TC)
-      assemble_tile_tl20_tc<FF>(tb.g[k], (int64_t)(t - tb.tileStart[k]), smem, *tcs, rot, TL20_NOW, -1, false, 0);
+      assemble_tile_tl20_tc<FF, T0::FORM>(tb.g[k], (int64_t)(t - tb.tileStart[k]), smem, *tcs, rot, TL20_NOW, -1, false,
+                                          0);
     else
       assemble_tile<T0::SHAPE, T0::RULE, T0::FORM, KT, T0::EPB, NT, FF>(tb.g[k], (int64_t)(t - tb.tileStart[k]) * T0::EPB,
                                                                         smem);

@@ -43,11 +43,12 @@ cudaError_t launch_assemble_variant(const GroupArgs& g, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-// the tensor-core tangent (tile variant 3) exists for the Hexa20 3x3x3 total-Lagrangian Neo-Hooke form
-// with an FP32 tangent
+// the tensor-core tangent (tile variant 3) exists for the Hexa20 3x3x3 total-Lagrangian Neo-Hooke
+// and small-strain (von Mises, linear elastic) forms with an FP32 tangent
 template <int SHAPE, int RULE, int FORM, typename KT>
 constexpr bool has_tc_variant() {
-  return SHAPE == EFE_HEXA20 && RULE == EFE_RULE_3D_3X3X3 && FORM == TLH && std::is_same<KT, float>::value;
+  return SHAPE == EFE_HEXA20 && RULE == EFE_RULE_3D_3X3X3 && (FORM == TLH || FORM == SS3) &&
+         std::is_same<KT, float>::value;
 }
 
 // Resident CTAs per SM of a kernel that allocates tmemCols TMEM columns per CTA, from its registers
@@ -76,12 +77,12 @@ cudaError_t resident_ctas_tmem(K kern, int nt, size_t dynBytes, int tmemCols, in
   return n >= 1 ? cudaSuccess : cudaErrorInvalidConfiguration;
 }
 
-template <bool FF>
+template <bool FF, int FORM>
 cudaError_t launch_assemble_tc(const GroupArgs& g, cudaStream_t st) {
   constexpr int NT = 128;
   constexpr size_t bytes = TL20Layout<FF>::bytes;
   static_assert(bytes <= 74 * 1024, "three tensor-core tiles must fit in one SM");
-  auto kern = assemble_kernel_tc<FF>;
+  auto kern = assemble_kernel_tc<FF, FORM>;
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (err != cudaSuccess) return err;
   // the largest shared-memory partition: without it the occupancy query (and the launch) assume the
@@ -102,7 +103,7 @@ cudaError_t launch_assemble_tc(const GroupArgs& g, cudaStream_t st) {
 template <int SHAPE, int RULE, int FORM, typename KT, bool FF = false>
 cudaError_t launch_assemble(const GroupArgs& g, cudaStream_t st) {
   if constexpr (has_tc_variant<SHAPE, RULE, FORM, KT>()) {
-    if (g.tileVariant == 3) return launch_assemble_tc<FF>(g, st);
+    if (g.tileVariant == 3) return launch_assemble_tc<FF, FORM>(g, st);
   }
   if (g.tileVariant == 1) return launch_assemble_variant<SHAPE, RULE, FORM, KT, FF, 1>(g, st);
   if constexpr (Tile<SHAPE, RULE, FORM, KT, 2>::MINB != Tile<SHAPE, RULE, FORM, KT, 0>::MINB) {

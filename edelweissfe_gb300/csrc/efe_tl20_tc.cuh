@@ -83,7 +83,8 @@ struct TL20Layout {
   // pair slots and row lengths of two consecutive elements (the pending K_e and the current one)
   static constexpr size_t ps_off = g_off + 8 * T::NQ * T::NDOF;         // int [2][NN][NN]
   static constexpr size_t rl_off = ps_off + sizeof(int) * 2 * T::NN * T::NN;  // int [2][NN]
-  static constexpr size_t tc_off = (rl_off + sizeof(int) * 2 * T::NN + 127) / 128 * 128;
+  static constexpr size_t mc_off = (rl_off + sizeof(int) * 2 * T::NN + 15) / 16 * 16;  // VMConst (small strain)
+  static constexpr size_t tc_off = (mc_off + sizeof(VMConst) + 127) / 128 * 128;
   static constexpr size_t bytes = tc_off + T::tc_bytes;
 };
 
@@ -164,9 +165,10 @@ struct TL20Small {
   double u[3];
   bool valid;
 };
-template <bool FF>
+template <bool FF, int FORM>
 __device__ __forceinline__ TL20Small tl20_load_small(const GroupArgs& g, int64_t e, int a) {
   constexpr int NN = TL20::NN, DIM = 3;
+  const double* Ux = FORM == SS3 ? g.dU : g.U;  // small strain: the increment; TL: the total
   TL20Small r{0, {0.0, 0.0, 0.0}, false};
   const int32_t node = g.conn[e * NN + a];
   if (!in_bounds(g, node, g.nNodes, e)) return r;
@@ -179,9 +181,9 @@ __device__ __forceinline__ TL20Small tl20_load_small(const GroupArgs& g, int64_t
     const int32_t node0 = g.conn[e * NN];
     const int32_t dof0 = in_bounds(g, node0, g.nNodes, e) ? g.nodeDof[node0] : dof;
     const int32_t d0 = in_bounds(g, dof0, g.nDof - DIM + 1, e) ? dof0 : dof;
-    for (int c = 0; c < DIM; ++c) r.u[c] = g.U[dof + c] - g.U[d0 + c];
+    for (int c = 0; c < DIM; ++c) r.u[c] = Ux[dof + c] - Ux[d0 + c];
   } else {
-    for (int c = 0; c < DIM; ++c) r.u[c] = g.U[dof + c];
+    for (int c = 0; c < DIM; ++c) r.u[c] = Ux[dof + c];
   }
   return r;
 }
@@ -198,14 +200,14 @@ __device__ __forceinline__ void tl20_store_small(const TL20Small& r, unsigned ch
       reinterpret_cast<double*>(smem + L::u_off)[a * DIM + c] = r.u[c];
   }
 }
-template <bool FF>
+template <bool FF, int FORM>
 __device__ __forceinline__ void tl20_stage_small(const GroupArgs& g, int64_t e, unsigned char* smem, int par, int li,
                                                  int nth) {
   using L = TL20Layout<FF>;
   constexpr int NN = TL20::NN;
   int* sps = reinterpret_cast<int*>(smem + L::ps_off) + par * NN * NN;
   for (int t = li; t < NN * NN; t += nth) tc::cp_async4(sps + t, g.pairSlot + e * NN * NN + t);
-  if (li < NN) tl20_store_small<FF>(tl20_load_small<FF>(g, e, li), smem, par, li);
+  if (li < NN) tl20_store_small<FF>(tl20_load_small<FF, FORM>(g, e, li), smem, par, li);
 }
 
 // the float-float forms used by the per-point update of the mixed-ff pass
@@ -226,14 +228,14 @@ __device__ __forceinline__ ff ff_det2(ff a, ff b, ff c, ff d) {
 // U and row lengths into registers, scatter the pending K_e of element prev (its pair slots and
 // row lengths in buffer par ^ 1, U of this element already consumed), then -- once all three
 // warps are past the scatter -- store the next element's small data into buffer par ^ 1.
-template <bool FF>
+template <bool FF, int FORM>
 __device__ __forceinline__ void tl20_pending_and_next(const GroupArgs& g, int64_t prev, int64_t next, unsigned char* smem,
                                                       const unsigned char* tb, const int* sps, const int* srl, int par,
                                                       int li, bool failed) {
   using L = TL20Layout<FF>;
   constexpr int NN = TL20::NN, NTH = 96;
   TL20Small nx{0, {0.0, 0.0, 0.0}, false};
-  if (next >= 0 && li < NN) nx = tl20_load_small<FF>(g, next, li);
+  if (next >= 0 && li < NN) nx = tl20_load_small<FF, FORM>(g, next, li);
   if (prev >= 0 && !failed) tl20_scatter(g, prev, tb, sps + (par ^ 1) * NN * NN, srl + (par ^ 1) * NN, li, NTH);
   if (next >= 0) {
     asm volatile("bar.sync 1, %0;" ::"n"(NTH) : "memory");
@@ -257,7 +259,7 @@ constexpr int64_t TL20_NOW = -2;         // scatter this element's K_e at the en
 // three other warps while one warp runs this element's material update; after the last call the
 // caller scatters the pending one (tl20_scatter).  next >= 0: the element of the next call, staged
 // while this element's last MMAs run; staged: this element was staged that way by the previous call.
-template <bool FF>
+template <bool FF, int FORM>
 __device__ __forceinline__ void assemble_tile_tl20_tc(const GroupArgs& g, const int64_t e, unsigned char* smem,
                                                       TCState& tcs, int rot, int64_t prev, int64_t next, bool staged,
                                                       int par) {
@@ -280,13 +282,16 @@ __device__ __forceinline__ void assemble_tile_tl20_tc(const GroupArgs& g, const 
   // ---- phase 0: this element's dN/dX, pair slots, U and row lengths in shared memory
   if (!staged) {
     tl20_stage_g<FF>(g, e, smem);
-    tl20_stage_small<FF>(g, e, smem, par, rt, NT);
+    tl20_stage_small<FF, FORM>(g, e, smem, par, rt, NT);
   }
+  // small strain: the element's von Mises / elasticity constants, once per element
+  if (FORM == SS3 && tid == NT - 1)
+    *reinterpret_cast<VMConst*>(smem + L::mc_off) = vm_const(g.props + e * g.nProps, g.material == EFE_MAT_VON_MISES);
   tc::cp_async_wait_all();
   __syncthreads();
 
-  // ---- A0: F = I + sum_a U_a (x) dN_a/dX, one thread per (point, component); the float-float
-  // pass keeps H = F - I in float-float
+  // ---- A0: H = sum_a U_a (x) dN_a/dX (U: the increment dU for small strain), one thread per
+  // (point, component); the mixed TL pass keeps F = I + H, the others H
   for (int t = tid; t < NQ * 9; t += NT) {
     const int c = t / NQ, q = t - c * NQ, i = c / 3, j = c - 3 * i;
     const int g0 = j * NN * NQ + q;
@@ -299,15 +304,86 @@ __device__ __forceinline__ void assemble_tile_tl20_tc(const GroupArgs& g, const 
       const double* u = reinterpret_cast<const double*>(smem + L::u_off);
       double h = 0.0;
       for (int a = 0; a < NN; ++a) h += u[a * DIM + i] * sGd[g0 + a * NQ];
-      sF[q * 9 + i * 3 + j] = ((i == j) ? 1.0 : 0.0) + h;
+      sF[q * 9 + i * 3 + j] = ((FORM == TLH && i == j) ? 1.0 : 0.0) + h;
     }
   }
   __syncthreads();
 
-  // ---- A1: the material points.  Warp rot runs the per-point FP64 part (all of it in the mixed
-  // pass; in the mixed-ff pass only the Neo-Hooke scalars, between two float-float sub-phases that
-  // use every thread); meanwhile the other warps scatter the pending K_e of the previous element.
-  if constexpr (FF) {
+  // ---- A1: the material points.  Warp rot runs the per-point FP64 part (all of it for small strain
+  // and in the mixed TL pass; in the mixed-ff TL pass only the Neo-Hooke scalars, between two
+  // float-float sub-phases that use every thread); meanwhile the other warps scatter the pending
+  // K_e of the previous element.
+  if constexpr (FORM == SS3) {
+    // small strain (displacementelement/element.py:318-346): strain increment, von Mises return
+    // map or elasticity (FP64), state, s sigma for the residual, the FP32 tangent record
+    if (rt < 32) {
+      if (rt < NQ) {
+        const int q = rt;
+        const int64_t pt = e * NQ + q;
+        const VMConst& mc = *reinterpret_cast<const VMConst*>(smem + L::mc_off);
+        // de = sym(H), Voigt 11, 22, 33, 12, 13, 23 with engineering shears (element.py:322)
+        double de[6];
+        if constexpr (FF) {
+          const ff* H = reinterpret_cast<const ff*>(sF) + q * 9;
+          de[0] = ff_to_double_bits(H[0]);
+          de[1] = ff_to_double_bits(H[4]);
+          de[2] = ff_to_double_bits(H[8]);
+          de[3] = ff_to_double_bits(ff_sum(H[1], H[3]));
+          de[4] = ff_to_double_bits(ff_sum(H[2], H[6]));
+          de[5] = ff_to_double_bits(ff_sum(H[5], H[7]));
+        } else {
+          const double* H = sF + q * 9;
+          de[0] = H[0];
+          de[1] = H[4];
+          de[2] = H[8];
+          de[3] = H[1] + H[3];
+          de[4] = H[2] + H[6];
+          de[5] = H[5] + H[7];
+        }
+        double sig[6], eps[6], kappa = 0.0;
+        for (int f = 0; f < 6; ++f) {
+          sig[f] = g.stateRef[(int64_t)f * stride + pt];
+          eps[f] = g.stateRef[(int64_t)(6 + f) * stride + pt];
+        }
+        const bool hasM = g.material != EFE_MAT_LINEAR_ELASTIC;
+        if (hasM) kappa = g.stateRef[(int64_t)12 * stride + pt];
+        Tangent3 Tg;
+        bool ok = true;
+        if (g.material == EFE_MAT_VON_MISES)
+          ok = von_mises_3d<true>(mc, sig, de, kappa, Tg);
+        else
+          linear_elastic_3d(mc, sig, de, Tg);
+        for (int f = 0; f < 6; ++f) {
+          g.stateTemp[(int64_t)f * stride + pt] = sig[f];
+          g.stateTemp[(int64_t)(6 + f) * stride + pt] = eps[f] + de[f];
+        }
+        if (hasM) g.stateTemp[(int64_t)12 * stride + pt] = kappa;
+        bool finite = true;
+        for (int f = 0; f < 6; ++f) finite = finite && finite_bits(sig[f]);
+        if (!ok) report(g.status, EFE_STATUS_CUTBACK, g.elementOffset + e, 1);
+        if (!finite) atomicOr(g.status, EFE_STATUS_NONFINITE);
+        const double s = g.geomS[pt];
+        // s sigma (rows 11 12 13 / 12 22 23 / 13 23 33) for the residual r_a = s sigma . G_a
+        const double S3[9] = {sig[0], sig[3], sig[4], sig[3], sig[1], sig[5], sig[4], sig[5], sig[2]};
+        const double N3[9] = {Tg.n[0], Tg.n[3], Tg.n[4], Tg.n[3], Tg.n[1], Tg.n[5], Tg.n[4], Tg.n[5], Tg.n[2]};
+        float* r = rk + q * T::RK;
+        for (int c = 0; c < 9; ++c) {
+          const double pq = s * S3[c];
+          if constexpr (FF)
+            reinterpret_cast<ff*>(smem + L::pq_off)[q * 9 + c] = ff_split_bits(pq);
+          else
+            reinterpret_cast<double*>(smem + L::pq_off)[q * 9 + c] = pq;
+          r[T::R_F + c] = d2f_trunc(N3[c]);
+        }
+        // tangent lambda' G (x) G + mu' (delta G.G + G (x) G swapped) - a (nG) (x) (nG), times s
+        r[T::R_C + 0] = d2f_trunc(Tg.c12 * s);
+        r[T::R_C + 1] = d2f_trunc(Tg.c44 * s);
+        r[T::R_C + 2] = d2f_trunc(Tg.a * s);
+      }
+    } else {
+      tl20_pending_and_next<FF, FORM>(g, prev, next, smem, tb, sps, srl, par, rt - 32, tcs.failed);
+    }
+  } else if constexpr (FF) {
     const ff* sH = reinterpret_cast<const ff*>(sF);
     ff* sA1 = reinterpret_cast<ff*>(tb + T::a1_off);  // [q][E 0-5 | C 6-14 | B 15-20]
     T::A1Scalars* sSc = reinterpret_cast<T::A1Scalars*>(tb + T::a1s_off);
@@ -378,7 +454,7 @@ __device__ __forceinline__ void assemble_tile_tl20_tc(const GroupArgs& g, const 
         sSc[q] = sc;
       }
     } else {
-      tl20_pending_and_next<FF>(g, prev, next, smem, tb, sps, srl, par, rt - 32, tcs.failed);
+      tl20_pending_and_next<FF, FORM>(g, prev, next, smem, tb, sps, srl, par, rt - 32, tcs.failed);
     }
     __syncthreads();
     // A1c: one thread per (point, entry (i, j)): F^-1, s tau F^-T, the FP32 record, state
@@ -484,7 +560,7 @@ __device__ __forceinline__ void assemble_tile_tl20_tc(const GroupArgs& g, const 
         if (!finite) atomicOr(g.status, EFE_STATUS_NONFINITE);
       }
     } else {
-      tl20_pending_and_next<FF>(g, prev, next, smem, tb, sps, srl, par, rt - 32, tcs.failed);
+      tl20_pending_and_next<FF, FORM>(g, prev, next, smem, tb, sps, srl, par, rt - 32, tcs.failed);
     }
   }
   __syncthreads();
@@ -520,23 +596,41 @@ __device__ __forceinline__ void assemble_tile_tl20_tc(const GroupArgs& g, const 
         else
           G[l] = d2f_trunc(sGd[(l * NN + a) * NQ + q]);
       }
-      float h[3], gg[3], th[3];
+      if constexpr (FORM == SS3) {
+        // plain [lambda' G_a, -a nG_a] . [G_b, nG_b], swapped mu' G_b[j] G_a[k], diagonal mu' G_a . G_b
+        float nG[3];
 #pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        h[i] = r[T::R_FI + 0 * 3 + i] * G[0] + r[T::R_FI + 1 * 3 + i] * G[1] + r[T::R_FI + 2 * 3 + i] * G[2];
-        gg[i] = r[T::R_F + i * 3 + 0] * G[0] + r[T::R_F + i * 3 + 1] * G[1] + r[T::R_F + i * 3 + 2] * G[2];
-        th[i] = r[T::R_PQ + i * 3 + 0] * G[0] + r[T::R_PQ + i * 3 + 1] * G[1] + r[T::R_PQ + i * 3 + 2] * G[2];
-      }
-      const float c1s = r[T::R_C + 0], c2s = r[T::R_C + 1], c3s = r[T::R_C + 2], c4s = r[T::R_C + 3];
+        for (int i = 0; i < 3; ++i)
+          nG[i] = r[T::R_F + i * 3 + 0] * G[0] + r[T::R_F + i * 3 + 1] * G[1] + r[T::R_F + i * 3 + 2] * G[2];
+        const float Lq = r[T::R_C + 0], Mq = r[T::R_C + 1], Aq = r[T::R_C + 2];
 #pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        const float bh = r[T::R_B + j * 3 + 0] * h[0] + r[T::R_B + j * 3 + 1] * h[1] + r[T::R_B + j * 3 + 2] * h[2];
-        const int row = 3 * a + j;
-        tc_put2<T::SBO_PS>(tb + T::a_hi, tb + T::a_lo, row, 2 * ql, c2s * h[j] + c3s * bh, c4s * h[j]);
-        tc_put<T::SBO_PS>(tb + T::a_hi, tb + T::a_lo, 64 + row, 2 * ql, c1s * gg[j] - th[j]);
-        tc_put2<T::SBO_PS>(tb + T::b_hi, tb + T::b_lo, row, 2 * ql, h[j], gg[j]);
-        tc_put<T::SBO_D>(tb + T::dA_hi, tb + T::dA_lo, a, 3 * ql + j, c1s * G[j]);
-        tc_put<T::SBO_D>(tb + T::dB_hi, tb + T::dB_lo, a, 3 * ql + j, G[j]);
+        for (int j = 0; j < 3; ++j) {
+          const int row = 3 * a + j;
+          tc_put2<T::SBO_PS>(tb + T::a_hi, tb + T::a_lo, row, 2 * ql, Lq * G[j], -Aq * nG[j]);
+          tc_put<T::SBO_PS>(tb + T::a_hi, tb + T::a_lo, 64 + row, 2 * ql, Mq * G[j]);
+          tc_put2<T::SBO_PS>(tb + T::b_hi, tb + T::b_lo, row, 2 * ql, G[j], nG[j]);
+          tc_put<T::SBO_D>(tb + T::dA_hi, tb + T::dA_lo, a, 3 * ql + j, Mq * G[j]);
+          tc_put<T::SBO_D>(tb + T::dB_hi, tb + T::dB_lo, a, 3 * ql + j, G[j]);
+        }
+      } else {
+        float h[3], gg[3], th[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          h[i] = r[T::R_FI + 0 * 3 + i] * G[0] + r[T::R_FI + 1 * 3 + i] * G[1] + r[T::R_FI + 2 * 3 + i] * G[2];
+          gg[i] = r[T::R_F + i * 3 + 0] * G[0] + r[T::R_F + i * 3 + 1] * G[1] + r[T::R_F + i * 3 + 2] * G[2];
+          th[i] = r[T::R_PQ + i * 3 + 0] * G[0] + r[T::R_PQ + i * 3 + 1] * G[1] + r[T::R_PQ + i * 3 + 2] * G[2];
+        }
+        const float c1s = r[T::R_C + 0], c2s = r[T::R_C + 1], c3s = r[T::R_C + 2], c4s = r[T::R_C + 3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const float bh = r[T::R_B + j * 3 + 0] * h[0] + r[T::R_B + j * 3 + 1] * h[1] + r[T::R_B + j * 3 + 2] * h[2];
+          const int row = 3 * a + j;
+          tc_put2<T::SBO_PS>(tb + T::a_hi, tb + T::a_lo, row, 2 * ql, c2s * h[j] + c3s * bh, c4s * h[j]);
+          tc_put<T::SBO_PS>(tb + T::a_hi, tb + T::a_lo, 64 + row, 2 * ql, c1s * gg[j] - th[j]);
+          tc_put2<T::SBO_PS>(tb + T::b_hi, tb + T::b_lo, row, 2 * ql, h[j], gg[j]);
+          tc_put<T::SBO_D>(tb + T::dA_hi, tb + T::dA_lo, a, 3 * ql + j, c1s * G[j]);
+          tc_put<T::SBO_D>(tb + T::dB_hi, tb + T::dB_lo, a, 3 * ql + j, G[j]);
+        }
       }
     }
     // residual of the chunk's points: P_e[a][j] -= sum_q sum_l Pq[j][l] G_qa[l]

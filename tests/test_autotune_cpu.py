@@ -52,8 +52,8 @@ def test_tuner_picks_caches_and_reuses(tmp_path, monkeypatch):
 
 
 def test_tensor_variant_only_where_the_library_has_it():
-    """Tile variant 3 (the tensor-core tangent) is timed only for Hexa20 3x3x3 total-Lagrangian
-    hyperelastic groups with an FP32 tangent."""
+    """Tile variant 3 (the tensor-core tangent) is timed only for Hexa20 3x3x3 groups, total-Lagrangian
+    hyperelastic or small strain, with an FP32 tangent."""
     from edelweissfe_gb300 import _lib as L
     from edelweissfe_gb300 import autotune
 
@@ -65,7 +65,11 @@ def test_tensor_variant_only_where_the_library_has_it():
     assert autotune.variants_for(asm("C3D20TL", "neohookewa", L.EFE_K_FP64), 0) == (0, 1, 2)
     assert autotune.variants_for(asm("C3D20TL", "vonmises", L.EFE_K_FP32), 0) == (0, 1, 2)
     assert autotune.variants_for(asm("C3D20RTL", "neohookewa", L.EFE_K_FP32), 0) == (0, 1, 2)
-    assert autotune.variants_for(asm("C3D20", "linearelastic", L.EFE_K_FP32), 0) == (0, 1, 2)
+    assert autotune.variants_for(asm("C3D20", "linearelastic", L.EFE_K_FP32), 0) == (0, 1, 2, 3)
+    assert autotune.variants_for(asm("C3D20", "vonmises", L.EFE_K_FP32_FF), 0) == (0, 1, 2, 3)
+    assert autotune.variants_for(asm("C3D20", "vonmises", L.EFE_K_FP64), 0) == (0, 1, 2)
+    assert autotune.variants_for(asm("C3D20R", "vonmises", L.EFE_K_FP32), 0) == (0, 1, 2)
+    assert autotune.variants_for(asm("C3D20TL", "vonmises", L.EFE_K_FP32), 0) == (0, 1, 2)
     assert autotune.variants_for(asm("C3D8TL", "neohookewa", L.EFE_K_FP32), 0) == (0, 1, 2)
 
 

@@ -1,5 +1,6 @@
-"""The Hexa20 total-Lagrangian Neo-Hooke element tangent on the tensor cores (tile variant 3: tcgen05
-TF32 MMAs with a hi/lo split, FP32 accumulation in TMEM) against the reference and the oracle.
+"""The Hexa20 3x3x3 element tangent on the tensor cores (tile variant 3: tcgen05 TF32 MMAs with a hi/lo
+split, FP32 accumulation in TMEM), total-Lagrangian Neo-Hooke and small strain, against the reference
+and the oracle.
 
 * The reference's own fixtures of C3D20TL with Neo-Hooke a, b, c (tests/golden, recorded from
   displacementtlelement/element.py:346-427 and neohookepencegouformulation{a,b,c}.py): P, F and
@@ -151,3 +152,84 @@ def test_tensor_tangent_on_a_block_against_oracle_and_simt(precision):
     assert err <= RTOL_K, f"K vs oracle rel err {err:.3e}"
     assert _rel(K, out[0][2]) <= RTOL_K
     assert _rel(P, out[0][0]) <= RTOL  # the residual does not depend on the tangent's form
+
+
+@pytest.mark.parametrize("precision", ["mixed", "mixed-ff"])
+@pytest.mark.parametrize("name", ["ss_c3d20_li", "ss_c3d20_vmn", "ss_c3d20_vo", "cutback_c3d20_vm"])
+def test_small_strain_tensor_tangent_matches_reference_fixtures(name, precision):
+    """The small-strain Hexa20 3x3x3 form on the tensor cores (lambda' G (x) G - a nG (x) nG plain,
+    mu' G (x) G swapped, mu' G.G diagonal; displacementelement/element.py:318-346 with
+    vonmises.py:186-254 / linearelastic.py): the reference's C3D20 fixtures, elastic and plastic
+    increments with state acceptance, and the cutback request of the reference's own run."""
+    from edelweissfe_gb300 import CutbackRequest, ElementGroup, GPUAssembler
+
+    case = gc.load(name)
+    g = ElementGroup(str(case["elType"]), str(case["kind"]), case["props"], case["conn"], case["thickness"])
+    asm = GPUAssembler(case["coords"], case["node_dof"], int(case["nDof"]), [g], precision=precision)
+    asm._groups_c[0].tileVariant = TC
+    for call in gc.calls(case):
+        if call["accept_before"]:
+            asm.acceptLastState()
+        P, F, K = asm.constructDofVector(), asm.constructDofVector(), asm.constructSystemMatrix()
+        U = torch.tensor(call["U"], device=asm.device)
+        dU = torch.tensor(call["dU"], device=asm.device)
+        if call["raised"] >= 0:
+            with pytest.raises(CutbackRequest) as ei:
+                asm.computeElements(None, U, dU, P, K, F)
+            assert f"element {call['raised']} " in str(ei.value)
+            return
+        if name == "cutback_c3d20_vm":
+            # rounding-critical return map: with the FP32-tangent modes' faster return-map
+            # arithmetic a cutback one call early is an allowed outcome (as in test_gpu_parity)
+            try:
+                asm.computeElements(None, U, dU, P, K, F)
+            except CutbackRequest:
+                return
+        else:
+            asm.computeElements(None, U, dU, P, K, F)
+        assert _rel(P.cpu().numpy(), call["P"]) <= RTOL
+        assert _rel(F.cpu().numpy(), call["F"]) <= RTOL
+        if call["Kdata"] is not None:
+            err = _rel(K.double().cpu().numpy(), call["Kdata"])
+            assert err <= RTOL_K, f"K rel err {err:.3e}"
+        assert _rel(asm.group_state(0), call["state"]) <= RTOL
+
+
+@pytest.mark.parametrize("precision", ["mixed", "mixed-ff"])
+def test_small_strain_tensor_tangent_plastic_block(precision):
+    """A jittered 6 x 5 x 4 C3D20 von Mises block in a plastic increment (per-element yield stress):
+    the tensor-core tangent against the oracle's pass and the SIMT tangent (K 2e-6; P, F, state
+    1e-12, the residual independent of the tangent's form)."""
+    from edelweissfe_gb300 import ElementGroup, GPUAssembler, meshes
+    from oracle.assembly import Model
+
+    coords, conn, nodeDof, nDof = meshes.box(6, 5, 4, lX=1.0, lY=1.0, lZ=0.8, nNodes=20)
+    coords = meshes.jitter(coords, 0.08, [1 / 6, 1 / 5, 0.2], 7, [0, 0, 0], [1, 1, 0.8])
+    rng = np.random.default_rng(13)
+    E = len(conn)
+    props = np.tile([210e3, 0.3, 250.0, 1000.0, 0.0, 0.0], (E, 1))
+    props[:, 2] *= rng.uniform(0.8, 1.2, E)
+    dU = np.zeros(nDof)
+    for c in range(3):
+        dU[nodeDof + c] = coords @ (0.004 * rng.normal(size=3)) + 0.0005 * rng.normal(size=len(coords))
+    model = Model(coords, nodeDof, nDof, [dict(elType="C3D20", kind="vonmises", props=props, conn=conn.astype(np.int64),
+                                               thickness=np.ones(E), order=np.arange(E))])  # fmt: skip
+    ref = model.compute_elements(dU, dU, model.initial_state())
+    assert ref["first_failed_element"] is None
+    st = ref["stateTemp"][0]["state"]
+    assert (st[..., 12] > 0).mean() > 0.2  # a plastic increment
+    out = {}
+    for variant in (TC, 0):
+        asm = GPUAssembler(coords, nodeDof, nDof, [ElementGroup("C3D20", "vonmises", props, conn)], precision=precision)
+        asm._groups_c[0].tileVariant = variant
+        P, F, K = asm.constructDofVector(), asm.constructDofVector(), asm.constructSystemMatrix()
+        d = torch.tensor(dU, device=asm.device)
+        asm.computeElements(None, d, d, P, K, F)
+        out[variant] = (P.cpu().numpy(), F.cpu().numpy(), K.double().cpu().numpy(), asm.group_state(0))
+    P, F, K, S = out[TC]
+    assert _rel(P, ref["P"]) <= RTOL and _rel(F, ref["F"]) <= RTOL
+    assert _rel(S, st) <= RTOL
+    err = _rel(K, ref["Kdata"])
+    assert err <= RTOL_K, f"K vs oracle rel err {err:.3e}"
+    assert _rel(K, out[0][2]) <= RTOL_K
+    assert _rel(P, out[0][0]) <= RTOL
