@@ -36,11 +36,11 @@ template <typename KT> struct TypeOf<1, KT> : TypeOfBase<EFE_HEXA20, EFE_RULE_3D
 template <typename KT> struct TypeOf<2, KT> : TypeOfBase<EFE_HEXA8, EFE_RULE_3D_2X2X2, TLH, KT, 2> {};
 template <typename KT> struct TypeOf<3, KT> : TypeOfBase<EFE_HEXA8, EFE_RULE_3D_2X2X2, SS3, KT, 3> {};
 template <typename KT> struct TypeOf<4, KT> : TypeOfBase<EFE_QUAD8, EFE_RULE_2D_2X2, TLH, KT, 4> {};
-// type 0 with its tangent on the tensor cores (tile variant 3, efe_tl20_tc.cuh; FP32 tangent only)
+// type 0 with its tangent on the tensor cores (tile variant 3, efe_hexa20_tc.cuh; FP32 tangent only)
 template <> struct TypeOf<5, float> {
   using T = PersistentType<EFE_HEXA20, EFE_RULE_3D_3X3X3, TLH, 1, true>;
-  static constexpr size_t bytes = TL20Layout<false>::bytes;
-  static_assert(TL20Layout<false>::bytes == TL20Layout<true>::bytes, "one tile size for both forms");
+  static constexpr size_t bytes = H20TCLayout<false>::bytes;
+  static_assert(H20TCLayout<false>::bytes == H20TCLayout<true>::bytes, "one tile size for both forms");
   static constexpr int NT = 128, SRC = 0;
 };
 
@@ -73,7 +73,7 @@ cudaError_t run_list(const GroupArgs (*groups)[MAX_PERSISTENT_GROUPS], const int
   if ((err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return err;
   // a list with a tensor-core type allocates TMEM (the runtime's occupancy query then answers 1)
   if constexpr ((TypeOf<IDX, KT>::T::TC || ...)) {
-    if ((err = resident_ctas_tmem(kern, NT, bytes, (int)TL20::TMEM_COLS, &perSM)) != cudaSuccess) return err;
+    if ((err = resident_ctas_tmem(kern, NT, bytes, (int)H20TC::TMEM_COLS, &perSM)) != cudaSuccess) return err;
   } else {
     if ((err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, NT, bytes)) != cudaSuccess) return err;
   }

@@ -1,6 +1,10 @@
-// efe_tl20_tc.cuh -- the Hexa20 3x3x3 total-Lagrangian Neo-Hooke element pass with its element
-// tangent on the tensor cores (tile variant 3): one element per 128-thread CTA tile.
+// efe_hexa20_tc.cuh -- the Hexa20 3x3x3 element pass, total-Lagrangian Neo-Hooke or small strain
+// (von Mises, linear elastic), with its element tangent on the tensor cores (tile variant 3): one
+// element per 128-thread CTA tile.
 //
+// The small-strain tangent (displacementelement/element.py:342) has the same three kinds of terms
+// as the one below, with G for h and g: lambda' G_a[j] G_b[k] - a (nG_a)[j] (nG_b)[k] plain,
+// mu' G_b[j] G_a[k] swapped, mu' G_a . G_b on the node-pair diagonal.
 // The tangent of the TL Neo-Hooke form (displacementtlelement/element.py:408-412 in closed form) is,
 // with per-point scalars c1s..c4s and per-node vectors G = dN/dX, h = F^-T G, g = F G,
 // p = c1s g - s tau h, q = c2s h + c3s B h,
@@ -32,7 +36,7 @@
 
 namespace efe {
 
-struct TL20 {
+struct H20TC {
   static constexpr int NN = 20, NQ = 27, NDOF = 60, QC = 9, NCH = 3;
   static constexpr int RK = 44;  // floats per point of the FP32 record (16-byte rows)
   // FP32 record offsets: F, F^-1 (row-major, F^-1[l][m] at 3l+m), B = F F^T, Pq = s tau F^-T,
@@ -69,8 +73,8 @@ struct TL20 {
 };
 
 template <bool FF>
-struct TL20Layout {
-  using T = TL20;
+struct H20TCLayout {
+  using T = H20TC;
   static constexpr size_t u_off = 0;                                          // ff or double [NN][3]
   static constexpr size_t f_off = u_off + 8 * T::NN * 3;                      // double [NQ][9]: F
   static constexpr size_t pq_off = f_off + 8 * T::NQ * 9;                     // ff or double [NQ][9]: s tau F^-T
@@ -116,9 +120,9 @@ __device__ __forceinline__ void tc_put2(unsigned char* hi, unsigned char* lo, in
 // K_e of element e (the accumulators copied to the tile's shared memory by its epilogue) into the
 // CSR data: Ke[(a,j),(b,k)] at row dof(b,k), column dof(a,j) = slot(a,b) + k rowLen(b) + j, with the
 // element's staged pair slots sps and row lengths srl, by threads ti = 0 .. nth - 1.
-__device__ __forceinline__ void tl20_scatter(const GroupArgs& g, int64_t e, const unsigned char* tb, const int* sps,
+__device__ __forceinline__ void h20tc_scatter(const GroupArgs& g, int64_t e, const unsigned char* tb, const int* sps,
                                              const int* srl, int ti, int nth) {
-  using T = TL20;
+  using T = H20TC;
   constexpr int NN = T::NN;
   const float* sP = reinterpret_cast<const float*>(tb + T::sP);
   const float* sX = reinterpret_cast<const float*>(tb + T::sX);
@@ -139,12 +143,12 @@ __device__ __forceinline__ void tl20_scatter(const GroupArgs& g, int64_t e, cons
 }
 
 // Stage element e into shared memory, in two parts that complete after tc::cp_async_wait_all:
-// tl20_stage_g (every thread): dN/dX by cp.async; tl20_stage_small (threads li = 0 .. nth - 1,
+// h20tc_stage_g (every thread): dN/dX by cp.async; h20tc_stage_small (threads li = 0 .. nth - 1,
 // nth >= NN): the pair slots by cp.async into buffer par, U and the row lengths by plain loads.
 template <bool FF>
-__device__ __forceinline__ void tl20_stage_g(const GroupArgs& g, int64_t e, unsigned char* smem) {
-  using T = TL20;
-  using L = TL20Layout<FF>;
+__device__ __forceinline__ void h20tc_stage_g(const GroupArgs& g, int64_t e, unsigned char* smem) {
+  using T = H20TC;
+  using L = H20TCLayout<FF>;
   constexpr int NT = 128, NQ = T::NQ;
   const int64_t stride = g.nElements * NQ;
   for (int t = threadIdx.x; t < T::NDOF * NQ; t += NT) {
@@ -158,18 +162,18 @@ __device__ __forceinline__ void tl20_stage_g(const GroupArgs& g, int64_t e, unsi
     }
   }
 }
-// The small per-element data of tl20_stage_small, loaded into registers first (so that the
+// The small per-element data of h20tc_stage_small, loaded into registers first (so that the
 // latency of the dependent loads can overlap other work) and stored later.
-struct TL20Small {
+struct H20TCSmall {
   int32_t rowLen;
   double u[3];
   bool valid;
 };
 template <bool FF, int FORM>
-__device__ __forceinline__ TL20Small tl20_load_small(const GroupArgs& g, int64_t e, int a) {
-  constexpr int NN = TL20::NN, DIM = 3;
+__device__ __forceinline__ H20TCSmall h20tc_load_small(const GroupArgs& g, int64_t e, int a) {
+  constexpr int NN = H20TC::NN, DIM = 3;
   const double* Ux = FORM == SS3 ? g.dU : g.U;  // small strain: the increment; TL: the total
-  TL20Small r{0, {0.0, 0.0, 0.0}, false};
+  H20TCSmall r{0, {0.0, 0.0, 0.0}, false};
   const int32_t node = g.conn[e * NN + a];
   if (!in_bounds(g, node, g.nNodes, e)) return r;
   r.rowLen = g.nodeRowLen[node];
@@ -188,9 +192,9 @@ __device__ __forceinline__ TL20Small tl20_load_small(const GroupArgs& g, int64_t
   return r;
 }
 template <bool FF>
-__device__ __forceinline__ void tl20_store_small(const TL20Small& r, unsigned char* smem, int par, int a) {
-  using L = TL20Layout<FF>;
-  constexpr int NN = TL20::NN, DIM = 3;
+__device__ __forceinline__ void h20tc_store_small(const H20TCSmall& r, unsigned char* smem, int par, int a) {
+  using L = H20TCLayout<FF>;
+  constexpr int NN = H20TC::NN, DIM = 3;
   reinterpret_cast<int*>(smem + L::rl_off)[par * NN + a] = r.rowLen;
   if (!r.valid) return;
   for (int c = 0; c < DIM; ++c) {
@@ -201,13 +205,13 @@ __device__ __forceinline__ void tl20_store_small(const TL20Small& r, unsigned ch
   }
 }
 template <bool FF, int FORM>
-__device__ __forceinline__ void tl20_stage_small(const GroupArgs& g, int64_t e, unsigned char* smem, int par, int li,
+__device__ __forceinline__ void h20tc_stage_small(const GroupArgs& g, int64_t e, unsigned char* smem, int par, int li,
                                                  int nth) {
-  using L = TL20Layout<FF>;
-  constexpr int NN = TL20::NN;
+  using L = H20TCLayout<FF>;
+  constexpr int NN = H20TC::NN;
   int* sps = reinterpret_cast<int*>(smem + L::ps_off) + par * NN * NN;
   for (int t = li; t < NN * NN; t += nth) tc::cp_async4(sps + t, g.pairSlot + e * NN * NN + t);
-  if (li < NN) tl20_store_small<FF>(tl20_load_small<FF, FORM>(g, e, li), smem, par, li);
+  if (li < NN) h20tc_store_small<FF>(h20tc_load_small<FF, FORM>(g, e, li), smem, par, li);
 }
 
 // the float-float forms used by the per-point update of the mixed-ff pass
@@ -229,42 +233,42 @@ __device__ __forceinline__ ff ff_det2(ff a, ff b, ff c, ff d) {
 // row lengths in buffer par ^ 1, U of this element already consumed), then -- once all three
 // warps are past the scatter -- store the next element's small data into buffer par ^ 1.
 template <bool FF, int FORM>
-__device__ __forceinline__ void tl20_pending_and_next(const GroupArgs& g, int64_t prev, int64_t next, unsigned char* smem,
+__device__ __forceinline__ void h20tc_pending_and_next(const GroupArgs& g, int64_t prev, int64_t next, unsigned char* smem,
                                                       const unsigned char* tb, const int* sps, const int* srl, int par,
                                                       int li, bool failed) {
-  using L = TL20Layout<FF>;
-  constexpr int NN = TL20::NN, NTH = 96;
-  TL20Small nx{0, {0.0, 0.0, 0.0}, false};
-  if (next >= 0 && li < NN) nx = tl20_load_small<FF, FORM>(g, next, li);
-  if (prev >= 0 && !failed) tl20_scatter(g, prev, tb, sps + (par ^ 1) * NN * NN, srl + (par ^ 1) * NN, li, NTH);
+  using L = H20TCLayout<FF>;
+  constexpr int NN = H20TC::NN, NTH = 96;
+  H20TCSmall nx{0, {0.0, 0.0, 0.0}, false};
+  if (next >= 0 && li < NN) nx = h20tc_load_small<FF, FORM>(g, next, li);
+  if (prev >= 0 && !failed) h20tc_scatter(g, prev, tb, sps + (par ^ 1) * NN * NN, srl + (par ^ 1) * NN, li, NTH);
   if (next >= 0) {
     asm volatile("bar.sync 1, %0;" ::"n"(NTH) : "memory");
     int* nps = reinterpret_cast<int*>(smem + L::ps_off) + (par ^ 1) * NN * NN;
     for (int t = li; t < NN * NN; t += NTH) tc::cp_async4(nps + t, g.pairSlot + next * NN * NN + t);
-    if (li < NN) tl20_store_small<FF>(nx, smem, par ^ 1, li);
+    if (li < NN) h20tc_store_small<FF>(nx, smem, par ^ 1, li);
   }
 }
 
-// how a tile call scatters K_e (the prev argument of assemble_tile_tl20_tc)
-constexpr int64_t TL20_DEFER_NONE = -1;  // defer this element's K_e; nothing pending from before
-constexpr int64_t TL20_NOW = -2;         // scatter this element's K_e at the end of the call
+// how a tile call scatters K_e (the prev argument of assemble_tile_h20tc)
+constexpr int64_t H20TC_DEFER_NONE = -1;  // defer this element's K_e; nothing pending from before
+constexpr int64_t H20TC_NOW = -2;         // scatter this element's K_e at the end of the call
 
 // One element e of group g; every thread of the CTA (NT = 128) calls it.  tcs: the CTA's TMEM
-// columns (TL20::TMEM_COLS) and MMA-completion mbarrier.  rot (0-3): the warp that runs the
+// columns (H20TC::TMEM_COLS) and MMA-completion mbarrier.  rot (0-3): the warp that runs the
 // per-point material update; warp w of every CTA sits on the same SM sub-partition, so the caller
 // varies rot between the CTAs that share an SM.  par: the pair-slot buffer of this element
 // (alternate between consecutive calls).
-// prev == TL20_NOW: K_e is scattered at the end of the call.  Otherwise K_e stays pending in shared
+// prev == H20TC_NOW: K_e is scattered at the end of the call.  Otherwise K_e stays pending in shared
 // memory, and prev >= 0 is the previous call's pending element (same group), scattered by the
 // three other warps while one warp runs this element's material update; after the last call the
-// caller scatters the pending one (tl20_scatter).  next >= 0: the element of the next call, staged
+// caller scatters the pending one (h20tc_scatter).  next >= 0: the element of the next call, staged
 // while this element's last MMAs run; staged: this element was staged that way by the previous call.
 template <bool FF, int FORM>
-__device__ __forceinline__ void assemble_tile_tl20_tc(const GroupArgs& g, const int64_t e, unsigned char* smem,
+__device__ __forceinline__ void assemble_tile_h20tc(const GroupArgs& g, const int64_t e, unsigned char* smem,
                                                       TCState& tcs, int rot, int64_t prev, int64_t next, bool staged,
                                                       int par) {
-  using T = TL20;
-  using L = TL20Layout<FF>;
+  using T = H20TC;
+  using L = H20TCLayout<FF>;
   constexpr int NT = 128, NN = T::NN, NQ = T::NQ, DIM = 3;
   const int tid = threadIdx.x;
   const int rt = (tid - 32 * (rot & 3)) & (NT - 1);  // thread index with warp rot first
@@ -281,8 +285,8 @@ __device__ __forceinline__ void assemble_tile_tl20_tc(const GroupArgs& g, const 
 
   // ---- phase 0: this element's dN/dX, pair slots, U and row lengths in shared memory
   if (!staged) {
-    tl20_stage_g<FF>(g, e, smem);
-    tl20_stage_small<FF, FORM>(g, e, smem, par, rt, NT);
+    h20tc_stage_g<FF>(g, e, smem);
+    h20tc_stage_small<FF, FORM>(g, e, smem, par, rt, NT);
   }
   // small strain: the element's von Mises / elasticity constants, once per element
   if (FORM == SS3 && tid == NT - 1)
@@ -381,7 +385,7 @@ __device__ __forceinline__ void assemble_tile_tl20_tc(const GroupArgs& g, const 
         r[T::R_C + 2] = d2f_trunc(Tg.a * s);
       }
     } else {
-      tl20_pending_and_next<FF, FORM>(g, prev, next, smem, tb, sps, srl, par, rt - 32, tcs.failed);
+      h20tc_pending_and_next<FF, FORM>(g, prev, next, smem, tb, sps, srl, par, rt - 32, tcs.failed);
     }
   } else if constexpr (FF) {
     const ff* sH = reinterpret_cast<const ff*>(sF);
@@ -454,7 +458,7 @@ __device__ __forceinline__ void assemble_tile_tl20_tc(const GroupArgs& g, const 
         sSc[q] = sc;
       }
     } else {
-      tl20_pending_and_next<FF, FORM>(g, prev, next, smem, tb, sps, srl, par, rt - 32, tcs.failed);
+      h20tc_pending_and_next<FF, FORM>(g, prev, next, smem, tb, sps, srl, par, rt - 32, tcs.failed);
     }
     __syncthreads();
     // A1c: one thread per (point, entry (i, j)): F^-1, s tau F^-T, the FP32 record, state
@@ -560,7 +564,7 @@ __device__ __forceinline__ void assemble_tile_tl20_tc(const GroupArgs& g, const 
         if (!finite) atomicOr(g.status, EFE_STATUS_NONFINITE);
       }
     } else {
-      tl20_pending_and_next<FF, FORM>(g, prev, next, smem, tb, sps, srl, par, rt - 32, tcs.failed);
+      h20tc_pending_and_next<FF, FORM>(g, prev, next, smem, tb, sps, srl, par, rt - 32, tcs.failed);
     }
   }
   __syncthreads();
@@ -651,7 +655,7 @@ __device__ __forceinline__ void assemble_tile_tl20_tc(const GroupArgs& g, const 
     __syncthreads();
     // after the last chunk's operands and residual the staged dN/dX is dead: stage the next
     // element's while the MMAs run
-    if (ch == T::NCH - 1 && next >= 0) tl20_stage_g<FF>(g, next, smem);
+    if (ch == T::NCH - 1 && next >= 0) h20tc_stage_g<FF>(g, next, smem);
     if (tid == 0 && !tcs.failed) {
       tc::fence_after_sync();
       constexpr uint32_t idPS = tc::idesc_tf32(128, 64), idD = tc::idesc_tf32(128, 32);
@@ -740,7 +744,7 @@ __device__ __forceinline__ void assemble_tile_tl20_tc(const GroupArgs& g, const 
       }
     }
   }
-  if (prev == TL20_NOW && !tcs.failed) tl20_scatter(g, e, tb, sps + par * NN * NN, srl + par * NN, tid, NT);
+  if (prev == H20TC_NOW && !tcs.failed) h20tc_scatter(g, e, tb, sps + par * NN * NN, srl + par * NN, tid, NT);
 }
 
 }  // namespace efe

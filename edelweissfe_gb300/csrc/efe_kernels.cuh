@@ -917,16 +917,16 @@ __global__ void __launch_bounds__(NT, MINB) assemble_kernel(GroupArgs g) {
 // end, after a bounded wait for MMAs still in flight if a wait expired, warp 0 frees the columns.
 }  // namespace efe
 
-#include "efe_tl20_tc.cuh"
+#include "efe_hexa20_tc.cuh"
 
 namespace efe {
 
 // Set-up and tear-down of the tensor-core state of a CTA (every thread calls both): the mbarrier
-// of MMA completion and TL20::TMEM_COLS TMEM columns allocated by warp 0; at the end, after a
+// of MMA completion and H20TC::TMEM_COLS TMEM columns allocated by warp 0; at the end, after a
 // bounded wait for MMAs still in flight if a wait expired, warp 0 frees the columns.
 __device__ __forceinline__ TCState tc_begin(uint64_t* mbar, uint32_t* slot) {
   if (threadIdx.x == 0) tc::mbar_init(mbar, 1);
-  if (threadIdx.x < 32) tc::tmem_alloc(slot, TL20::TMEM_COLS);
+  if (threadIdx.x < 32) tc::tmem_alloc(slot, H20TC::TMEM_COLS);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -936,11 +936,11 @@ __device__ __forceinline__ void tc_end(TCState& tcs) {
   if (tcs.failed) tc::mbar_wait(tcs.mbar, tcs.phase, TC_WAIT_LIMIT);
   tc::fence_before_sync();
   __syncthreads();
-  if (threadIdx.x < 32) tc::tmem_dealloc(tcs.tmem, TL20::TMEM_COLS);
+  if (threadIdx.x < 32) tc::tmem_dealloc(tcs.tmem, H20TC::TMEM_COLS);
 }
 
 // Tile variant 3, the Hexa20 3x3x3 pass (total-Lagrangian Neo-Hooke or small strain) with the
-// tensor-core tangent (efe_tl20_tc.cuh): a grid of resident CTAs (sms per wave), one element per tile, tiles strided by
+// tensor-core tangent (efe_hexa20_tc.cuh): a grid of resident CTAs (sms per wave), one element per tile, tiles strided by
 // the grid; each CTA allocates its TMEM columns once and frees them at the end.  The CTAs of one
 // wave share no SM, so the wave index picks the warp of the per-point update.  Each element's
 // K_e scatter runs during the next element's material update (the last one after the loop).
@@ -951,17 +951,17 @@ __global__ void __launch_bounds__(128, 3) assemble_kernel_tc(GroupArgs g, int sm
   __shared__ uint32_t slot;
   TCState tcs = tc_begin(&mbar, &slot);
   int rot = (int)(blockIdx.x / (unsigned)sms), par = 0;
-  int64_t prev = TL20_DEFER_NONE;  // the element whose K_e is pending in shared memory
+  int64_t prev = H20TC_DEFER_NONE;  // the element whose K_e is pending in shared memory
   for (int64_t e = blockIdx.x; e < g.nElements; e += gridDim.x, ++rot, par ^= 1) {
     const int64_t next = e + gridDim.x < g.nElements ? e + gridDim.x : -1;
-    assemble_tile_tl20_tc<FF, FORM>(g, e, smem, tcs, rot, prev, next, prev >= 0, par);
+    assemble_tile_h20tc<FF, FORM>(g, e, smem, tcs, rot, prev, next, prev >= 0, par);
     prev = e;
     __syncthreads();
   }
   if (prev >= 0 && !tcs.failed) {
-    using L = TL20Layout<FF>;
-    tl20_scatter(g, prev, smem + L::tc_off, reinterpret_cast<const int*>(smem + L::ps_off) + (par ^ 1) * TL20::NN * TL20::NN,
-                 reinterpret_cast<const int*>(smem + L::rl_off) + (par ^ 1) * TL20::NN, threadIdx.x, 128);
+    using L = H20TCLayout<FF>;
+    h20tc_scatter(g, prev, smem + L::tc_off, reinterpret_cast<const int*>(smem + L::ps_off) + (par ^ 1) * H20TC::NN * H20TC::NN,
+                 reinterpret_cast<const int*>(smem + L::rl_off) + (par ^ 1) * H20TC::NN, threadIdx.x, 128);
   }
   tc_end(tcs);
 }
@@ -1010,7 +1010,7 @@ __device__ __forceinline__ bool persistent_tile(const GroupTables<N>& tabs, long
     int k = 0;
     while (t >= tb.tileStart[k + 1]) ++k;
     if constexpr (T0::TC)
-      assemble_tile_tl20_tc<FF, T0::FORM>(tb.g[k], (int64_t)(t - tb.tileStart[k]), smem, *tcs, rot, TL20_NOW, -1, false,
+      assemble_tile_h20tc<FF, T0::FORM>(tb.g[k], (int64_t)(t - tb.tileStart[k]), smem, *tcs, rot, H20TC_NOW, -1, false,
                                           0);
     else
       assemble_tile<T0::SHAPE, T0::RULE, T0::FORM, KT, T0::EPB, NT, FF>(tb.g[k], (int64_t)(t - tb.tileStart[k]) * T0::EPB,

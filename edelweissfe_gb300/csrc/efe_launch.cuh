@@ -80,7 +80,7 @@ cudaError_t resident_ctas_tmem(K kern, int nt, size_t dynBytes, int tmemCols, in
 template <bool FF, int FORM>
 cudaError_t launch_assemble_tc(const GroupArgs& g, cudaStream_t st) {
   constexpr int NT = 128;
-  constexpr size_t bytes = TL20Layout<FF>::bytes;
+  constexpr size_t bytes = H20TCLayout<FF>::bytes;
   static_assert(bytes <= 74 * 1024, "three tensor-core tiles must fit in one SM");
   auto kern = assemble_kernel_tc<FF, FORM>;
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
@@ -92,7 +92,7 @@ cudaError_t launch_assemble_tc(const GroupArgs& g, cudaStream_t st) {
   int dev = 0, sms = 0, perSM = 0;
   if ((err = cudaGetDevice(&dev)) != cudaSuccess) return err;
   if ((err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return err;
-  if ((err = resident_ctas_tmem(kern, NT, bytes, (int)TL20::TMEM_COLS, &perSM)) != cudaSuccess) return err;
+  if ((err = resident_ctas_tmem(kern, NT, bytes, (int)H20TC::TMEM_COLS, &perSM)) != cudaSuccess) return err;
   int64_t grid = (int64_t)sms * perSM;
   if (grid > g.nElements) grid = g.nElements;
   if (grid == 0) return cudaSuccess;
