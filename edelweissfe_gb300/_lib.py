@@ -10,7 +10,7 @@ import os
 from . import _build
 
 # constants of include/efe_gb300.h
-EFE_ABI_VERSION = 2
+EFE_ABI_VERSION = 3
 EFE_QUAD4, EFE_QUAD8, EFE_HEXA8, EFE_HEXA20 = 0, 1, 2, 3
 EFE_RULE_2D_1, EFE_RULE_2D_2X2, EFE_RULE_2D_3X3 = 0, 1, 2
 EFE_RULE_3D_1, EFE_RULE_3D_2X2X2, EFE_RULE_3D_3X3X3 = 3, 4, 5
@@ -193,7 +193,7 @@ def load(build_if_missing=False):
     lib.efe_adjoint_tl.restype = i32
     lib.efe_adjoint_tl.argtypes = [ctypes.POINTER(EfeMesh), ctypes.POINTER(EfeGroup), P, P, P, P, P]
     lib.efe_adjoint_small_strain.restype = i32
-    lib.efe_adjoint_small_strain.argtypes = [ctypes.POINTER(EfeMesh), ctypes.POINTER(EfeGroup), P, P, P, P, P, P, P, P]
+    lib.efe_adjoint_small_strain.argtypes = [ctypes.POINTER(EfeMesh), ctypes.POINTER(EfeGroup), P, P, P, P, P, P, P, P, P]
     lib.efe_compute_elements_persistent.restype = i32
     lib.efe_compute_elements_persistent.argtypes = [ctypes.POINTER(EfeWorkItem), i32, i32, P, P, P]
     lib.efe_compute_elements_persistent_noalloc.restype = i32

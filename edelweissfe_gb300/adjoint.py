@@ -152,11 +152,13 @@ class PathAdjoint:
             asm.adjointSmallStrain(gi, ck["states"][gi], ck["dU"], out, Pbar=v)
         return -out
 
-    def gradient(self, dirichletDofs, cP=None, cU=None, timing=None):
-        """dJ/dprops per group ([E, nProps] tensors) for J = cP . P_N + cU . u_N.  With a dict as
-        `timing`, the device time of the element work (tangent recomputation and the two reverse
-        passes per increment) and of the adjoint solves is added to timing["kernel_ms"] and
-        timing["solve_ms"] (CUDA events on the current stream)."""
+    def gradient(self, dirichletDofs, cP=None, cU=None, timing=None, coordinates=False):
+        """dJ/dprops per group ([E, nProps] tensors) for J = cP . P_N + cU . u_N; with
+        coordinates=True, (that list, dJ/dX) with dJ/dX [nNodes, dim] in the node order of the
+        assembler's coordinates (the prescribed displacements and the nodal loads held fixed).
+        With a dict as `timing`, the device time of the element work (tangent recomputation and the
+        two reverse passes per increment) and of the adjoint solves is added to timing["kernel_ms"]
+        and timing["solve_ms"] (CUDA events on the current stream)."""
 
         def event():
             if timing is None:
@@ -177,6 +179,7 @@ class PathAdjoint:
         gP = [torch.zeros((len(g.conn), g._dev["props"].shape[1]), dtype=torch.float64, device=dev)
               for g in asm.groups]  # fmt: skip
         carry = asm.constructDofVector()
+        gX = torch.zeros((asm.nNodes, asm.dim), dtype=torch.float64, device=dev) if coordinates else None
         self.linearIterations = []
         N = len(self.checkpoints)
         for n in reversed(range(N)):
@@ -191,7 +194,7 @@ class PathAdjoint:
             sprev = [torch.zeros_like(s) for s in sbar]
             for gi in range(len(asm.groups)):
                 asm.adjointSmallStrain(gi, ck["states"][gi], ck["dU"], a, Pbar=cP if last else None,
-                                       stateBarIn=sbar[gi], stateBarOut=sprev[gi], gProps=gP[gi])  # fmt: skip
+                                       stateBarIn=sbar[gi], stateBarOut=sprev[gi], gProps=gP[gi], gX=gX)  # fmt: skip
             e1 = event()
             rhs = a + carry
             if last and cU is not None:
@@ -218,7 +221,7 @@ class PathAdjoint:
             b = asm.constructDofVector()
             for gi in range(len(asm.groups)):
                 asm.adjointSmallStrain(gi, ck["states"][gi], ck["dU"], b, Pbar=lam, stateBarOut=sprev[gi],
-                                       gProps=gP[gi])  # fmt: skip
+                                       gProps=gP[gi], gX=gX)  # fmt: skip
             e3 = event()
             marks.append((e0, e1, e2, e3))
             carry = -(a + b)
@@ -230,4 +233,4 @@ class PathAdjoint:
             timing["kernel_ms"] = timing.get("kernel_ms", 0.0) + sum(
                 a.elapsed_time(b) + c.elapsed_time(d) for a, b, c, d in marks)
             timing["solve_ms"] = timing.get("solve_ms", 0.0) + sum(b.elapsed_time(c) for a, b, c, d in marks)
-        return gP
+        return (gP, gX) if coordinates else gP

@@ -355,11 +355,12 @@ class GPUAssembler:
         return gX, gP
 
     def adjointSmallStrain(self, group, stateBefore, dU, dUbar, Pbar=None, stateBarIn=None, stateBarOut=None,
-                           gProps=None):
+                           gProps=None, gX=None):
         """Reverse mode of one small-strain pass of a group (efe_adjoint_small_strain): accumulates
-        into dUbar [nDof], stateBarOut ([S, nPts], optional) and gProps ([E, nProps], optional) the
-        adjoints of dU, of the state before the increment and of the properties, given the seeds
-        stateBarIn (adjoint of the new state) and Pbar (adjoint of the residual P)."""
+        into dUbar [nDof], stateBarOut ([S, nPts], optional), gProps ([E, nProps], optional) and gX
+        ([nNodes, dim], optional) the adjoints of dU, of the state before the increment, of the
+        properties and of the nodal coordinates, given the seeds stateBarIn (adjoint of the new
+        state) and Pbar (adjoint of the residual P)."""
 
         def ptr(t):
             return None if t is None else ctypes.c_void_p(t.data_ptr())
@@ -367,7 +368,7 @@ class GPUAssembler:
         L.check(
             self.lib.efe_adjoint_small_strain(
                 ctypes.byref(self.mesh), ctypes.byref(self._groups_c[group]), ptr(stateBefore), ptr(dU), ptr(Pbar),
-                ptr(stateBarIn), ptr(stateBarOut), ptr(dUbar), ptr(gProps), self._stream(),
+                ptr(stateBarIn), ptr(stateBarOut), ptr(dUbar), ptr(gProps), ptr(gX), self._stream(),
             ),
             "efe_adjoint_small_strain",
         )  # fmt: skip

@@ -383,7 +383,7 @@ int32_t efe_adjoint_tl(const EfeMesh* mesh, const EfeGroup* g, const double* U, 
 
 int32_t efe_adjoint_small_strain(const EfeMesh* mesh, const EfeGroup* g, const double* stateBefore, const double* dU,
                                  const double* Pbar, const double* stateBarIn, double* stateBarOut, double* dUbar,
-                                 double* gProps, void* stream) {
+                                 double* gProps, double* gX, void* stream) {
   if (!mesh || !g || !stateBefore || !dU || !dUbar) return fail(EFE_ERR_ARGUMENT, "null argument");
   int32_t rc = check_group(mesh, *g);
   if (rc) return rc;
@@ -414,6 +414,11 @@ int32_t efe_adjoint_small_strain(const EfeMesh* mesh, const EfeGroup* g, const d
   a.barOut = stateBarOut;
   a.dUbar = dUbar;
   a.gProps = gProps;
+  a.gX = gX;
+  a.coords = mesh->coords;
+  if (gX && !mesh->coords) return fail(EFE_ERR_ARGUMENT, "coordinate adjoints need the mesh coordinates");
+  static const efe::Hexa20Fix fix = hexa20_fix();
+  a.fix = fix;
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e = cudaErrorInvalidValue;
   switch (g->shape) {

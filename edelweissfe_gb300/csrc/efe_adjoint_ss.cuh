@@ -11,6 +11,11 @@
 // so the derivatives are those of the exact return map, consistent with the reference's
 // consistent tangent (vonmises.py:241-251).
 //
+// With gX, also the adjoint of the nodal coordinates: per point, G = dN/dX enters de = B dU and
+// the residual, s = det J w t the residual; Gbar_a = sym(deBar) u_a - s sigma PBar_a and
+// sBar = -sigma : (B PBar), and through G = J^-1 D (D = J G, J = D' X with the Hexa20 quirk row in
+// D'): Xbar_a = -M^T G_a + s sBar G_a (+ the quirk row's term), M = sum_a Gbar_a (x) G_a.
+//
 // Tile layout as the forward pass: EPB elements per CTA; phase 0 gathers dU_e and PBar_e, phase A
 // runs one thread per point, phase C reduces the per-point contributions per DOF (one atomic per
 // element DOF) and per property (plain stores: one thread owns an element's property).
@@ -110,6 +115,91 @@ __device__ inline void hypo3d_reverse(const VMConst& c, double E, double nu, boo
              Gbar * G / (1.0 + nu);
 }
 
+// Coordinate adjoint of one point (see the head comment), accumulated into a.gX.  u and pb: the
+// element's dU and PBar as staged by phase 0 (float-float relative to node 0 in the FF form, which
+// leaves M unchanged: sum_a G_a = 0).
+template <int SHAPE, int RULE, bool FF>
+__device__ __forceinline__ void coordinate_adjoint(const SSAdjointArgs& a, int64_t e, int q, int64_t pt, int64_t stride,
+                                                   double s, const VMConst& mc, bool vm, const double sig0[6], double k0,
+                                                   const double de[6], const double deBar[6], const double bp[6],
+                                                   const double* u, const double* pb) {
+  constexpr int DIM = ShapeInfo<SHAPE>::DIM, NN = ShapeInfo<SHAPE>::NN;
+  // the new stress (the FP64 form of the forward update)
+  double sn[6], kn = k0;
+  for (int f = 0; f < 6; ++f) sn[f] = sig0[f];
+  Tangent3 Tt;
+  if (vm)
+    von_mises_3d<false>(mc, sn, de, kn, Tt);
+  else
+    linear_elastic_3d(mc, sn, de, Tt);
+  // Voigt 11, 22, 33, 12, 13, 23 (engineering shears in de, bp) as symmetric matrices
+  const double S[3][3] = {{sn[0], sn[3], sn[4]}, {sn[3], sn[1], sn[5]}, {sn[4], sn[5], sn[2]}};
+  const double Db[3][3] = {{deBar[0], deBar[3], deBar[4]}, {deBar[3], deBar[1], deBar[5]},
+                           {deBar[4], deBar[5], deBar[2]}};
+  double sBar = 0.0;
+  if constexpr (DIM == 3) {
+    for (int f = 0; f < 6; ++f) sBar -= sn[f] * bp[f];
+  } else {
+    sBar = -(sn[0] * bp[0] + sn[1] * bp[1] + sn[3] * bp[3]);
+  }
+  auto val = [&](const double* arr, int k) {
+    if constexpr (FF)
+      return ff_to_double(reinterpret_cast<const ff*>(arr)[k]);
+    else
+      return arr[k];
+  };
+  double M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int n = 0; n < NN; ++n) {
+    double G[3], ua[3], pa[3], Gb[3];
+    for (int c = 0; c < DIM; ++c) {
+      G[c] = a.geomG[(int64_t)(c * NN + n) * stride + pt];
+      ua[c] = val(u, n * DIM + c);
+      pa[c] = val(pb, n * DIM + c);
+    }
+    for (int k = 0; k < DIM; ++k) {
+      double v = 0.0;
+      for (int l = 0; l < DIM; ++l) v += Db[k][l] * ua[l] - s * S[k][l] * pa[l];
+      Gb[k] = v;
+    }
+    for (int k = 0; k < DIM; ++k)
+      for (int c = 0; c < DIM; ++c) M[k][c] += Gb[k] * G[c];
+  }
+  // the Hexa20 quirk row of J (J[2][c] += (zeta - xi) sum_a r_a X_a[c]): Jbar[2][c] feeds it
+  double Jb2[3] = {0, 0, 0}, qk = 0.0;
+  if constexpr (SHAPE == EFE_HEXA20) {
+    double xi, eta, zeta, w;
+    quadrature_point(RULE, q, xi, eta, zeta, w);
+    qk = zeta - xi;
+    const double p[3] = {eta, xi, zeta};
+    double D[3][NN];
+    shape_derivatives<SHAPE>(p, D);
+    double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int n = 0; n < NN; ++n) {
+      const int32_t node = a.conn[e * NN + n];
+      for (int c = 0; c < 3; ++c) {
+        const double x = a.coords[(int64_t)node * 3 + c];
+        for (int r = 0; r < 3; ++r) J[r][c] += (D[r][n] + (r == 2 ? qk * a.fix.r[n] : 0.0)) * x;
+      }
+    }
+    double iJ[3][3];
+    inv3(J, det3(J), iJ);
+    for (int c = 0; c < 3; ++c) {
+      double v = s * sBar * iJ[c][2];
+      for (int k = 0; k < 3; ++k) v -= iJ[k][2] * M[k][c];
+      Jb2[c] = v;
+    }
+  }
+  for (int n = 0; n < NN; ++n) {
+    const int32_t node = a.conn[e * NN + n];
+    for (int c = 0; c < DIM; ++c) {
+      double v = s * sBar * a.geomG[(int64_t)(c * NN + n) * stride + pt];
+      for (int k = 0; k < DIM; ++k) v -= M[k][c] * a.geomG[(int64_t)(k * NN + n) * stride + pt];
+      if constexpr (SHAPE == EFE_HEXA20) v += qk * a.fix.r[n] * Jb2[c];
+      atomicAdd(a.gX + (int64_t)node * DIM + c, v);
+    }
+  }
+}
+
 template <int SHAPE, int RULE>
 struct SSAdjointTile {
   static constexpr int DIM = ShapeInfo<SHAPE>::DIM, NN = ShapeInfo<SHAPE>::NN, NQ = RuleInfo<RULE>::NQ;
@@ -126,7 +216,7 @@ struct SSAdjointTile {
 // FF: the three B-products (B dU, B PBar, B^T deBar) in float-float arithmetic on the FP32 pipe from the
 // float-float geometry (geomG32 + geomGlo), with nodal values taken relative to the element's first
 // node (sum_a dN_a/dX = 0); the reverse return map stays FP64.  ~2^-48 relative accuracy.
-template <int SHAPE, int RULE, bool FF>
+template <int SHAPE, int RULE, bool FF, bool GX>
 __global__ void __launch_bounds__(SSAdjointTile<SHAPE, RULE>::NT) adjoint_ss_kernel(SSAdjointArgs a) {
   using T = SSAdjointTile<SHAPE, RULE>;
   constexpr int DIM = T::DIM, NN = T::NN, NQ = T::NQ, NDOF = T::NDOF, EPB = T::EPB, NT = T::NT;
@@ -277,6 +367,8 @@ __global__ void __launch_bounds__(SSAdjointTile<SHAPE, RULE>::NT) adjoint_ss_ker
     }
     double* gq = sg + (le * NQ + q) * 6;
     for (int k = 0; k < 6; ++k) gq[k] = pBar[k];
+    if constexpr (GX) coordinate_adjoint<SHAPE, RULE, FF>(a, e, q, pt, stride, s, mc, vm, sig0, k0, de, deBar, bp,
+                                                 su + le * NDOF, sp + le * NDOF);
     // dU_e contribution B^T deBar
     double* rq = sr + (le * NQ + q) * NDOF;
     if constexpr (FF) {
@@ -362,7 +454,9 @@ template <int SHAPE, int RULE>
 cudaError_t launch_adjoint_ss(const SSAdjointArgs& a, cudaStream_t st) {
   using T = SSAdjointTile<SHAPE, RULE>;
   if (a.nEl == 0) return cudaSuccess;
-  auto kern = (a.geomG32 && a.geomGlo) ? adjoint_ss_kernel<SHAPE, RULE, true> : adjoint_ss_kernel<SHAPE, RULE, false>;
+  const bool ff = a.geomG32 && a.geomGlo;
+  auto kern = a.gX ? (ff ? adjoint_ss_kernel<SHAPE, RULE, true, true> : adjoint_ss_kernel<SHAPE, RULE, false, true>)
+                   : (ff ? adjoint_ss_kernel<SHAPE, RULE, true, false> : adjoint_ss_kernel<SHAPE, RULE, false, false>);
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::bytes);
   if (err != cudaSuccess) return err;
   const int64_t blocks = (a.nEl + T::EPB - 1) / T::EPB;

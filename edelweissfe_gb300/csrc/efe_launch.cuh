@@ -171,6 +171,11 @@ struct SSAdjointArgs {
   double* barOut;             // [S][nPts] or null (accumulated)
   double* dUbar;              // [nDof] (accumulated)
   double* gProps;             // [nEl][nProps] or null (accumulated)
+  // nodal coordinate adjoints [nNodes][dim] (accumulated) or null; coords and the Hexa20 table for
+  // the Jacobian of the Hexa20 quirk
+  double* gX;
+  const double* coords;
+  Hexa20Fix fix;
 };
 
 template <int SHAPE, int RULE>

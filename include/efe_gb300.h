@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define EFE_ABI_VERSION 2
+#define EFE_ABI_VERSION 3
 
 /* element shapes (node numbering of computeNOperator, _elementcomputationmatrices.py:106-212) */
 enum { EFE_QUAD4 = 0, EFE_QUAD8 = 1, EFE_HEXA8 = 2, EFE_HEXA20 = 3 };
@@ -208,12 +208,15 @@ int32_t efe_adjoint_tl(const EfeMesh* mesh, const EfeGroup* group, const double*
      dUbar       += (ds/d dU)^T stateBarIn + (dP/d dU)^T Pbar                 (DOF vector),
      stateBarOut += (ds/d stateBefore)^T stateBarIn + (dP/d stateBefore)^T Pbar (may be NULL),
      gProps      += the same for the material properties, [nElements][nProps] (may be NULL;
-                    E, nu for linear elasticity; E, nu, fy0, HLin, dfy, delta for von Mises).
+                    E, nu for linear elasticity; E, nu, fy0, HLin, dfy, delta for von Mises),
+     gX          += the same for the nodal coordinates, [nNodes][dim] in the node order of
+                    mesh->coords (may be NULL; through dN/dX and det J, the Hexa20 Jacobian term
+                    included).
    With stateBarIn = NULL and Pbar = v, dUbar gets -K v (K the consistent tangent).  Solids and
    plane strain; needs efe_setup_geometry (geomG, geomS). */
 int32_t efe_adjoint_small_strain(const EfeMesh* mesh, const EfeGroup* group, const double* stateBefore,
                                  const double* dU, const double* Pbar, const double* stateBarIn, double* stateBarOut,
-                                 double* dUbar, double* gProps, void* stream);
+                                 double* dUbar, double* gProps, double* gX, void* stream);
 
 /* The element pass of several groups, possibly of different meshes and dimensions (e.g. batches of
    2D meshes and batches of 3D meshes), in ONE persistent launch: the resident CTAs take tiles of all

@@ -6,11 +6,13 @@ over plastic load increments (PathAdjoint), in FP64, against central differences
    derivatives of L in dU, in the state s0 and in the six material properties, h = 1e-7 relative;
    agreement to 1e-6 relative.  Both forms of the reverse pass: FP64 B-products (FP64 assembler)
    and float-float B-products (mixed assembler, which carries the float-float geometry).
+   The nodal coordinates too (dN/dX and det J, the Hexa20 Jacobian term included), against central
+   differences of L over moved nodes (geometry set up again).
 2. The plastic path: C3D20 (3x3x3 Gauss) von Mises cube, 2x2x2 elements with per-element yield
    stress U[200, 300] and hardening U[800, 1200]; bottom u_y = 0, left u_x = 0, back u_z = 0, top
-   u_y -> 0.5 % in 4 increments; J = the total top reaction.  dJ/d(fy0, H) by the path adjoint vs
-   central differences of J through full Newton solves (h = 1e-6 relative), and the mixed
-   (FP32-tangent, device PCG with refinement) adjoint vs the FP64 one.
+   u_y -> 0.5 % in 4 increments; J = the total top reaction.  dJ/d(fy0, H) and dJ/dX by the path
+   adjoint vs central differences of J through full Newton solves (h = 1e-6 relative), and the
+   mixed (FP32-tangent, device PCG with refinement) adjoint vs the FP64 one.
 """
 
 import numpy as np
@@ -82,9 +84,24 @@ def test_increment_reverse_matches_finite_differences(elType, material, precisio
     dUbar = asm.constructDofVector()
     s0bar = torch.zeros_like(s0)
     gp = torch.zeros_like(props_t)
-    asm.adjointSmallStrain(0, s0, dU, dUbar, Pbar=pbar, stateBarIn=sbar, stateBarOut=s0bar, gProps=gp)
+    gx = torch.zeros((asm.nNodes, asm.dim), dtype=torch.float64, device=dev)
+    asm.adjointSmallStrain(0, s0, dU, dUbar, Pbar=pbar, stateBarIn=sbar, stateBarOut=s0bar, gProps=gp, gX=gx)
+    # the coordinate adjoint changes nothing else: the other adjoints equal those of a pass without
+    # gX (to the rounding of the atomic sums' order)
+    dUbar2, gp2 = asm.constructDofVector(), torch.zeros_like(props_t)
+    asm.adjointSmallStrain(0, s0, dU, dUbar2, Pbar=pbar, stateBarIn=sbar, gProps=gp2)
+    for x, y in ((dUbar, dUbar2), (gp, gp2)):
+        assert float((x - y).abs().max()) <= 1e-13 * float(y.abs().max())
+
+    def LX(X):
+        asm.setCoordinates(X)
+        try:
+            return L(dU, s0, props_t)
+        finally:
+            asm.setCoordinates(coords)
+
     h = 1e-7
-    for what in ("dU", "state", "props"):
+    for what in ("dU", "state", "props", "coords"):
         for k in range(2):
             if what == "dU":
                 d = torch.tensor(rng.normal(0, 1, nDof), device=dev) * 1e-3
@@ -94,23 +111,28 @@ def test_increment_reverse_matches_finite_differences(elType, material, precisio
                 d = torch.tensor(rng.normal(0, 1, tuple(s0.shape)), device=dev) * s0.abs().amax(1, keepdim=True)
                 fd = (L(dU, s0 + h * d, props_t) - L(dU, s0 - h * d, props_t)) / (2 * h)
                 ad = float((s0bar * d).sum())
-            else:
+            elif what == "props":
                 d = torch.tensor(rng.normal(0, 1, tuple(props_t.shape)), device=dev) * props_t
                 fd = (L(dU, s0, props_t + h * d) - L(dU, s0, props_t - h * d)) / (2 * h)
                 ad = float((gp * d).sum())
+            else:  # node coordinates (element size ~0.3-0.5): dN/dX and det J
+                d = rng.normal(0, 0.05, coords.shape)
+                fd = (LX(coords + h * d) - LX(coords - h * d)) / (2 * h)
+                ad = float((gx.cpu().numpy() * d).sum())
             assert abs(ad - fd) <= 1e-6 * max(abs(fd), 1e-3 * abs(L0)), (what, k, ad, fd)
 
 
-def _path_problem(fy0, H, precision="fp64", linsolver="superlu"):
+def _path_problem(fy0, H, precision="fp64", linsolver="superlu", coords=None):
     from edelweissfe_gb300 import ElementGroup, GPUAssembler, meshes
     from edelweissfe_gb300.adjoint import PathAdjoint
     from edelweissfe_gb300.solver import AdaptiveTimeStepper, Dirichlet, NISTGPU
 
-    coords, conn, nodeDof, nDof = meshes.box(2, 2, 2, nNodes=20)
+    c0, conn, nodeDof, nDof = meshes.box(2, 2, 2, nNodes=20)
+    coords = c0 if coords is None else coords
     E = len(conn)
     props = np.stack([np.full(E, 210e3), np.full(E, 0.3), fy0, H, np.zeros(E), np.zeros(E)], 1)
     asm = GPUAssembler(coords, nodeDof, nDof, [ElementGroup("C3D20", "vonmises", props, conn)], precision=precision)
-    x, y, z = coords[:, 0], coords[:, 1], coords[:, 2]
+    x, y, z = c0[:, 0], c0[:, 1], c0[:, 2]  # the boundary sets of the unmoved box
     top = nodeDof[y > 1 - 1e-9] + 1
     dirichlets = [Dirichlet(nodeDof[y < 1e-9] + 1, 0.0), Dirichlet(nodeDof[x < 1e-9], 0.0),
                   Dirichlet(nodeDof[z < 1e-9] + 2, 0.0), Dirichlet(top, 0.005)]  # fmt: skip
@@ -143,6 +165,26 @@ def test_path_adjoint_matches_finite_differences():
         fd = (_path_problem(fy0 + h * dfy, H + h * dH)[0] - _path_problem(fy0 - h * dfy, H - h * dH)[0]) / (2 * h)
         ad = float(np.sum(g[:, 2] * dfy) + np.sum(g[:, 3] * dH))
         assert abs(ad - fd) <= 1e-6 * abs(fd), (k, ad, fd)
+
+
+def test_path_adjoint_coordinates_match_finite_differences():
+    """dJ/dX of the plastic path (the total top reaction after the C3D20 von Mises increments) by
+    the path adjoint against central differences of J through full Newton solves on moved nodes
+    (h = 1e-6 in units of a 0.05 node displacement; the prescribed values held)."""
+    rng = np.random.default_rng(10)
+    fy0 = rng.uniform(200, 300, 8)
+    H = rng.uniform(800, 1200, 8)
+    J0, adj, ddofs, top, asm = _path_problem(fy0, H)
+    cP = asm.constructDofVector()
+    cP[torch.as_tensor(top, device=asm.device)] = -1.0
+    gX = adj.gradient(ddofs, cP=cP, coordinates=True)[1].cpu().numpy()
+    coords = asm.coords.cpu().numpy().copy()
+    h = 1e-6
+    for k in range(2):
+        d = rng.normal(0, 0.05, coords.shape)
+        fd = (_path_problem(fy0, H, coords=coords + h * d)[0] - _path_problem(fy0, H, coords=coords - h * d)[0]) / (2 * h)
+        ad = float(np.sum(gX * d))
+        assert abs(ad - fd) <= 1e-6 * max(abs(fd), 1e-3 * abs(J0)), (k, ad, fd)
 
 
 def test_path_adjoint_mixed_matches_fp64():
