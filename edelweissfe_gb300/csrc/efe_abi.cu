@@ -391,8 +391,6 @@ int32_t efe_adjoint_small_strain(const EfeMesh* mesh, const EfeGroup* g, const d
     return fail(EFE_ERR_UNSUPPORTED, "efe_adjoint_small_strain covers small-strain groups");
   if (g->material != EFE_MAT_LINEAR_ELASTIC && g->material != EFE_MAT_VON_MISES)
     return fail(EFE_ERR_UNSUPPORTED, "efe_adjoint_small_strain covers linear elastic and von Mises groups");
-  if (mesh->dim == 2 && g->plane != EFE_PLANE_STRAIN)
-    return fail(EFE_ERR_UNSUPPORTED, "efe_adjoint_small_strain covers solids and plane strain");
   if (g->nElements == 0) return EFE_OK;
   if (!mesh->nodeDof || !g->conn || !g->props || !g->geomG || !g->geomS)
     return fail(EFE_ERR_ARGUMENT, "null group buffer (has efe_setup_geometry run?)");
@@ -400,6 +398,7 @@ int32_t efe_adjoint_small_strain(const EfeMesh* mesh, const EfeGroup* g, const d
   a.nEl = g->nElements;
   a.nProps = g->nProps;
   a.material = g->material;
+  a.planeStress = mesh->dim == 2 && g->plane == EFE_PLANE_STRESS;
   a.conn = g->conn;
   a.nodeDof = mesh->nodeDof;
   a.props = g->props;

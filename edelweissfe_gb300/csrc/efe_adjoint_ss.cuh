@@ -16,6 +16,8 @@
 // sBar = -sigma : (B PBar), and through G = J^-1 D (D = J G, J = D' X with the Hexa20 quirk row in
 // D'): Xbar_a = -M^T G_a + s sBar G_a (+ the quirk row's term), M = sum_a Gbar_a (x) G_a.
 //
+// Plane stress (2D): the reverse of the reference's local Newton on eps33, iteration by iteration.
+//
 // Tile layout as the forward pass: EPB elements per CTA; phase 0 gathers dU_e and PBar_e, phase A
 // runs one thread per point, phase C reduces the per-point contributions per DOF (one atomic per
 // element DOF) and per property (plain stores: one thread owns an element's property).
@@ -24,10 +26,12 @@
 
 namespace efe {
 
-// Adjoint of the hypoelastic 3D update.  Accumulates into sig0Bar, k0Bar, deBar, pBar[6].
+// Adjoint of the hypoelastic 3D update.  Accumulates into sig0Bar, k0Bar, deBar, pBar[6].  c22Bar:
+// adjoint of the tangent's entry C_33,33 (the plane-stress Newton divides by it), 0 otherwise.
 __device__ inline void hypo3d_reverse(const VMConst& c, double E, double nu, bool vonMises, const double sig0[6],
                                       double k0, const double de[6], const double sBar[6], double kBar,
-                                      double sig0Bar[6], double& k0Bar, double deBar[6], double pBar[6]) {
+                                      double sig0Bar[6], double& k0Bar, double deBar[6], double pBar[6],
+                                      double c22Bar = 0.0) {
   const Iso& Ei = c.Ei;
   const double G = c.G;
   double trBar[6];
@@ -76,7 +80,31 @@ __device__ inline void hypo3d_reverse(const VMConst& c, double E, double nu, boo
         nd += nBar * dev[i];
       }
       double qBar = -nd / (q * q);
-      const double dKBar = kBar + g2Bar * 2.0 * G * sqrt(1.5);
+      double kTBar = 0.0;  // adjoint of the final kappa through the tangent
+      if (c22Bar != 0.0) {
+        // C22 = Ei.c11 - 2/3 beta - a n2^2, beta = 2G g2 / q, a = 2G (tfac - g2 / q), n2 = dev2 / q,
+        // tfac = 1 / (1 + z), z = (H + dsat(kappa)) / 3G  (vonmises.py:241-251); the Ei.c11 term is
+        // taken with the trial's elasticity below
+        const double inv = 1.0 / q, n2 = dev[2] * inv;
+        const double z = (c.H + vm_dsat(c, k)) / (3.0 * G), tfac = 1.0 / (1.0 + z);
+        const double aT = 2.0 * G * (tfac - g2 * inv);
+        const double betaBar = -(2.0 / 3.0) * c22Bar, aBar = -c22Bar * n2 * n2, n2Bar = -c22Bar * 2.0 * aT * n2;
+        Gbar += aBar * 2.0 * (tfac - g2 * inv) + betaBar * 2.0 * g2 * inv;
+        g2Bar += (betaBar - aBar) * 2.0 * G * inv;
+        const double invBar = (betaBar - aBar) * 2.0 * G * g2 + n2Bar * dev[2];
+        devBar[2] += n2Bar * inv;
+        qBar -= invBar * inv * inv;
+        const double zBar = -tfac * tfac * aBar * 2.0 * G;
+        Gbar -= zBar * z / G;
+        pBar[3] += zBar / (3.0 * G);
+        // dsat(kappa) = dfy delta exp(-delta kappa)
+        const double dsBar = zBar / (3.0 * G), ek = exp(-c.delta * k);
+        pBar[4] += dsBar * c.delta * ek;
+        pBar[5] += dsBar * c.dfy * ek * (1.0 - c.delta * k);
+        kTBar = -dsBar * c.dfy * c.delta * c.delta * ek;
+      }
+      k0Bar += kTBar;
+      const double dKBar = kBar + kTBar + g2Bar * 2.0 * G * sqrt(1.5);
       Gbar += g2Bar * 2.0 * sqrt(1.5) * dK;
       // dK(q, kappa0, G, fy0, H, dfy, delta) from R = 0: x_bar += dK_bar * (dR/dx) / D
       const double dfyk = c.H + vm_dsat(c, k);
@@ -86,7 +114,8 @@ __device__ inline void hypo3d_reverse(const VMConst& c, double E, double nu, boo
       Gbar += -sq6 * dK * w;
       pBar[2] += -sq23 * w;
       pBar[3] += -sq23 * k * w;
-      if (c.dfy != 0.0) {
+      {
+        // sat = dfy (1 - exp(-delta kappa)) is linear in dfy: its derivative holds at dfy = 0 too
         const double ek = exp(-c.delta * k);
         pBar[4] += -sq23 * (1.0 - ek) * w;
         pBar[5] += -sq23 * c.dfy * k * ek * w;
@@ -105,7 +134,7 @@ __device__ inline void hypo3d_reverse(const VMConst& c, double E, double nu, boo
     deBar[i] += dd[i];
   }
   // properties through C11, C12, C44 and G
-  const double c11Bar = trBar[0] * de[0] + trBar[1] * de[1] + trBar[2] * de[2];
+  const double c11Bar = trBar[0] * de[0] + trBar[1] * de[1] + trBar[2] * de[2] + c22Bar;
   const double c12Bar = trBar[0] * (de[1] + de[2]) + trBar[1] * (de[0] + de[2]) + trBar[2] * (de[0] + de[1]);
   const double c44Bar = trBar[3] * de[3] + trBar[4] * de[4] + trBar[5] * de[5];
   const double den = (1.0 + nu) * (1.0 - 2.0 * nu);
@@ -115,23 +144,127 @@ __device__ inline void hypo3d_reverse(const VMConst& c, double E, double nu, boo
              Gbar * G / (1.0 + nu);
 }
 
+// Adjoint of the plane-stress von Mises update (von_mises_plane_stress; basehypoelasticmaterial.py:71-130).
+// Forward: d_1 = -de0 - de1; iteration i evaluates the 3D update from a zero stress with the kappa the
+// previous iteration left, s3_i, kappa_i = VM3D(0, kappa_{i-1}, de(d_i)), and steps
+// d_{i+1} = d_i - rev_i s3_i[2], rev_i = 1 / C22_i (clamped to +-1e10), until |s3_n[2]| is small;
+// sig = sig0 + s3_n, kappa = kappa_n, eps33 += d_n.  Because kappa carries over between the local
+// iterations, the result depends on the iterates, so the reverse sweep runs through every iteration
+// (with the derivative of rev_i) rather than through the converged equation alone.  e2Bar: adjoint of
+// the strain increment d_n stored in eps33.
+__device__ inline void von_mises_plane_stress_reverse(const VMConst& c, double E, double nu, const double sig0[6],
+                                                      double k0, const double de[6], const double sBar[6],
+                                                      double kBar, double e2Bar, double sig0Bar[6], double& k0Bar,
+                                                      double deBar[6], double pBar[6]) {
+  constexpr int MAXIT = 13;
+  double D2[MAXIT], K0[MAXIT], R2[MAXIT], RV[MAXIT];
+  double dd[6];
+  for (int f = 0; f < 6; ++f) dd[f] = de[f];
+  dd[2] = -de[0] - de[1];
+  double kap = k0;
+  int n = 0;                // index of the last evaluated iteration
+  uint32_t clampMask = 0;   // bit i: step i's rev was clamped (no derivative through it)
+  for (int counter = 1;; ++counter) {
+    D2[n] = dd[2];
+    K0[n] = kap;
+    double s3[6] = {0, 0, 0, 0, 0, 0};
+    Tangent3 T;
+    if (!von_mises_3d<false>(c, s3, dd, kap, T)) break;
+    const double residual = fabs(s3[2]);
+    if (residual < 1e-11 || (counter > 7 && residual < 1e-8) || counter == MAXIT) break;
+    double rev = 1.0 / tangent3_entry(T, 2, 2);
+    if (isnan(rev) || fabs(rev) > 1e10) {
+      rev = 1e10 * (rev > 0 ? 1.0 : (rev < 0 ? -1.0 : rev));
+      clampMask |= 1u << n;
+    }
+    RV[n] = rev;
+    R2[n] = s3[2];
+    dd[2] -= rev * s3[2];
+    ++n;
+  }
+  for (int f = 0; f < 6; ++f) sig0Bar[f] += sBar[f];  // sig = sig0 + s3_n
+  const double zero[6] = {0, 0, 0, 0, 0, 0};
+  double scratch[6] = {0, 0, 0, 0, 0, 0};
+  double inBar[6] = {0, 0, 0, 0, 0, 0};  // adjoints of the in-plane increments over all iterations
+  double dBar = e2Bar, kCarry = 0.0;
+  for (int i = n; i >= 0; --i) {
+    double sSeed[6] = {0, 0, 0, 0, 0, 0}, kSeed, c22Bar = 0.0;
+    if (i == n) {
+      for (int f = 0; f < 6; ++f) sSeed[f] = sBar[f];
+      kSeed = kBar;
+    } else {
+      // d_{i+1} = d_i - rev_i r_i: dBar carries to d_i unchanged
+      const double rev = RV[i];
+      sSeed[2] = -rev * dBar;
+      if (!(clampMask >> i & 1u)) c22Bar = rev * rev * R2[i] * dBar;  // revBar = -r_i dBar, rev = 1 / C22
+      kSeed = kCarry;
+    }
+    double ddi[6], ddBar[6] = {0, 0, 0, 0, 0, 0}, kinBar = 0.0;
+    for (int f = 0; f < 6; ++f) ddi[f] = de[f];
+    ddi[2] = D2[i];
+    hypo3d_reverse(c, E, nu, true, zero, K0[i], ddi, sSeed, kSeed, scratch, kinBar, ddBar, pBar, c22Bar);
+    dBar += ddBar[2];
+    for (int f = 0; f < 6; ++f)
+      if (f != 2) inBar[f] += ddBar[f];
+    kCarry = kinBar;
+  }
+  k0Bar += kCarry;
+  // d_1 = -de0 - de1
+  deBar[0] += inBar[0] - dBar;
+  deBar[1] += inBar[1] - dBar;
+  deBar[3] += inBar[3];
+  deBar[4] += inBar[4];
+  deBar[5] += inBar[5];
+}
+
+// Adjoint of the plane-stress linear-elastic update (linear_elastic_plane_stress; linearelastic.py:127-154):
+// sig += C(E, nu) de over 11, 22, 12 and eps33 += -nu / (1 - nu) (de0 + de1).
+__device__ inline void linear_elastic_plane_stress_reverse(double E, double nu, const double de[6],
+                                                           const double sBar[6], double e2Bar, double sig0Bar[6],
+                                                           double deBar[6], double pBar[6]) {
+  const double f = E / (1.0 - nu * nu), c11 = f, c12 = f * nu, c33 = f * ((1.0 - nu) / 2.0);
+  const double r = nu / (1.0 - nu);
+  for (int i = 0; i < 6; ++i) sig0Bar[i] += sBar[i];
+  deBar[0] += c11 * sBar[0] + c12 * sBar[1] - r * e2Bar;
+  deBar[1] += c12 * sBar[0] + c11 * sBar[1] - r * e2Bar;
+  deBar[3] += c33 * sBar[3];
+  const double c11Bar = sBar[0] * de[0] + sBar[1] * de[1], c12Bar = sBar[0] * de[1] + sBar[1] * de[0],
+               c33Bar = sBar[3] * de[3], rBar = -e2Bar * (de[0] + de[1]);
+  const double dfdnu = 2.0 * nu * f / (1.0 - nu * nu);
+  pBar[0] += (c11Bar * c11 + c12Bar * c12 + c33Bar * c33) / E;
+  pBar[1] += c11Bar * dfdnu + c12Bar * (dfdnu * nu + f) + c33Bar * (dfdnu * (1.0 - nu) / 2.0 - f / 2.0) +
+             rBar / ((1.0 - nu) * (1.0 - nu));
+}
+
 // Coordinate adjoint of one point (see the head comment), accumulated into a.gX.  u and pb: the
 // element's dU and PBar as staged by phase 0 (float-float relative to node 0 in the FF form, which
 // leaves M unchanged: sum_a G_a = 0).
 template <int SHAPE, int RULE, bool FF>
 __device__ __forceinline__ void coordinate_adjoint(const SSAdjointArgs& a, int64_t e, int q, int64_t pt, int64_t stride,
-                                                   double s, const VMConst& mc, bool vm, const double sig0[6], double k0,
-                                                   const double de[6], const double deBar[6], const double bp[6],
-                                                   const double* u, const double* pb) {
+                                                   double s, const VMConst& mc, bool vm, bool planeStress,
+                                                   const double sig0[6], double k0, const double de[6],
+                                                   const double deBar[6], const double bp[6], const double* u,
+                                                   const double* pb) {
   constexpr int DIM = ShapeInfo<SHAPE>::DIM, NN = ShapeInfo<SHAPE>::NN;
   // the new stress (the FP64 form of the forward update)
-  double sn[6], kn = k0;
-  for (int f = 0; f < 6; ++f) sn[f] = sig0[f];
-  Tangent3 Tt;
-  if (vm)
-    von_mises_3d<false>(mc, sn, de, kn, Tt);
-  else
-    linear_elastic_3d(mc, sn, de, Tt);
+  double sn[6], kn = k0, dp[6];
+  for (int f = 0; f < 6; ++f) {
+    sn[f] = sig0[f];
+    dp[f] = de[f];
+  }
+  if (planeStress) {
+    Tangent2 C2;
+    if (vm)
+      von_mises_plane_stress<false>(mc, sn, dp, kn, C2);
+    else
+      linear_elastic_plane_stress(a.props + e * a.nProps, sn, dp, C2);
+  } else {
+    Tangent3 Tt;
+    if (vm)
+      von_mises_3d<false>(mc, sn, de, kn, Tt);
+    else
+      linear_elastic_3d(mc, sn, de, Tt);
+  }
   // Voigt 11, 22, 33, 12, 13, 23 (engineering shears in de, bp) as symmetric matrices
   const double S[3][3] = {{sn[0], sn[3], sn[4]}, {sn[3], sn[1], sn[5]}, {sn[4], sn[5], sn[2]}};
   const double Db[3][3] = {{deBar[0], deBar[3], deBar[4]}, {deBar[3], deBar[1], deBar[5]},
@@ -357,7 +490,20 @@ __global__ void __launch_bounds__(SSAdjointTile<SHAPE, RULE>::NT) adjoint_ss_ker
     double sig0Bar[6] = {0, 0, 0, 0, 0, 0}, k0Bar = 0.0, pBar[6] = {0, 0, 0, 0, 0, 0};
     double deBar[6];
     for (int f = 0; f < 6; ++f) deBar[f] = eBar[f];  // eps = eps0 + de
-    hypo3d_reverse(mc, props[0], props[1], vm, sig0, k0, de, sBar, kBar, sig0Bar, k0Bar, deBar, pBar);
+    bool planeStress = false;
+    if constexpr (DIM == 2) planeStress = a.planeStress;
+    if (planeStress) {
+      // eps33 receives the plane-stress solution's increment, not a B-product: its seed enters the
+      // local Newton
+      deBar[2] = 0.0;
+      if (vm)
+        von_mises_plane_stress_reverse(mc, props[0], props[1], sig0, k0, de, sBar, kBar, eBar[2], sig0Bar, k0Bar,
+                                       deBar, pBar);
+      else
+        linear_elastic_plane_stress_reverse(props[0], props[1], de, sBar, eBar[2], sig0Bar, deBar, pBar);
+    } else {
+      hypo3d_reverse(mc, props[0], props[1], vm, sig0, k0, de, sBar, kBar, sig0Bar, k0Bar, deBar, pBar);
+    }
     if (a.barOut) {
       for (int f = 0; f < 6; ++f) {
         a.barOut[(int64_t)f * stride + pt] += sig0Bar[f];
@@ -367,8 +513,8 @@ __global__ void __launch_bounds__(SSAdjointTile<SHAPE, RULE>::NT) adjoint_ss_ker
     }
     double* gq = sg + (le * NQ + q) * 6;
     for (int k = 0; k < 6; ++k) gq[k] = pBar[k];
-    if constexpr (GX) coordinate_adjoint<SHAPE, RULE, FF>(a, e, q, pt, stride, s, mc, vm, sig0, k0, de, deBar, bp,
-                                                 su + le * NDOF, sp + le * NDOF);
+    if constexpr (GX) coordinate_adjoint<SHAPE, RULE, FF>(a, e, q, pt, stride, s, mc, vm, planeStress, sig0, k0, de,
+                                                 deBar, bp, su + le * NDOF, sp + le * NDOF);
     // dU_e contribution B^T deBar
     double* rq = sr + (le * NQ + q) * NDOF;
     if constexpr (FF) {

@@ -157,6 +157,7 @@ cudaError_t launch_adjoint_tl(const AdjointArgs& a, cudaStream_t st);
 struct SSAdjointArgs {
   int64_t nEl;
   int32_t nProps, material;
+  int32_t planeStress;  // 2D groups: 1 for plane stress (local Newton on eps33), 0 for plane strain
   const int32_t* conn;
   const int32_t* nodeDof;
   const double* props;

@@ -212,8 +212,9 @@ int32_t efe_adjoint_tl(const EfeMesh* mesh, const EfeGroup* group, const double*
      gX          += the same for the nodal coordinates, [nNodes][dim] in the node order of
                     mesh->coords (may be NULL; through dN/dX and det J, the Hexa20 Jacobian term
                     included).
-   With stateBarIn = NULL and Pbar = v, dUbar gets -K v (K the consistent tangent).  Solids and
-   plane strain; needs efe_setup_geometry (geomG, geomS). */
+   With stateBarIn = NULL and Pbar = v, dUbar gets -K v (K the consistent tangent).  Solids, plane
+   strain and plane stress (through the reference's local Newton on eps33, iteration by iteration,
+   basehypoelasticmaterial.py:71-130); needs efe_setup_geometry (geomG, geomS). */
 int32_t efe_adjoint_small_strain(const EfeMesh* mesh, const EfeGroup* group, const double* stateBefore,
                                  const double* dU, const double* Pbar, const double* stateBarIn, double* stateBarOut,
                                  double* dUbar, double* gProps, double* gX, void* stream);
