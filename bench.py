@@ -738,6 +738,18 @@ def run_hexa20tl(args):
     under F = I + 0.05 N(0,1): CUDA-event time per pass for each precision with an FP32 tangent and
     tile variants 0 (SIMT tangent), 2 and 3 (tangent on the tensor cores), and the difference of each
     variant's K and P from variant 0's."""
+    return _run_hexa20(args, "tl")
+
+
+def run_hexa20ss(args):
+    """The C3D20 (3x3x3 Gauss) von Mises element pass of a plastic increment on an n x n x n/2 box
+    (default n = 32: 16,384 elements; E = 210 GPa, nu = 0.3, fy0 = 250 MPa, H = 1 GPa, saturation 50
+    MPa at delta 10): a first increment of 0.3 % uniaxial strain plus noise is accepted, the timed
+    pass runs the second (0.1 %).  Same report as the hexa20tl workload."""
+    return _run_hexa20(args, "ss")
+
+
+def _run_hexa20(args, kind):
     import torch
 
     from edelweissfe_gb300 import ElementGroup, GPUAssembler, meshes
@@ -745,25 +757,47 @@ def run_hexa20tl(args):
     n = args.n if args.n != N_CUBE else 32
     coords, conn, nodeDof, nDof = meshes.box(n, n, max(1, n // 2), nNodes=20)
     rng = np.random.default_rng(1)
-    Fbar = np.eye(3) + 0.05 * rng.normal(size=(3, 3))
-    disp = coords @ (Fbar - np.eye(3)).T
-    U = np.zeros(nDof)
-    for c in range(3):
-        U[nodeDof + c] = disp[:, c]
-    out = {"metric": "assembled elem/s (K+R), C3D20TL Neo-Hooke (a) element pass", "unit": "elem/s",
-           "config": {"workload": f"C3D20TL {n}x{n}x{max(1, n // 2)} box, F = I + 0.05 N(0,1)", "elements": len(conn)},
+    box = f"{n}x{n}x{max(1, n // 2)}"
+    if kind == "tl":
+        Fbar = np.eye(3) + 0.05 * rng.normal(size=(3, 3))
+        disp = coords @ (Fbar - np.eye(3)).T
+        U1 = np.zeros(nDof)
+        for c in range(3):
+            U1[nodeDof + c] = disp[:, c]
+        dU2 = U1
+        elType, material, props = "C3D20TL", "neohookewa", [300.0, 3000.0]
+        metric, workload = "C3D20TL Neo-Hooke (a) element pass", f"C3D20TL {box} box, F = I + 0.05 N(0,1)"
+    else:
+        def uniaxial(strain, noise):
+            U = np.zeros(nDof)
+            U[nodeDof + 1] = strain * coords[:, 1]
+            U[nodeDof + 0] = -0.3 * strain * coords[:, 0]
+            U[nodeDof + 2] = -0.3 * strain * coords[:, 2]
+            return U + rng.normal(0, noise / n, nDof)
+
+        U1, dU2 = uniaxial(0.003, 1e-3), uniaxial(0.001, 5e-4)
+        elType, material, props = "C3D20", "vonmises", [210e3, 0.3, 250.0, 1000.0, 50.0, 10.0]
+        metric = "C3D20 von Mises element pass (plastic increment)"
+        workload = f"C3D20 J2 {box} box, second increment of uniaxial strain"
+    out = {"metric": f"assembled elem/s (K+R), {metric}", "unit": "elem/s",
+           "config": {"workload": workload, "elements": len(conn)},
            "steps": args.steps, "warmup": args.warmup, "precisions": {}}  # fmt: skip
     for prec in ("mixed", "mixed-ff"):
-        asm = GPUAssembler(coords, nodeDof, nDof, [ElementGroup("C3D20TL", "neohookewa", [300.0, 3000.0], conn)],
-                           precision=prec)  # fmt: skip
-        Ud = torch.tensor(U, device=asm.device)
+        asm = GPUAssembler(coords, nodeDof, nDof, [ElementGroup(elType, material, props, conn)], precision=prec)
         P, F, K = asm.constructDofVector(), asm.constructDofVector(), asm.constructSystemMatrix()
+        Ud = torch.tensor(U1, device=asm.device)
+        if kind == "ss":
+            asm.launch(Ud, Ud, P, K, F)  # the first increment, accepted: a plastic state
+            asm.check_status()
+            asm.acceptLastState()
+            Ud = Ud + torch.tensor(dU2, device=asm.device)
+        dUd = torch.tensor(dU2, device=asm.device)
         ref, res = None, {}
         for v in (0, 2, 3):
             asm._groups_c[0].tileVariant = v
             for _ in range(max(1, args.warmup)):
                 P.zero_(), K.zero_(), F.zero_()
-                asm.launch(Ud, Ud, P, K, F)
+                asm.launch(Ud, dUd, P, K, F)
             torch.cuda.synchronize()
             asm.check_status()
             Kc, Pc = K.double().cpu().numpy(), P.cpu().numpy()
@@ -771,7 +805,7 @@ def run_hexa20tl(args):
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record()
             for _ in range(args.steps):
-                asm.launch(Ud, Ud, P, K, F)
+                asm.launch(Ud, dUd, P, K, F)
             b.record()
             torch.cuda.synchronize()
             ms = a.elapsed_time(b) / args.steps
@@ -1184,12 +1218,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tile variant (0)")
     ap.add_argument("--workload", default="all",
-                    choices=["all", "cube", "batched", "newton", "adjoint", "plastic", "hexa20tl"],
+                    choices=["all", "cube", "batched", "newton", "adjoint", "plastic", "hexa20tl", "hexa20ss"],
                     help="all (default): the 64^3 von Mises headline line, with the batched, adjoint and plastic "
                          "workloads under its 'configs' key (one GPU); cube: the headline only; batched: the "
                          "uneven-mesh batch; newton: Newton iterations FP64 vs mixed on the 64^3 cube; adjoint: "
                          "32^3 Neo-Hooke gradients; plastic: Hexa20 J2 96x96x48 path adjoint; hexa20tl: the "
-                         "C3D20TL Neo-Hooke pass alone (n x n x n/2) per precision and tile variant")
+                         "C3D20TL Neo-Hooke pass alone (n x n x n/2) per precision and tile variant; hexa20ss: "
+                         "the same for the C3D20 von Mises pass of a plastic increment")
     ap.add_argument("--plastic-fd", type=int, default=0, help="FD directions for the plastic workload")
     ap.add_argument("--plastic-n", type=int, default=0,
                     help="plastic workload mesh (n x n x n/2); 0: 96, or 48 inside the default 'all' run")
@@ -1215,10 +1250,10 @@ def main():
         if rank == 0:
             run_reference(args)
         return
-    if args.workload in ("batched", "adjoint", "plastic", "hexa20tl"):
+    if args.workload in ("batched", "adjoint", "plastic", "hexa20tl", "hexa20ss"):
         if rank == 0:
             fn = {"batched": run_batched, "adjoint": run_adjoint, "plastic": run_plastic,
-                  "hexa20tl": run_hexa20tl}[args.workload]  # fmt: skip
+                  "hexa20tl": run_hexa20tl, "hexa20ss": run_hexa20ss}[args.workload]  # fmt: skip
             print(json.dumps(fn(args), default=str))
         return
     if args.workload == "newton":

@@ -103,13 +103,12 @@ class GPUAssembler:
             offset += len(g.conn)
         self.nElements = offset
         self._groups_c = (L.EfeGroup * len(structs))(*structs)
-        # default tile: the tensor-core tangent where the library has it (measured faster than the
-        # SIMT tangent for every such group); the autotuner may choose otherwise
-        from .autotune import TENSOR_VARIANT, variants_for
+        # default tile (autotune.default_variant): the tensor-core tangent where it measured faster;
+        # the autotuner may choose otherwise
+        from .autotune import default_variant
 
         for i in range(len(self.groups)):
-            if TENSOR_VARIANT in variants_for(self, i):
-                self._groups_c[i].tileVariant = TENSOR_VARIANT
+            self._groups_c[i].tileVariant = default_variant(self, i)
         self._setup_geometry()
 
     # ------------------------------------------------------------------ set-up

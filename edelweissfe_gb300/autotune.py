@@ -28,6 +28,25 @@ def variants_for(asm, gi):
     return VARIANTS + ((TENSOR_VARIANT,) if tc else ())
 
 
+def default_variant(asm, gi):
+    """Tile variant of group gi before (or without) autotuning.  The tensor-core tangent for total-
+    Lagrangian Hexa20 groups (faster than the SIMT tiles in both FP32-tangent modes) and for small-
+    strain Hexa20 groups with an FP64 residual (mixed); 0 for small-strain Hexa20 groups with a
+    float-float residual (mixed-ff), where the tensor-core tile, which runs the FP64 return map of an
+    element's 27 points on one warp, is about even with the SIMT tile for linear hardening and slower
+    for saturation hardening (C3D20 J2 plastic increment, 16,384 elements: 16.1 against 17.8 M
+    elem/s)."""
+    from . import _lib as L
+    from .library import element_type
+
+    if TENSOR_VARIANT not in variants_for(asm, gi):
+        return 0
+    et = element_type(asm.groups[gi].elType)
+    if not et.totalLagrangian and asm.kPrecision == L.EFE_K_FP32_FF:
+        return 0
+    return TENSOR_VARIANT
+
+
 def _key(asm, gi):
     g = asm.groups[gi]
     n = max(1, len(g.conn))

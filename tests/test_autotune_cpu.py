@@ -71,6 +71,13 @@ def test_tensor_variant_only_where_the_library_has_it():
     assert autotune.variants_for(asm("C3D20R", "vonmises", L.EFE_K_FP32), 0) == (0, 1, 2)
     assert autotune.variants_for(asm("C3D20TL", "vonmises", L.EFE_K_FP32), 0) == (0, 1, 2)
     assert autotune.variants_for(asm("C3D8TL", "neohookewa", L.EFE_K_FP32), 0) == (0, 1, 2)
+    # the default before tuning: the tensor-core tile except for small strain with a float-float residual
+    assert autotune.default_variant(asm("C3D20TL", "neohookewa", L.EFE_K_FP32), 0) == 3
+    assert autotune.default_variant(asm("C3D20TL", "neohookewa", L.EFE_K_FP32_FF), 0) == 3
+    assert autotune.default_variant(asm("C3D20", "vonmises", L.EFE_K_FP32), 0) == 3
+    assert autotune.default_variant(asm("C3D20", "vonmises", L.EFE_K_FP32_FF), 0) == 0
+    assert autotune.default_variant(asm("C3D20", "vonmises", L.EFE_K_FP64), 0) == 0
+    assert autotune.default_variant(asm("C3D8", "vonmises", L.EFE_K_FP32), 0) == 0
 
 
 def test_unreadable_cache_starts_empty(tmp_path, monkeypatch):
