@@ -88,7 +88,14 @@ struct H20TCLayout {
   static constexpr size_t ps_off = g_off + 8 * T::NQ * T::NDOF;         // int [2][NN][NN]
   static constexpr size_t rl_off = ps_off + sizeof(int) * 2 * T::NN * T::NN;  // int [2][NN]
   static constexpr size_t mc_off = (rl_off + sizeof(int) * 2 * T::NN + 15) / 16 * 16;  // VMConst (small strain)
-  static constexpr size_t tc_off = (mc_off + sizeof(VMConst) + 127) / 128 * 128;
+  // staged with dN/dX (cp.async): det J w t per point and the element's properties (at most 8)
+  static constexpr size_t s_off = (mc_off + sizeof(VMConst) + 15) / 16 * 16;  // double [NQ]
+  static constexpr size_t pr_off = s_off + 8 * T::NQ;                        // double [8]
+  static constexpr int NPR = 8;
+  // first DOF of each node of two consecutive elements (-1 where a bounds check failed), for the
+  // element residual's atomics
+  static constexpr size_t dof_off = pr_off + 8 * NPR;  // int [2][NN]
+  static constexpr size_t tc_off = (dof_off + sizeof(int) * 2 * T::NN + 127) / 128 * 128;
   static constexpr size_t bytes = tc_off + T::tc_bytes;
 };
 
@@ -161,11 +168,14 @@ __device__ __forceinline__ void h20tc_stage_g(const GroupArgs& g, int64_t e, uns
       tc::cp_async8(reinterpret_cast<double*>(smem + L::g_off) + t, g.geomG + gi);
     }
   }
+  if (threadIdx.x < NQ) tc::cp_async8(reinterpret_cast<double*>(smem + L::s_off) + threadIdx.x, g.geomS + e * NQ + threadIdx.x);
+  if (threadIdx.x < g.nProps && threadIdx.x < L::NPR)
+    tc::cp_async8(reinterpret_cast<double*>(smem + L::pr_off) + threadIdx.x, g.props + e * g.nProps + threadIdx.x);
 }
 // The small per-element data of h20tc_stage_small, loaded into registers first (so that the
 // latency of the dependent loads can overlap other work) and stored later.
 struct H20TCSmall {
-  int32_t rowLen;
+  int32_t rowLen, dof;
   double u[3];
   bool valid;
 };
@@ -173,13 +183,14 @@ template <bool FF, int FORM>
 __device__ __forceinline__ H20TCSmall h20tc_load_small(const GroupArgs& g, int64_t e, int a) {
   constexpr int NN = H20TC::NN, DIM = 3;
   const double* Ux = FORM == SS3 ? g.dU : g.U;  // small strain: the increment; TL: the total
-  H20TCSmall r{0, {0.0, 0.0, 0.0}, false};
+  H20TCSmall r{0, -1, {0.0, 0.0, 0.0}, false};
   const int32_t node = g.conn[e * NN + a];
   if (!in_bounds(g, node, g.nNodes, e)) return r;
   r.rowLen = g.nodeRowLen[node];
   const int32_t dof = g.nodeDof[node];
   if (!in_bounds(g, dof, g.nDof - DIM + 1, e)) return r;
   r.valid = true;
+  r.dof = dof;
   if constexpr (FF) {
     // displacement relative to node 0 (sum_a dN_a/dX = 0): no cancellation in F
     const int32_t node0 = g.conn[e * NN];
@@ -196,6 +207,7 @@ __device__ __forceinline__ void h20tc_store_small(const H20TCSmall& r, unsigned 
   using L = H20TCLayout<FF>;
   constexpr int NN = H20TC::NN, DIM = 3;
   reinterpret_cast<int*>(smem + L::rl_off)[par * NN + a] = r.rowLen;
+  reinterpret_cast<int*>(smem + L::dof_off)[par * NN + a] = r.valid ? r.dof : -1;
   if (!r.valid) return;
   for (int c = 0; c < DIM; ++c) {
     if constexpr (FF)
@@ -238,7 +250,7 @@ __device__ __forceinline__ void h20tc_pending_and_next(const GroupArgs& g, int64
                                                       int li, bool failed) {
   using L = H20TCLayout<FF>;
   constexpr int NN = H20TC::NN, NTH = 96;
-  H20TCSmall nx{0, {0.0, 0.0, 0.0}, false};
+  H20TCSmall nx{0, -1, {0.0, 0.0, 0.0}, false};
   if (next >= 0 && li < NN) nx = h20tc_load_small<FF, FORM>(g, next, li);
   if (prev >= 0 && !failed) h20tc_scatter(g, prev, tb, sps + (par ^ 1) * NN * NN, srl + (par ^ 1) * NN, li, NTH);
   if (next >= 0) {
@@ -288,11 +300,13 @@ __device__ __forceinline__ void assemble_tile_h20tc(const GroupArgs& g, const in
     h20tc_stage_g<FF>(g, e, smem);
     h20tc_stage_small<FF, FORM>(g, e, smem, par, rt, NT);
   }
-  // small strain: the element's von Mises / elasticity constants, once per element
-  if (FORM == SS3 && tid == NT - 1)
-    *reinterpret_cast<VMConst*>(smem + L::mc_off) = vm_const(g.props + e * g.nProps, g.material == EFE_MAT_VON_MISES);
   tc::cp_async_wait_all();
   __syncthreads();
+  const double* sS = reinterpret_cast<const double*>(smem + L::s_off);    // det J w t per point
+  const double* sPr = reinterpret_cast<const double*>(smem + L::pr_off);  // the element's properties
+  // small strain: the element's von Mises / elasticity constants, once per element (read in A1)
+  if (FORM == SS3 && tid == NT - 1)
+    *reinterpret_cast<VMConst*>(smem + L::mc_off) = vm_const(sPr, g.material == EFE_MAT_VON_MISES);
 
   // ---- A0: H = sum_a U_a (x) dN_a/dX (U: the increment dU for small strain), one thread per
   // (point, component); the mixed TL pass keeps F = I + H, the others H
@@ -366,7 +380,7 @@ __device__ __forceinline__ void assemble_tile_h20tc(const GroupArgs& g, const in
         for (int f = 0; f < 6; ++f) finite = finite && finite_bits(sig[f]);
         if (!ok) report(g.status, EFE_STATUS_CUTBACK, g.elementOffset + e, 1);
         if (!finite) atomicOr(g.status, EFE_STATUS_NONFINITE);
-        const double s = g.geomS[pt];
+        const double s = sS[q];
         // s sigma (rows 11 12 13 / 12 22 23 / 13 23 33) for the residual r_a = s sigma . G_a
         const double S3[9] = {sig[0], sig[3], sig[4], sig[3], sig[1], sig[5], sig[4], sig[5], sig[2]};
         const double N3[9] = {Tg.n[0], Tg.n[3], Tg.n[4], Tg.n[3], Tg.n[1], Tg.n[5], Tg.n[4], Tg.n[5], Tg.n[2]};
@@ -427,7 +441,7 @@ __device__ __forceinline__ void assemble_tile_h20tc(const GroupArgs& g, const in
       if (rt < NQ) {
         const int q = rt;
         const int64_t pt = e * NQ + q;
-        const double* props = g.props + e * g.nProps;
+        const double* props = sPr;
         const ff* H = sH + q * 9;
         const ff* A = sA1 + q * T::NA1;
         ff Jf = ff_mul(ff_sum(H[0], ff{1.0f, 0.0f}), A[6 + 0]);  // F00 C00 + F01 C10 + F02 C20
@@ -443,7 +457,7 @@ __device__ __forceinline__ void assemble_tile_h20tc(const GroupArgs& g, const in
         ff_add(rJ, ff{1.0f, 0.0f});
         rJ = ff_mul(rJ, ff{r0, 0.0f});
         ff_add(rJ, ff{r0, 0.0f});
-        const double s = g.geomS[pt];
+        const double s = sS[q];
         T::A1Scalars sc;
         sc.sB = ff_split_bits(o.sB);
         sc.sI = ff_split_bits(o.sI);
@@ -499,7 +513,7 @@ __device__ __forceinline__ void assemble_tile_h20tc(const GroupArgs& g, const in
       if (rt < NQ) {
         const int q = rt;
         const int64_t pt = e * NQ + q;
-        const double* props = g.props + e * g.nProps;
+        const double* props = sPr;
         double F[3][3];
         for (int i = 0; i < 3; ++i)
           for (int j = 0; j < 3; ++j) F[i][j] = sF[q * 9 + i * 3 + j];
@@ -536,7 +550,7 @@ __device__ __forceinline__ void assemble_tile_h20tc(const GroupArgs& g, const in
         const double sig[6] = {o.sB * B[0][0] + o.sI, o.sB * B[1][1] + o.sI, o.sB * B[2][2] + o.sI,
                                o.sB * B[0][1],        o.sB * B[1][2],        o.sB * B[0][2]};
         const double eps[6] = {Eg[0][0], Eg[1][1], Eg[2][2], 2.0 * Eg[0][1], 2.0 * Eg[1][2], 2.0 * Eg[0][2]};
-        const double s = g.geomS[pt];
+        const double s = sS[q];
         // s tau F^-T = (s sB) F + (s sI) F^-T
         const double aF = s * o.sB, aI = s * o.sI;
         float* r = rk + q * T::RK;
@@ -735,13 +749,11 @@ __device__ __forceinline__ void assemble_tile_h20tc(const GroupArgs& g, const in
     } else {
       p = (pe[0] + pe[1]) + pe[2];
     }
-    const int32_t node = g.conn[e * NN + ra];
-    if (in_bounds(g, node, g.nNodes, e)) {
-      const int32_t dof = g.nodeDof[node] + rj;
-      if (in_bounds(g, dof, g.nDof, e)) {
-        atomicAdd(g.P + dof, p);
-        atomicAdd(g.F + dof, fabs(p));
-      }
+    // the node's first DOF as staged (-1: its bounds check failed and was reported)
+    const int32_t d0 = reinterpret_cast<const int*>(smem + L::dof_off)[par * NN + ra];
+    if (d0 >= 0) {
+      atomicAdd(g.P + d0 + rj, p);
+      atomicAdd(g.F + d0 + rj, fabs(p));
     }
   }
   if (prev == H20TC_NOW && !tcs.failed) h20tc_scatter(g, e, tb, sps + par * NN * NN, srl + par * NN, tid, NT);
