@@ -34,7 +34,7 @@ def default_variant(asm, gi):
     strain Hexa20 groups with an FP64 residual (mixed); 0 for small-strain Hexa20 groups with a
     float-float residual (mixed-ff), where the tensor-core tile, which runs the FP64 return map of an
     element's 27 points on one warp, is about even with the SIMT tile for linear hardening and slower
-    for saturation hardening (C3D20 J2 plastic increment, 16,384 elements: 16.1 against 17.8 M
+    for saturation hardening (C3D20 J2 plastic increment, 16,384 elements: 16.7 against 17.7 M
     elem/s)."""
     from . import _lib as L
     from .library import element_type
