@@ -26,12 +26,40 @@
 
 namespace efe {
 
+// Per-element constants of the reverse pass: the forward update's (VMConst) and the reciprocals and
+// derivatives the property adjoints need, formed once per element (the pass is FP64-bound, and an
+// FP64 division costs several FP64 instructions).
+struct SSRevConst {
+  VMConst c;
+  double E, nu;
+  double rE, r1nu;  // 1 / E, 1 / (1 + nu)
+  double f, df;     // f = E / ((1 + nu)(1 - 2 nu)) and df/dnu = E (1 + 4 nu) / ((1 + nu)(1 - 2 nu))^2
+  double rDR;       // 1 / (sqrt(6) G + sqrt(2/3) H): minus the return map's Newton factor (linear hardening)
+  double r3G;       // 1 / (3 G)
+};
+__device__ inline SSRevConst ss_rev_const(const double* props, bool vonMises) {
+  SSRevConst r;
+  r.c = vm_const(props, vonMises);
+  r.E = props[0];
+  r.nu = props[1];
+  r.rE = 1.0 / r.E;
+  r.r1nu = 1.0 / (1.0 + r.nu);
+  const double rden = 1.0 / ((1.0 + r.nu) * (1.0 - 2.0 * r.nu));
+  r.f = r.E * rden;
+  r.df = r.E * (1.0 + 4.0 * r.nu) * rden * rden;
+  r.rDR = -r.c.invdR;
+  r.r3G = 1.0 / (3.0 * r.c.G);
+  return r;
+}
+
 // Adjoint of the hypoelastic 3D update.  Accumulates into sig0Bar, k0Bar, deBar, pBar[6].  c22Bar:
 // adjoint of the tangent's entry C_33,33 (the plane-stress Newton divides by it), 0 otherwise.
-__device__ inline void hypo3d_reverse(const VMConst& c, double E, double nu, bool vonMises, const double sig0[6],
-                                      double k0, const double de[6], const double sBar[6], double kBar,
-                                      double sig0Bar[6], double& k0Bar, double deBar[6], double pBar[6],
-                                      double c22Bar = 0.0) {
+// Divisions are taken as products with reciprocals (per point: 1 / |dev|; per element: SSRevConst),
+// which changes the recomputed state only by rounding.
+__device__ inline void hypo3d_reverse(const SSRevConst& rc, bool vonMises, const double sig0[6], double k0,
+                                      const double de[6], const double sBar[6], double kBar, double sig0Bar[6],
+                                      double& k0Bar, double deBar[6], double pBar[6], double c22Bar = 0.0) {
+  const VMConst& c = rc.c;
   const Iso& Ei = c.Ei;
   const double G = c.G;
   double trBar[6];
@@ -52,53 +80,54 @@ __device__ inline void hypo3d_reverse(const VMConst& c, double E, double nu, boo
     dev[3] = tr[3];
     dev[4] = tr[4];
     dev[5] = tr[5];
-    const double q = sqrt(dev[0] * dev[0] + dev[1] * dev[1] + dev[2] * dev[2] +
-                          2.0 * (dev[3] * dev[3] + dev[4] * dev[4] + dev[5] * dev[5]));
+    // |dev| and 1 / |dev| from one reciprocal square root (as the forward pass with an FP32 tangent)
+    double q, iq;
+    vm_dev_norm(dev, q, iq);
     const double sq23 = sqrt(2.0 / 3.0), sq6 = sqrt(6.0);
     const double fy_k0 = c.fy0 + c.H * k0 + vm_sat(c, k0);
     if (q - sq23 * fy_k0 > 0.0) {
-      // the scalar Newton of the FP64 form of the forward pass, step for step (the FP32-tangent form
-      // forms 1/|dev| and the step with reciprocals: its dK differs by rounding, immaterial here)
+      // the scalar Newton of the forward return map (converged dK; with linear hardening its factor
+      // is the per-element constant, as in the forward pass with an FP32 tangent)
+      const bool lin = c.dfy == 0.0;
       double dK = 0.0;
       for (int counter = 0;; ++counter) {
         const double k = k0 + dK;
         const double R = q - sq6 * G * dK - sq23 * (c.fy0 + c.H * k + vm_sat(c, k));
         if (!(fabs(R) > 1e-12) || counter == 15) break;
-        const double dR = -sq6 * G - sq23 * (c.H + vm_dsat(c, k));
-        dK -= R / dR;
+        if (lin)
+          dK += R * rc.rDR;
+        else
+          dK -= R / (-sq6 * G - sq23 * (c.H + vm_dsat(c, k)));
       }
       const double k = k0 + dK;
       const double g2 = 2.0 * G * (sqrt(1.5) * dK);  // sig = tr - g2 n, n = dev / q
-      double n[6], g2Bar = 0.0, nd = 0.0, devBar[6];
-      for (int i = 0; i < 6; ++i) {
-        n[i] = dev[i] / q;
-        g2Bar -= sBar[i] * n[i];
-      }
+      double g2Bar = 0.0, nd = 0.0, devBar[6];
+      for (int i = 0; i < 6; ++i) g2Bar -= sBar[i] * (dev[i] * iq);
       for (int i = 0; i < 6; ++i) {
         const double nBar = -g2 * sBar[i];
-        devBar[i] = nBar / q;
+        devBar[i] = nBar * iq;
         nd += nBar * dev[i];
       }
-      double qBar = -nd / (q * q);
+      double qBar = -nd * iq * iq;
       double kTBar = 0.0;  // adjoint of the final kappa through the tangent
       if (c22Bar != 0.0) {
         // C22 = Ei.c11 - 2/3 beta - a n2^2, beta = 2G g2 / q, a = 2G (tfac - g2 / q), n2 = dev2 / q,
         // tfac = 1 / (1 + z), z = (H + dsat(kappa)) / 3G  (vonmises.py:241-251); the Ei.c11 term is
         // taken with the trial's elasticity below
-        const double inv = 1.0 / q, n2 = dev[2] * inv;
-        const double z = (c.H + vm_dsat(c, k)) / (3.0 * G), tfac = 1.0 / (1.0 + z);
-        const double aT = 2.0 * G * (tfac - g2 * inv);
+        const double n2 = dev[2] * iq;
+        const double z = (c.H + vm_dsat(c, k)) * rc.r3G, tfac = lin ? c.tfac : 1.0 / (1.0 + z);
+        const double aT = 2.0 * G * (tfac - g2 * iq);
         const double betaBar = -(2.0 / 3.0) * c22Bar, aBar = -c22Bar * n2 * n2, n2Bar = -c22Bar * 2.0 * aT * n2;
-        Gbar += aBar * 2.0 * (tfac - g2 * inv) + betaBar * 2.0 * g2 * inv;
-        g2Bar += (betaBar - aBar) * 2.0 * G * inv;
+        Gbar += aBar * 2.0 * (tfac - g2 * iq) + betaBar * 2.0 * g2 * iq;
+        g2Bar += (betaBar - aBar) * 2.0 * G * iq;
         const double invBar = (betaBar - aBar) * 2.0 * G * g2 + n2Bar * dev[2];
-        devBar[2] += n2Bar * inv;
-        qBar -= invBar * inv * inv;
+        devBar[2] += n2Bar * iq;
+        qBar -= invBar * iq * iq;
         const double zBar = -tfac * tfac * aBar * 2.0 * G;
-        Gbar -= zBar * z / G;
-        pBar[3] += zBar / (3.0 * G);
+        Gbar -= zBar * z * 3.0 * rc.r3G;  // dz/dG = -z / G
+        pBar[3] += zBar * rc.r3G;
         // dsat(kappa) = dfy delta exp(-delta kappa)
-        const double dsBar = zBar / (3.0 * G), ek = exp(-c.delta * k);
+        const double dsBar = zBar * rc.r3G, ek = exp(-c.delta * k);
         pBar[4] += dsBar * c.delta * ek;
         pBar[5] += dsBar * c.dfy * ek * (1.0 - c.delta * k);
         kTBar = -dsBar * c.dfy * c.delta * c.delta * ek;
@@ -108,7 +137,7 @@ __device__ inline void hypo3d_reverse(const VMConst& c, double E, double nu, boo
       Gbar += g2Bar * 2.0 * sqrt(1.5) * dK;
       // dK(q, kappa0, G, fy0, H, dfy, delta) from R = 0: x_bar += dK_bar * (dR/dx) / D
       const double dfyk = c.H + vm_dsat(c, k);
-      const double w = dKBar / (sq6 * G + sq23 * dfyk);
+      const double w = lin ? dKBar * rc.rDR : dKBar / (sq6 * G + sq23 * dfyk);
       qBar += w;
       k0Bar += -sq23 * dfyk * w;
       Gbar += -sq6 * dK * w;
@@ -116,12 +145,13 @@ __device__ inline void hypo3d_reverse(const VMConst& c, double E, double nu, boo
       pBar[3] += -sq23 * k * w;
       {
         // sat = dfy (1 - exp(-delta kappa)) is linear in dfy: its derivative holds at dfy = 0 too
-        const double ek = exp(-c.delta * k);
+        const double ek = c.delta == 0.0 ? 1.0 : exp(-c.delta * k);
         pBar[4] += -sq23 * (1.0 - ek) * w;
         pBar[5] += -sq23 * c.dfy * k * ek * w;
       }
       // q = |dev| with doubled shear terms, dev = deviatoric part of tr
-      for (int i = 0; i < 6; ++i) devBar[i] += qBar * (i < 3 ? 1.0 : 2.0) * dev[i] / q;
+      const double qi = qBar * iq;
+      for (int i = 0; i < 6; ++i) devBar[i] += qi * (i < 3 ? 1.0 : 2.0) * dev[i];
       const double mb = (devBar[0] + devBar[1] + devBar[2]) * (1.0 / 3.0);
       for (int i = 0; i < 6; ++i) trBar[i] += devBar[i] - (i < 3 ? mb : 0.0);
     }
@@ -137,11 +167,10 @@ __device__ inline void hypo3d_reverse(const VMConst& c, double E, double nu, boo
   const double c11Bar = trBar[0] * de[0] + trBar[1] * de[1] + trBar[2] * de[2] + c22Bar;
   const double c12Bar = trBar[0] * (de[1] + de[2]) + trBar[1] * (de[0] + de[2]) + trBar[2] * (de[0] + de[1]);
   const double c44Bar = trBar[3] * de[3] + trBar[4] * de[4] + trBar[5] * de[5];
-  const double den = (1.0 + nu) * (1.0 - 2.0 * nu);
-  const double f = E / den, df = E * (1.0 + 4.0 * nu) / (den * den);
-  pBar[0] += (c11Bar * Ei.c11 + c12Bar * Ei.c12 + c44Bar * Ei.c44 + Gbar * G) / E;
+  const double nu = rc.nu, f = rc.f, df = rc.df;
+  pBar[0] += (c11Bar * Ei.c11 + c12Bar * Ei.c12 + c44Bar * Ei.c44 + Gbar * G) * rc.rE;
   pBar[1] += c11Bar * (df * (1.0 - nu) - f) + c12Bar * (df * nu + f) + c44Bar * (df * (1.0 - 2.0 * nu) / 2.0 - f) -
-             Gbar * G / (1.0 + nu);
+             Gbar * G * rc.r1nu;
 }
 
 // Adjoint of the plane-stress von Mises update (von_mises_plane_stress; basehypoelasticmaterial.py:71-130).
@@ -152,10 +181,10 @@ __device__ inline void hypo3d_reverse(const VMConst& c, double E, double nu, boo
 // iterations, the result depends on the iterates, so the reverse sweep runs through every iteration
 // (with the derivative of rev_i) rather than through the converged equation alone.  e2Bar: adjoint of
 // the strain increment d_n stored in eps33.
-__device__ inline void von_mises_plane_stress_reverse(const VMConst& c, double E, double nu, const double sig0[6],
-                                                      double k0, const double de[6], const double sBar[6],
-                                                      double kBar, double e2Bar, double sig0Bar[6], double& k0Bar,
-                                                      double deBar[6], double pBar[6]) {
+__device__ inline void von_mises_plane_stress_reverse(const SSRevConst& rc, const double sig0[6], double k0,
+                                                      const double de[6], const double sBar[6], double kBar,
+                                                      double e2Bar, double sig0Bar[6], double& k0Bar, double deBar[6],
+                                                      double pBar[6]) {
   constexpr int MAXIT = 13;
   double D2[MAXIT], K0[MAXIT], R2[MAXIT], RV[MAXIT];
   double dd[6];
@@ -169,7 +198,7 @@ __device__ inline void von_mises_plane_stress_reverse(const VMConst& c, double E
     K0[n] = kap;
     double s3[6] = {0, 0, 0, 0, 0, 0};
     Tangent3 T;
-    if (!von_mises_3d<false>(c, s3, dd, kap, T)) break;
+    if (!von_mises_3d<false>(rc.c, s3, dd, kap, T)) break;
     const double residual = fabs(s3[2]);
     if (residual < 1e-11 || (counter > 7 && residual < 1e-8) || counter == MAXIT) break;
     double rev = 1.0 / tangent3_entry(T, 2, 2);
@@ -202,7 +231,7 @@ __device__ inline void von_mises_plane_stress_reverse(const VMConst& c, double E
     double ddi[6], ddBar[6] = {0, 0, 0, 0, 0, 0}, kinBar = 0.0;
     for (int f = 0; f < 6; ++f) ddi[f] = de[f];
     ddi[2] = D2[i];
-    hypo3d_reverse(c, E, nu, true, zero, K0[i], ddi, sSeed, kSeed, scratch, kinBar, ddBar, pBar, c22Bar);
+    hypo3d_reverse(rc, true, zero, K0[i], ddi, sSeed, kSeed, scratch, kinBar, ddBar, pBar, c22Bar);
     dBar += ddBar[2];
     for (int f = 0; f < 6; ++f)
       if (f != 2) inBar[f] += ddBar[f];
@@ -337,32 +366,59 @@ template <int SHAPE, int RULE>
 struct SSAdjointTile {
   static constexpr int DIM = ShapeInfo<SHAPE>::DIM, NN = ShapeInfo<SHAPE>::NN, NQ = RuleInfo<RULE>::NQ;
   static constexpr int NDOF = NN * DIM, NT = 128;
-  static constexpr size_t per_el = sizeof(double) * (2 * NDOF + NQ * NDOF + NQ * 6);
+  // per element: dU_e and PBar_e; its points' dN/dX (NDOF x NQ, 8 bytes each: doubles, or float-float
+  // hi and lo floats), property adjoints (6) and strain adjoints (6)
+  static constexpr size_t per_el = sizeof(double) * (2 * NDOF + NQ * NDOF + NQ * 12);
   static constexpr int EPB0 = NT / NQ > 0 ? NT / NQ : 1;
   static constexpr int EPB = (size_t)EPB0 * per_el <= 96 * 1024 ? EPB0 : (int)((96 * 1024) / per_el);
   static_assert(EPB >= 1, "one element must fit in shared memory");
+  // the staged dN/dX: row r = l NN + a (component l of dN_a/dX) over the tile's points, an odd row
+  // stride so that the per-DOF reads of phase C (different rows, one point) spread over the banks
+  static constexpr int NP = EPB * NQ, NPS = NP | 1;
   static constexpr size_t u_off = 0, p_off = u_off + sizeof(double) * EPB * NDOF,
-                          r_off = p_off + sizeof(double) * EPB * NDOF, g_off = r_off + sizeof(double) * EPB * NQ * NDOF,
-                          bytes = g_off + sizeof(double) * EPB * NQ * 6;
+                          g_off = p_off + sizeof(double) * EPB * NDOF,
+                          q_off = g_off + sizeof(double) * NDOF * NPS,  // double [NP][6]: property adjoints
+                          d_off = q_off + sizeof(double) * NP * 6,      // double or ff [NP][6]: strain adjoints
+                          c_off = d_off + sizeof(double) * NP * 6,      // SSRevConst [EPB]
+                          bytes = c_off + sizeof(SSRevConst) * EPB;
 };
 
 // FF: the three B-products (B dU, B PBar, B^T deBar) in float-float arithmetic on the FP32 pipe from the
 // float-float geometry (geomG32 + geomGlo), with nodal values taken relative to the element's first
 // node (sum_a dN_a/dX = 0); the reverse return map stays FP64.  ~2^-48 relative accuracy.
+// Phase 0 stages the tile's dN/dX rows in shared memory (cp.async), so that phase A (one thread per
+// point: B dU, B PBar, the reverse update) and phase C (one thread per element DOF: B^T deBar summed
+// over the points) read it there rather than twice from global memory.
 template <int SHAPE, int RULE, bool FF, bool GX>
 __global__ void __launch_bounds__(SSAdjointTile<SHAPE, RULE>::NT) adjoint_ss_kernel(SSAdjointArgs a) {
   using T = SSAdjointTile<SHAPE, RULE>;
-  constexpr int DIM = T::DIM, NN = T::NN, NQ = T::NQ, NDOF = T::NDOF, EPB = T::EPB, NT = T::NT;
+  constexpr int DIM = T::DIM, NN = T::NN, NQ = T::NQ, NDOF = T::NDOF, EPB = T::EPB, NT = T::NT, NPS = T::NPS;
   extern __shared__ __align__(128) unsigned char smem[];
   double* su = reinterpret_cast<double*>(smem + T::u_off);
   double* sp = reinterpret_cast<double*>(smem + T::p_off);
-  double* sr = reinterpret_cast<double*>(smem + T::r_off);
-  double* sg = reinterpret_cast<double*>(smem + T::g_off);
+  float* sGh = reinterpret_cast<float*>(smem + T::g_off);  // FF: hi floats, then lo floats
+  float* sGl = sGh + NDOF * NPS;
+  double* sGd = reinterpret_cast<double*>(smem + T::g_off);  // FP64 dN/dX
+  double* sg = reinterpret_cast<double*>(smem + T::q_off);
+  double* sd = reinterpret_cast<double*>(smem + T::d_off);
+  SSRevConst* src = reinterpret_cast<SSRevConst*>(smem + T::c_off);
   const int64_t e0 = (int64_t)blockIdx.x * EPB;
   const int64_t nEl = a.nEl, stride = nEl * NQ;
   const bool vm = a.material == EFE_MAT_VON_MISES;
+  const int nLoc = nEl - e0 < EPB ? (int)(nEl - e0) : EPB;  // elements of this tile
 
-  // ---- phase 0: dU_e and PBar_e
+  // ---- phase 0: dN/dX rows (cp.async), dU_e and PBar_e, the elements' constants
+  for (int t = threadIdx.x; t < NDOF * nLoc * NQ; t += NT) {
+    const int r = t / (nLoc * NQ), j = t - r * (nLoc * NQ);
+    const int64_t gi = (int64_t)r * stride + e0 * NQ + j;
+    if constexpr (FF) {
+      tc::cp_async4(sGh + r * NPS + j, a.geomG32 + gi);
+      tc::cp_async4(sGl + r * NPS + j, a.geomGlo + gi);
+    } else {
+      tc::cp_async8(sGd + r * NPS + j, a.geomG + gi);
+    }
+  }
+  if (threadIdx.x < nLoc) src[threadIdx.x] = ss_rev_const(a.props + (e0 + threadIdx.x) * a.nProps, vm);
   for (int t = threadIdx.x; t < EPB * NN; t += NT) {
     const int le = t / NN, n = t % NN;
     const int64_t e = e0 + le;
@@ -383,6 +439,7 @@ __global__ void __launch_bounds__(SSAdjointTile<SHAPE, RULE>::NT) adjoint_ss_ker
       }
     }
   }
+  tc::cp_async_wait_all();
   __syncthreads();
 
   // ---- phase A: one thread per point
@@ -391,8 +448,7 @@ __global__ void __launch_bounds__(SSAdjointTile<SHAPE, RULE>::NT) adjoint_ss_ker
     const int64_t e = e0 + le;
     if (e >= nEl) continue;
     const int64_t pt = e * NQ + q;
-    // G is read where it is used (twice) rather than held across the return map: fewer registers
-    const double* Gp = a.geomG + pt;
+    const int pl = le * NQ + q;  // the point in the tile
     const double s = a.geomS[pt];
     // B u and B PBar (small-strain Voigt 11,22,33,12,13,23, engineering shear)
     double de[6] = {0, 0, 0, 0, 0, 0}, bp[6] = {0, 0, 0, 0, 0, 0};
@@ -401,10 +457,10 @@ __global__ void __launch_bounds__(SSAdjointTile<SHAPE, RULE>::NT) adjoint_ss_ker
       const ff* pf = reinterpret_cast<const ff*>(sp) + le * NDOF;
       ff ad[6] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}}, ab[6] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}};
       for (int n = 0; n < NN; ++n) {
-        const ff gx = ff{a.geomG32[(int64_t)n * stride + pt], a.geomGlo[(int64_t)n * stride + pt]};
-        const ff gy = ff{a.geomG32[(int64_t)(NN + n) * stride + pt], a.geomGlo[(int64_t)(NN + n) * stride + pt]};
+        const ff gx = ff{sGh[n * NPS + pl], sGl[n * NPS + pl]};
+        const ff gy = ff{sGh[(NN + n) * NPS + pl], sGl[(NN + n) * NPS + pl]};
         if constexpr (DIM == 3) {
-          const ff gz = ff{a.geomG32[(int64_t)(2 * NN + n) * stride + pt], a.geomGlo[(int64_t)(2 * NN + n) * stride + pt]};
+          const ff gz = ff{sGh[(2 * NN + n) * NPS + pl], sGl[(2 * NN + n) * NPS + pl]};
           const ff ux = uf[n * 3], uy = uf[n * 3 + 1], uz = uf[n * 3 + 2];
           const ff px = pf[n * 3], py = pf[n * 3 + 1], pz = pf[n * 3 + 2];
           ff_fma(ad[0], gx, ux);
@@ -446,9 +502,9 @@ __global__ void __launch_bounds__(SSAdjointTile<SHAPE, RULE>::NT) adjoint_ss_ker
       const double* u = su + le * NDOF;
       const double* pb = sp + le * NDOF;
       for (int n = 0; n < NN; ++n) {
-        const double gx = Gp[(int64_t)n * stride], gy = Gp[(int64_t)(NN + n) * stride];
+        const double gx = sGd[n * NPS + pl], gy = sGd[(NN + n) * NPS + pl];
         if constexpr (DIM == 3) {
-          const double gz = Gp[(int64_t)(2 * NN + n) * stride];
+          const double gz = sGd[(2 * NN + n) * NPS + pl];
           const double ux = u[n * 3], uy = u[n * 3 + 1], uz = u[n * 3 + 2];
           const double px = pb[n * 3], py = pb[n * 3 + 1], pz = pb[n * 3 + 2];
           de[0] = fma(gx, ux, de[0]);
@@ -486,7 +542,8 @@ __global__ void __launch_bounds__(SSAdjointTile<SHAPE, RULE>::NT) adjoint_ss_ker
     for (int f = 0; f < 6; ++f) sig0[f] = a.stateBefore[(int64_t)f * stride + pt];
     if (vm) k0 = a.stateBefore[(int64_t)12 * stride + pt];
     const double* props = a.props + e * a.nProps;
-    const VMConst mc = vm_const(props, vm);
+    const SSRevConst& rc = src[le];
+    const VMConst& mc = rc.c;
     double sig0Bar[6] = {0, 0, 0, 0, 0, 0}, k0Bar = 0.0, pBar[6] = {0, 0, 0, 0, 0, 0};
     double deBar[6];
     for (int f = 0; f < 6; ++f) deBar[f] = eBar[f];  // eps = eps0 + de
@@ -497,12 +554,11 @@ __global__ void __launch_bounds__(SSAdjointTile<SHAPE, RULE>::NT) adjoint_ss_ker
       // local Newton
       deBar[2] = 0.0;
       if (vm)
-        von_mises_plane_stress_reverse(mc, props[0], props[1], sig0, k0, de, sBar, kBar, eBar[2], sig0Bar, k0Bar,
-                                       deBar, pBar);
+        von_mises_plane_stress_reverse(rc, sig0, k0, de, sBar, kBar, eBar[2], sig0Bar, k0Bar, deBar, pBar);
       else
         linear_elastic_plane_stress_reverse(props[0], props[1], de, sBar, eBar[2], sig0Bar, deBar, pBar);
     } else {
-      hypo3d_reverse(mc, props[0], props[1], vm, sig0, k0, de, sBar, kBar, sig0Bar, k0Bar, deBar, pBar);
+      hypo3d_reverse(rc, vm, sig0, k0, de, sBar, kBar, sig0Bar, k0Bar, deBar, pBar);
     }
     if (a.barOut) {
       for (int f = 0; f < 6; ++f) {
@@ -511,76 +567,50 @@ __global__ void __launch_bounds__(SSAdjointTile<SHAPE, RULE>::NT) adjoint_ss_ker
       }
       if (vm) a.barOut[(int64_t)12 * stride + pt] += k0Bar;
     }
-    double* gq = sg + (le * NQ + q) * 6;
+    double* gq = sg + pl * 6;
     for (int k = 0; k < 6; ++k) gq[k] = pBar[k];
     if constexpr (GX) coordinate_adjoint<SHAPE, RULE, FF>(a, e, q, pt, stride, s, mc, vm, planeStress, sig0, k0, de,
                                                  deBar, bp, su + le * NDOF, sp + le * NDOF);
-    // dU_e contribution B^T deBar
-    double* rq = sr + (le * NQ + q) * NDOF;
+    // the strain adjoint, for B^T deBar in phase C
     if constexpr (FF) {
-      ff db[6];
-      for (int f = 0; f < 6; ++f) db[f] = ff_split(deBar[f]);
-      ff* rf = reinterpret_cast<ff*>(rq);
-      for (int n = 0; n < NN; ++n) {
-        const ff gx = ff{a.geomG32[(int64_t)n * stride + pt], a.geomGlo[(int64_t)n * stride + pt]};
-        const ff gy = ff{a.geomG32[(int64_t)(NN + n) * stride + pt], a.geomGlo[(int64_t)(NN + n) * stride + pt]};
-        if constexpr (DIM == 3) {
-          const ff gz = ff{a.geomG32[(int64_t)(2 * NN + n) * stride + pt], a.geomGlo[(int64_t)(2 * NN + n) * stride + pt]};
-          ff r0{0, 0}, r1{0, 0}, r2{0, 0};
-          ff_fma(r0, db[0], gx);
-          ff_fma(r0, db[3], gy);
-          ff_fma(r0, db[4], gz);
-          ff_fma(r1, db[3], gx);
-          ff_fma(r1, db[1], gy);
-          ff_fma(r1, db[5], gz);
-          ff_fma(r2, db[4], gx);
-          ff_fma(r2, db[5], gy);
-          ff_fma(r2, db[2], gz);
-          rf[n * 3 + 0] = r0;
-          rf[n * 3 + 1] = r1;
-          rf[n * 3 + 2] = r2;
-        } else {
-          ff r0{0, 0}, r1{0, 0};
-          ff_fma(r0, db[0], gx);
-          ff_fma(r0, db[3], gy);
-          ff_fma(r1, db[3], gx);
-          ff_fma(r1, db[1], gy);
-          rf[n * 2 + 0] = r0;
-          rf[n * 2 + 1] = r1;
-        }
-      }
+      ff* df = reinterpret_cast<ff*>(sd) + pl * 6;
+      for (int f = 0; f < 6; ++f) df[f] = ff_split(deBar[f]);
     } else {
-      for (int n = 0; n < NN; ++n) {
-        const double gx = Gp[(int64_t)n * stride], gy = Gp[(int64_t)(NN + n) * stride];
-        if constexpr (DIM == 3) {
-          const double gz = Gp[(int64_t)(2 * NN + n) * stride];
-          rq[n * 3 + 0] = deBar[0] * gx + deBar[3] * gy + deBar[4] * gz;
-          rq[n * 3 + 1] = deBar[3] * gx + deBar[1] * gy + deBar[5] * gz;
-          rq[n * 3 + 2] = deBar[4] * gx + deBar[5] * gy + deBar[2] * gz;
-        } else {
-          rq[n * 2 + 0] = deBar[0] * gx + deBar[3] * gy;
-          rq[n * 2 + 1] = deBar[3] * gx + deBar[1] * gy;
-        }
-      }
+      for (int f = 0; f < 6; ++f) sd[pl * 6 + f] = deBar[f];
     }
   }
   __syncthreads();
 
-  // ---- phase C: per element DOF and per element property
+  // ---- phase C: per element DOF (node n, component c): sum over the points of (B^T deBar)_(n,c) =
+  // row c of the symmetric strain adjoint (Voigt, engineering shear) times dN_n/dX; one atomic per
+  // element DOF.  Per element property: plain stores (one thread owns an element's property).
   for (int t = threadIdx.x; t < EPB * NDOF; t += NT) {
-    const int le = t / NDOF, k = t % NDOF;
+    const int le = t / NDOF, k = t % NDOF, n = k / DIM, c = k % DIM;
     const int64_t e = e0 + le;
     if (e >= nEl) continue;
-    double v = 0.0;
+    // row c: 3D (11 12 13 | 12 22 23 | 13 23 33) = Voigt (0 3 4 | 3 1 5 | 4 5 2); 2D (0 3 | 3 1)
+    const int v0 = c == 0 ? 0 : (c == 1 ? 3 : 4), v1 = c == 0 ? 3 : (c == 1 ? 1 : 5), v2 = c == 0 ? 4 : (c == 1 ? 5 : 2);
+    double v;
     if constexpr (FF) {
-      const ff* rf = reinterpret_cast<const ff*>(sr);
+      const ff* df = reinterpret_cast<const ff*>(sd);
       ff acc{0, 0};
-      for (int q = 0; q < NQ; ++q) ff_add(acc, rf[(le * NQ + q) * NDOF + k]);
+      for (int q = 0; q < NQ; ++q) {
+        const int pl = le * NQ + q;
+        ff_fma(acc, df[pl * 6 + v0], ff{sGh[n * NPS + pl], sGl[n * NPS + pl]});
+        ff_fma(acc, df[pl * 6 + v1], ff{sGh[(NN + n) * NPS + pl], sGl[(NN + n) * NPS + pl]});
+        if constexpr (DIM == 3) ff_fma(acc, df[pl * 6 + v2], ff{sGh[(2 * NN + n) * NPS + pl], sGl[(2 * NN + n) * NPS + pl]});
+      }
       v = ff_to_double(acc);
     } else {
-      for (int q = 0; q < NQ; ++q) v += sr[(le * NQ + q) * NDOF + k];
+      v = 0.0;
+      for (int q = 0; q < NQ; ++q) {
+        const int pl = le * NQ + q;
+        double r = sd[pl * 6 + v0] * sGd[n * NPS + pl] + sd[pl * 6 + v1] * sGd[(NN + n) * NPS + pl];
+        if constexpr (DIM == 3) r += sd[pl * 6 + v2] * sGd[(2 * NN + n) * NPS + pl];
+        v += r;
+      }
     }
-    const int32_t dof = a.nodeDof[a.conn[e * NN + k / DIM]] + k % DIM;
+    const int32_t dof = a.nodeDof[a.conn[e * NN + n]] + c;
     atomicAdd(a.dUbar + dof, v);
   }
   if (a.gProps) {
