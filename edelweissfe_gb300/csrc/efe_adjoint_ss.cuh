@@ -18,9 +18,11 @@
 //
 // Plane stress (2D): the reverse of the reference's local Newton on eps33, iteration by iteration.
 //
-// Tile layout as the forward pass: EPB elements per CTA; phase 0 gathers dU_e and PBar_e, phase A
-// runs one thread per point, phase C reduces the per-point contributions per DOF (one atomic per
-// element DOF) and per property (plain stores: one thread owns an element's property).
+// Tile: EPB elements per CTA.  Phase 0 gathers dU_e and PBar_e, stages the tile's dN/dX rows in
+// shared memory (cp.async) and forms the elements' constants once; phase A runs one thread per
+// point (B dU, B PBar, the reverse update, the point's strain adjoint); phase C forms B^T deBar per
+// element DOF over the points (one atomic per element DOF) and sums the property adjoints (plain
+// stores: one thread owns an element's property).
 #pragma once
 #include "efe_launch.cuh"
 
