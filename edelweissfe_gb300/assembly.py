@@ -359,7 +359,29 @@ class GPUAssembler:
         into dUbar [nDof], stateBarOut ([S, nPts], optional), gProps ([E, nProps], optional) and gX
         ([nNodes, dim], optional) the adjoints of dU, of the state before the increment, of the
         properties and of the nodal coordinates, given the seeds stateBarIn (adjoint of the new
-        state) and Pbar (adjoint of the residual P)."""
+        state) and Pbar (adjoint of the residual P).  Every buffer is checked here (dtype, device,
+        contiguity, exact shape): the kernel writes through them."""
+        d = self.groups[group]._dev
+
+        def need(t, name, shape, required=False):
+            if t is None:
+                if required:
+                    raise ValueError(f"adjointSmallStrain: {name} is required")
+                return
+            if (not isinstance(t, torch.Tensor) or t.dtype != torch.float64 or t.device != self.device
+                    or tuple(t.shape) != tuple(shape) or not t.is_contiguous()):  # fmt: skip
+                raise ValueError(f"adjointSmallStrain: {name} must be a contiguous float64 tensor of shape "
+                                 f"{tuple(shape)} on {self.device}")  # fmt: skip
+
+        S = tuple(d["stateRef"].shape)
+        need(stateBefore, "stateBefore", S, True)
+        need(stateBarIn, "stateBarIn", S)
+        need(stateBarOut, "stateBarOut", S)
+        need(dU, "dU", (self.nDof,), True)
+        need(dUbar, "dUbar", (self.nDof,), True)
+        need(Pbar, "Pbar", (self.nDof,))
+        need(gProps, "gProps", tuple(d["props"].shape))
+        need(gX, "gX", (self.nNodes, self.dim))
 
         def ptr(t):
             return None if t is None else ctypes.c_void_p(t.data_ptr())

@@ -139,6 +139,28 @@ def test_increment_reverse_matches_finite_differences(elType, material, precisio
             assert abs(ad - fd) <= 1e-6 * max(abs(fd), 1e-3 * abs(L0)), (what, k, ad, fd)
 
 
+def test_reverse_pass_refuses_wrong_buffers():
+    """Buffers of the wrong shape, dtype or device are refused on the host, before any launch."""
+    asm, coords, nodeDof, nDof, props = _model("C3D8", "vonmises", 5)
+    dev = asm.device
+    g = asm.groups[0]._dev
+    s0 = g["stateRef"].clone()
+    dU = asm.constructDofVector()
+    ok = dict(dUbar=asm.constructDofVector())
+    bad = {
+        "gX": torch.zeros((asm.nNodes - 1, asm.dim), dtype=torch.float64, device=dev),
+        "gProps": torch.zeros((1, 6), dtype=torch.float64, device=dev),
+        "stateBarOut": torch.zeros_like(s0)[:, :-1],
+        "Pbar": torch.zeros(nDof, dtype=torch.float32, device=dev),
+        "stateBarIn": torch.zeros_like(s0).cpu(),
+    }
+    for name, t in bad.items():
+        with pytest.raises(ValueError, match=name):
+            asm.adjointSmallStrain(0, s0, dU, **ok, **{name: t})
+    with pytest.raises(ValueError, match="dUbar"):
+        asm.adjointSmallStrain(0, s0, dU, asm.constructDofVector()[:-1])
+
+
 def _path_problem(fy0, H, precision="fp64", linsolver="superlu", coords=None):
     from edelweissfe_gb300 import ElementGroup, GPUAssembler, meshes
     from edelweissfe_gb300.adjoint import PathAdjoint
