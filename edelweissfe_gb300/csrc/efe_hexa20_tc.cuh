@@ -150,8 +150,9 @@ __device__ __forceinline__ void h20tc_scatter(const GroupArgs& g, int64_t e, con
 }
 
 // Stage element e into shared memory, in two parts that complete after tc::cp_async_wait_all:
-// h20tc_stage_g (every thread): dN/dX by cp.async; h20tc_stage_small (threads li = 0 .. nth - 1,
-// nth >= NN): the pair slots by cp.async into buffer par, U and the row lengths by plain loads.
+// h20tc_stage_g (every thread): dN/dX, det J w t and the properties by cp.async; h20tc_stage_small
+// (threads li = 0 .. nth - 1, nth >= NN): the pair slots by cp.async into buffer par, U, the row
+// lengths and the node DOFs by plain loads.
 template <bool FF>
 __device__ __forceinline__ void h20tc_stage_g(const GroupArgs& g, int64_t e, unsigned char* smem) {
   using T = H20TC;
