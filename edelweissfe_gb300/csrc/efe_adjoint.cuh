@@ -67,63 +67,116 @@ __global__ void adjoint_tl_kernel(int64_t nEl, const int32_t* __restrict__ conn,
   double D[DIM][NN];
   shape_derivatives<SHAPE>(p, D);
   // nodal coordinates, U and lambda are read where they are used (L1-resident) rather than held
-  // in registers across the whole point: fewer registers, no spills
+  // in registers across the whole point: fewer registers, no spills.  The nodal sums (J, dN/dX, F,
+  // Lambda, and in reverse Gbar and iJbar) run in float-float arithmetic on the FP32 pipe with the
+  // nodal values taken relative to node 0 (sum_a dN_a = 0); the material part stays FP64.
   const int32_t* en = conn + e * NN;
-  // Jacobian table row 2 of Hexa20 carries (zeta - xi) * inv(A)[5] (the reference's _J3D20)
+  const int32_t n0 = en[0];
+  const int32_t dof0 = nodeDof[n0];
+  // Jacobian table row 2 of Hexa20 carries (zeta - xi) * inv(A)[5] (the reference's _J3D20); that
+  // row does not sum to zero over the nodes, so its sum times X_0 is added back in FP64
   const double quirk = (SHAPE == EFE_HEXA20) ? (zeta - xi) : 0.0;
-  double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 1}};
+  ff Dff[DIM][NN];
+  #pragma unroll
   for (int r = 0; r < DIM; ++r)
-    for (int c = 0; c < DIM; ++c) {
-      double s = 0.0;
-      for (int a = 0; a < NN; ++a) {
-        double d = D[r][a];
-        if constexpr (SHAPE == EFE_HEXA20) {
-          if (r == 2) d += quirk * fix.r[a % 20];
-        }
-        s += d * coords[(int64_t)en[a] * DIM + c];
+    #pragma unroll 1
+    for (int a = 0; a < NN; ++a) {
+      double d = D[r][a];
+      if constexpr (SHAPE == EFE_HEXA20) {
+        if (r == 2) d += quirk * fix.r[a % 20];
       }
-      J[r][c] = s;
+      Dff[r][a] = ff_split_bits(d);
     }
+  ff Jff[3][3] = {{{0, 0}, {0, 0}, {0, 0}}, {{0, 0}, {0, 0}, {0, 0}}, {{0, 0}, {0, 0}, {0, 0}}};
+  #pragma unroll 1
+  for (int a = 1; a < NN; ++a)
+    #pragma unroll
+    for (int c = 0; c < DIM; ++c) {
+      const ff xr = ff_split_bits(coords[(int64_t)en[a] * DIM + c] - coords[(int64_t)n0 * DIM + c]);
+      #pragma unroll
+      for (int r = 0; r < DIM; ++r) ff_fma(Jff[r][c], Dff[r][a], xr);
+    }
+  double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 1}};
+  #pragma unroll
+  for (int r = 0; r < DIM; ++r)
+    #pragma unroll
+    for (int c = 0; c < DIM; ++c) J[r][c] = ff_to_double_bits(Jff[r][c]);
+  if constexpr (SHAPE == EFE_HEXA20) {
+    double rs = 0.0;
+    #pragma unroll 1
+    for (int a = 0; a < NN; ++a) rs += fix.r[a % 20];
+    #pragma unroll
+    for (int c = 0; c < DIM; ++c) J[2][c] += quirk * rs * coords[(int64_t)n0 * DIM + c];
+  }
   double detJ, iJ[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 1}};
   if constexpr (DIM == 2) {
     detJ = J[0][0] * J[1][1] - J[0][1] * J[1][0];
-    iJ[0][0] = J[1][1] / detJ;
-    iJ[0][1] = -J[0][1] / detJ;
-    iJ[1][0] = -J[1][0] / detJ;
-    iJ[1][1] = J[0][0] / detJ;
+    const double rd = 1.0 / detJ;
+    iJ[0][0] = J[1][1] * rd;
+    iJ[0][1] = -J[0][1] * rd;
+    iJ[1][0] = -J[1][0] * rd;
+    iJ[1][1] = J[0][0] * rd;
   } else {
     detJ = det3(J);
     inv3(J, detJ, iJ);
   }
-  double G[DIM][NN];
-  for (int c = 0; c < DIM; ++c)
-    for (int a = 0; a < NN; ++a) {
-      double s = 0.0;
-      for (int r = 0; r < DIM; ++r) s += iJ[c][r] * D[r][a];
-      G[c][a] = s;
-    }
+  // G = J^-1 dN/dxi (the plain table, without the Hexa20 row term: G uses the reference's
+  // shape-function derivatives)
+  ff G[DIM][NN];
+  {
+    ff iJf[DIM][DIM];
+    #pragma unroll
+    for (int c = 0; c < DIM; ++c)
+      #pragma unroll
+      for (int r = 0; r < DIM; ++r) iJf[c][r] = ff_split_bits(iJ[c][r]);
+    #pragma unroll
+    for (int c = 0; c < DIM; ++c)
+      #pragma unroll 1
+      for (int a = 0; a < NN; ++a) {
+        ff g{0, 0};
+        #pragma unroll
+        for (int r = 0; r < DIM; ++r) ff_fma(g, iJf[c][r], ff_split_bits(D[r][a]));
+        G[c][a] = g;
+      }
+  }
   const double th = (DIM == 2 && thickness) ? thickness[e] : 1.0;
   const double s = detJ * w * th;
   double F[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
-  for (int i = 0; i < DIM; ++i)
-    for (int j = 0; j < DIM; ++j) {
-      double h = 0.0;
-      for (int a = 0; a < NN; ++a) h += U[nodeDof[en[a]] + i] * G[j][a];
-      F[i][j] += h;
+  double Lam[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  {
+    ff Ff[DIM][DIM], Lf[DIM][DIM];
+    #pragma unroll
+    for (int i = 0; i < DIM; ++i)
+      #pragma unroll
+      for (int j = 0; j < DIM; ++j) Ff[i][j] = Lf[i][j] = ff{0, 0};
+    #pragma unroll 1
+    for (int a = 1; a < NN; ++a) {
+      const int32_t dof = nodeDof[en[a]];
+      #pragma unroll
+      for (int i = 0; i < DIM; ++i) {
+        const ff ur = ff_split_bits(U[dof + i] - U[dof0 + i]);
+        const ff lr = ff_split_bits(lam[dof + i] - lam[dof0 + i]);
+        #pragma unroll
+        for (int j = 0; j < DIM; ++j) {
+          ff_fma(Ff[i][j], ur, G[j][a]);
+          ff_fma(Lf[i][j], lr, G[j][a]);
+        }
+      }
     }
+    #pragma unroll
+    for (int i = 0; i < DIM; ++i)
+      #pragma unroll
+      for (int j = 0; j < DIM; ++j) {
+        F[i][j] += ff_to_double_bits(Ff[i][j]);
+        Lam[i][j] = ff_to_double_bits(Lf[i][j]);
+      }
+  }
   const double Jf = det3(F);
   double iF[3][3];
   inv3(F, Jf, iF);
   const double mu = props[e * nProps + 0], Kb = props[e * nProps + 1];
   NeoHookeOut o;
   neo_hooke(material, mu, Kb, F, o);
-  double Lam[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-  for (int i = 0; i < DIM; ++i)
-    for (int k = 0; k < DIM; ++k) {
-      double v = 0.0;
-      for (int a = 0; a < NN; ++a) v += lam[nodeDof[en[a]] + i] * G[k][a];
-      Lam[i][k] = v;
-    }
   double M[3][3];
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) M[i][j] = Lam[i][0] * iF[0][j] + Lam[i][1] * iF[1][j] + Lam[i][2] * iF[2][j];
@@ -168,24 +221,45 @@ __global__ void adjoint_tl_kernel(int64_t nEl, const int32_t* __restrict__ conn,
       Lbar[i][j] = -s * (o.tau[i][0] * iF[j][0] + o.tau[i][1] * iF[j][1] + o.tau[i][2] * iF[j][2]);
     }
   const double sbar = -phi;
-  // Gbar[k][a] = sum_i Fbar[i][k] U[a][i] + Lbar[i][k] lambda[a][i]
-  double Gbar[DIM][NN];
-  for (int a = 0; a < NN; ++a) {
-    const int32_t dof = nodeDof[en[a]];
-    for (int k = 0; k < DIM; ++k) {
-      double v = 0.0;
-      for (int i = 0; i < DIM; ++i) v += Fbar[i][k] * U[dof + i] + Lbar[i][k] * lam[dof + i];
-      Gbar[k][a] = v;
-    }
-  }
-  // G = iJ D: iJbar[c][r] = sum_a Gbar[c][a] D[r][a]
+  // Gbar[k][a] = sum_i Fbar[i][k] U[a][i] + Lbar[i][k] lambda[a][i], and G = iJ D:
+  // iJbar[c][r] = sum_a Gbar[c][a] D[r][a] (U and lambda relative to node 0: sum_a D[r][a] = 0)
   double iJbar[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-  for (int c = 0; c < DIM; ++c)
-    for (int r = 0; r < DIM; ++r) {
-      double v = 0.0;
-      for (int a = 0; a < NN; ++a) v += Gbar[c][a] * D[r][a];
-      iJbar[c][r] = v;
+  {
+    ff Fb[DIM][DIM], Lb[DIM][DIM], ib[DIM][DIM];
+    #pragma unroll
+    for (int i = 0; i < DIM; ++i)
+      #pragma unroll
+      for (int k = 0; k < DIM; ++k) {
+        Fb[i][k] = ff_split_bits(Fbar[i][k]);
+        Lb[i][k] = ff_split_bits(Lbar[i][k]);
+        ib[i][k] = ff{0, 0};
+      }
+    #pragma unroll 1
+    for (int a = 1; a < NN; ++a) {
+      const int32_t dof = nodeDof[en[a]];
+      ff ur[DIM], lr[DIM];
+      #pragma unroll
+      for (int i = 0; i < DIM; ++i) {
+        ur[i] = ff_split_bits(U[dof + i] - U[dof0 + i]);
+        lr[i] = ff_split_bits(lam[dof + i] - lam[dof0 + i]);
+      }
+      #pragma unroll
+      for (int k = 0; k < DIM; ++k) {
+        ff gb{0, 0};
+        #pragma unroll
+        for (int i = 0; i < DIM; ++i) {
+          ff_fma(gb, Fb[i][k], ur[i]);
+          ff_fma(gb, Lb[i][k], lr[i]);
+        }
+        #pragma unroll
+        for (int r = 0; r < DIM; ++r) ff_fma(ib[k][r], gb, ff_split_bits(D[r][a]));
+      }
     }
+    #pragma unroll
+    for (int c = 0; c < DIM; ++c)
+      #pragma unroll
+      for (int r = 0; r < DIM; ++r) iJbar[c][r] = ff_to_double_bits(ib[c][r]);
+  }
   // Jbar = -iJ^T iJbar iJ^T + sbar * w * t * detJ * iJ^T, as two 3x3 products (A = iJ^T iJbar first)
   double A[3][3];
   for (int r = 0; r < DIM; ++r)
