@@ -77,9 +77,9 @@ __global__ void adjoint_tl_kernel(int64_t nEl, const int32_t* __restrict__ conn,
   // row does not sum to zero over the nodes, so its sum times X_0 is added back in FP64
   const double quirk = (SHAPE == EFE_HEXA20) ? (zeta - xi) : 0.0;
   ff Dff[DIM][NN];
-  #pragma unroll
+#pragma unroll
   for (int r = 0; r < DIM; ++r)
-    #pragma unroll 1
+#pragma unroll 1
     for (int a = 0; a < NN; ++a) {
       double d = D[r][a];
       if constexpr (SHAPE == EFE_HEXA20) {
@@ -88,24 +88,24 @@ __global__ void adjoint_tl_kernel(int64_t nEl, const int32_t* __restrict__ conn,
       Dff[r][a] = ff_split_bits(d);
     }
   ff Jff[3][3] = {{{0, 0}, {0, 0}, {0, 0}}, {{0, 0}, {0, 0}, {0, 0}}, {{0, 0}, {0, 0}, {0, 0}}};
-  #pragma unroll 1
+#pragma unroll 1
   for (int a = 1; a < NN; ++a)
-    #pragma unroll
+#pragma unroll
     for (int c = 0; c < DIM; ++c) {
       const ff xr = ff_split_bits(coords[(int64_t)en[a] * DIM + c] - coords[(int64_t)n0 * DIM + c]);
-      #pragma unroll
+#pragma unroll
       for (int r = 0; r < DIM; ++r) ff_fma(Jff[r][c], Dff[r][a], xr);
     }
   double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 1}};
-  #pragma unroll
+#pragma unroll
   for (int r = 0; r < DIM; ++r)
-    #pragma unroll
+#pragma unroll
     for (int c = 0; c < DIM; ++c) J[r][c] = ff_to_double_bits(Jff[r][c]);
   if constexpr (SHAPE == EFE_HEXA20) {
     double rs = 0.0;
-    #pragma unroll 1
+#pragma unroll 1
     for (int a = 0; a < NN; ++a) rs += fix.r[a % 20];
-    #pragma unroll
+#pragma unroll
     for (int c = 0; c < DIM; ++c) J[2][c] += quirk * rs * coords[(int64_t)n0 * DIM + c];
   }
   double detJ, iJ[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 1}};
@@ -125,16 +125,16 @@ __global__ void adjoint_tl_kernel(int64_t nEl, const int32_t* __restrict__ conn,
   ff G[DIM][NN];
   {
     ff iJf[DIM][DIM];
-    #pragma unroll
+#pragma unroll
     for (int c = 0; c < DIM; ++c)
-      #pragma unroll
+#pragma unroll
       for (int r = 0; r < DIM; ++r) iJf[c][r] = ff_split_bits(iJ[c][r]);
-    #pragma unroll
+#pragma unroll
     for (int c = 0; c < DIM; ++c)
-      #pragma unroll 1
+#pragma unroll 1
       for (int a = 0; a < NN; ++a) {
         ff g{0, 0};
-        #pragma unroll
+#pragma unroll
         for (int r = 0; r < DIM; ++r) ff_fma(g, iJf[c][r], ff_split_bits(D[r][a]));
         G[c][a] = g;
       }
@@ -145,27 +145,27 @@ __global__ void adjoint_tl_kernel(int64_t nEl, const int32_t* __restrict__ conn,
   double Lam[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
   {
     ff Ff[DIM][DIM], Lf[DIM][DIM];
-    #pragma unroll
+#pragma unroll
     for (int i = 0; i < DIM; ++i)
-      #pragma unroll
+#pragma unroll
       for (int j = 0; j < DIM; ++j) Ff[i][j] = Lf[i][j] = ff{0, 0};
-    #pragma unroll 1
+#pragma unroll 1
     for (int a = 1; a < NN; ++a) {
       const int32_t dof = nodeDof[en[a]];
-      #pragma unroll
+#pragma unroll
       for (int i = 0; i < DIM; ++i) {
         const ff ur = ff_split_bits(U[dof + i] - U[dof0 + i]);
         const ff lr = ff_split_bits(lam[dof + i] - lam[dof0 + i]);
-        #pragma unroll
+#pragma unroll
         for (int j = 0; j < DIM; ++j) {
           ff_fma(Ff[i][j], ur, G[j][a]);
           ff_fma(Lf[i][j], lr, G[j][a]);
         }
       }
     }
-    #pragma unroll
+#pragma unroll
     for (int i = 0; i < DIM; ++i)
-      #pragma unroll
+#pragma unroll
       for (int j = 0; j < DIM; ++j) {
         F[i][j] += ff_to_double_bits(Ff[i][j]);
         Lam[i][j] = ff_to_double_bits(Lf[i][j]);
@@ -226,38 +226,38 @@ __global__ void adjoint_tl_kernel(int64_t nEl, const int32_t* __restrict__ conn,
   double iJbar[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
   {
     ff Fb[DIM][DIM], Lb[DIM][DIM], ib[DIM][DIM];
-    #pragma unroll
+#pragma unroll
     for (int i = 0; i < DIM; ++i)
-      #pragma unroll
+#pragma unroll
       for (int k = 0; k < DIM; ++k) {
         Fb[i][k] = ff_split_bits(Fbar[i][k]);
         Lb[i][k] = ff_split_bits(Lbar[i][k]);
         ib[i][k] = ff{0, 0};
       }
-    #pragma unroll 1
+#pragma unroll 1
     for (int a = 1; a < NN; ++a) {
       const int32_t dof = nodeDof[en[a]];
       ff ur[DIM], lr[DIM];
-      #pragma unroll
+#pragma unroll
       for (int i = 0; i < DIM; ++i) {
         ur[i] = ff_split_bits(U[dof + i] - U[dof0 + i]);
         lr[i] = ff_split_bits(lam[dof + i] - lam[dof0 + i]);
       }
-      #pragma unroll
+#pragma unroll
       for (int k = 0; k < DIM; ++k) {
         ff gb{0, 0};
-        #pragma unroll
+#pragma unroll
         for (int i = 0; i < DIM; ++i) {
           ff_fma(gb, Fb[i][k], ur[i]);
           ff_fma(gb, Lb[i][k], lr[i]);
         }
-        #pragma unroll
+#pragma unroll
         for (int r = 0; r < DIM; ++r) ff_fma(ib[k][r], gb, ff_split_bits(D[r][a]));
       }
     }
-    #pragma unroll
+#pragma unroll
     for (int c = 0; c < DIM; ++c)
-      #pragma unroll
+#pragma unroll
       for (int r = 0; r < DIM; ++r) iJbar[c][r] = ff_to_double_bits(ib[c][r]);
   }
   // Jbar = -iJ^T iJbar iJ^T + sbar * w * t * detJ * iJ^T, as two 3x3 products (A = iJ^T iJbar first)
